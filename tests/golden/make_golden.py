@@ -1,0 +1,152 @@
+"""Regenerate the golden fixtures in this folder from the reference's regtests.
+
+Run in a container that holds the reference tree:
+
+    python tests/golden/make_golden.py [/path/to/plumed2]
+
+It only READS the reference's regtest inputs and expected outputs (the
+``*.reference`` files) and stores them, reshaped, as JSON next to this script,
+so that the tests run where the reference tree is absent.  Sources:
+
+* regtest/basic/rt20-switch-*           two-atom COORDINATION over
+  regtest/trajectories/switchtraj.xyz: COLVAR.reference, deriv.reference
+* regtest/basic/rt-make-switch          out_*.reference (value, derivative
+  at 10 points per switch type, stretched and not)
+* regtest/basic/rt42, rt42c             108-atom COORDINATION in a triclinic
+  box: check_{c,e,g}.reference, colvar.reference, ff.reference
+  (forces and virial of a RESTRAINT with SLOPE=1 on c+d)
+* regtest/tools/rt-Neigbourlist         unitTest.reference / testNoNL.reference
+  (exact neighbour sets on a simple-cubic lattice)
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_xyz(path):
+    frames, boxes = [], []
+    with open(path) as f:
+        lines = f.read().split("\n")
+    i = 0
+    while i < len(lines) and lines[i].strip():
+        n = int(lines[i].split()[0])
+        box = [float(x) for x in lines[i + 1].split()]
+        pos = [[float(x) for x in lines[i + 2 + k].split()[1:4]] for k in range(n)]
+        frames.append(pos)
+        boxes.append(box)
+        i += n + 2
+    return frames, boxes
+
+
+def read_table(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            if line.strip():
+                rows.append([float(x) for x in line.split()])
+    return rows
+
+
+def switch_defs(plumed_dat):
+    out = {}
+    for line in open(plumed_dat):
+        m = re.match(r"\s*(\w+):\s*COORDINATION\s+GROUPA=1\s+GROUPB=2\s+SWITCH=\{([^}]*)\}(.*)", line)
+        if m and "NUMERICAL_DERIVATIVES" not in m.group(3):
+            out[m.group(1)] = " ".join(m.group(2).split())
+    return out
+
+
+def main(ref):
+    reg = os.path.join(ref, "regtest")
+    # --- rt20-switch-* -----------------------------------------------------
+    traj, boxes = read_xyz(os.path.join(reg, "trajectories", "switchtraj.xyz"))
+    cases = {}
+    for name in sorted(os.listdir(os.path.join(reg, "basic"))):
+        if not name.startswith("rt20-switch-") or name in ("rt20-switch-lepton",):
+            continue
+        d = os.path.join(reg, "basic", name)
+        defs = switch_defs(os.path.join(d, "plumed.dat"))
+        if set(defs) != {"c", "cs"}:
+            continue
+        cases[name] = {"c": defs["c"], "cs": defs["cs"],
+                       "colvar": read_table(os.path.join(d, "COLVAR.reference")),
+                       "deriv": read_table(os.path.join(d, "deriv.reference"))}
+    json.dump({"source": "regtest/basic/rt20-switch-*, regtest/trajectories/switchtraj.xyz",
+               "traj": traj, "box": boxes, "cases": cases},
+              open(os.path.join(HERE, "rt20_switch.json"), "w"))
+
+    # --- rt-make-switch ----------------------------------------------------
+    src = open(os.path.join(reg, "basic", "rt-make-switch", "main.cpp")).read()
+    triples = re.findall(r'"([^"]+)",\s*(?://[^\n]*\n\s*)?"[^"]+",\s*"([^"]+)"', src)
+    table = {}
+    for definition, name in triples:
+        for stretch in (True, False):
+            fn = "out_%s%s.reference" % (name, "" if stretch else "_nostretch")
+            p = os.path.join(reg, "basic", "rt-make-switch", fn)
+            if not os.path.exists(p):
+                continue
+            rows = []
+            for line in open(p):
+                if ":" not in line or line.startswith("point"):
+                    continue
+                a, b = line.split(":")
+                v = b.split()
+                rows.append([float(a), float(v[0]), float(v[1])])
+            table[fn] = {"definition": definition + ("" if stretch else " NOSTRETCH"), "rows": rows}
+    json.dump({"source": "regtest/basic/rt-make-switch/out_*.reference (value, deriv at 6 decimals)",
+               "cases": table}, open(os.path.join(HERE, "rt_make_switch.json"), "w"))
+
+    # --- rt42 / rt42c ------------------------------------------------------
+    d42 = os.path.join(reg, "basic", "rt42")
+    frames, boxes = read_xyz(os.path.join(d42, "trajectory.xyz"))
+    keep = list(range(0, len(frames), 9))
+    ff_lines = open(os.path.join(d42, "ff.reference")).read().split("\n")
+    forces, virials = [], []
+    i = 0
+    while i < len(ff_lines) and ff_lines[i].strip():
+        n = int(ff_lines[i])
+        virials.append([float(x) for x in ff_lines[i + 1].split()])
+        forces.append([[float(x) for x in ff_lines[i + 2 + k].split()[1:4]] for k in range(n)])
+        i += n + 2
+    checks = {}
+    for lab in ("c", "e", "g"):
+        checks[lab] = [r[1] for r in read_table(os.path.join(d42, "check_%s.reference" % lab))]
+    colvar_c1 = [r[1] for r in read_table(os.path.join(reg, "basic", "rt42c", "colvar.reference"))]
+    json.dump({"source": "regtest/basic/rt42 (plumed.dat, trajectory.xyz, check_*.reference, ff.reference) "
+                         "and regtest/basic/rt42c/colvar.reference; every 9th frame",
+               "frames": [frames[k] for k in keep], "box": [boxes[k] for k in keep],
+               "c": [checks["c"][k] for k in keep], "e": [checks["e"][k] for k in keep],
+               "g": [checks["g"][k] for k in keep], "c_single": [colvar_c1[k] for k in keep],
+               "ff_forces": [forces[k] for k in keep], "ff_virial": [virials[k] for k in keep],
+               "inputs": {"c": "R0SYNTAX 6 0 1.0 0.0 twolist", "d": "RATIONAL R_0=1 (CUSTOM 1/(1+x^6))",
+                          "e": "R0SYNTAX 7 0 1.0 0.1 twolist", "f": "RATIONAL R_0=1 D_0=0.1 NN=7 MM=14 (CUSTOM)",
+                          "g": "EXP R_0=1", "c_single": "R0SYNTAX 6 0 1.0 0.0 single",
+                          "forces": "-(dc+dd) - 0.001*(dc - 0.5 dd - 0.5 dfast + de - df + dg - dh)"}},
+              open(os.path.join(HERE, "rt42.json"), "w"))
+
+    # --- rt-Neigbourlist ---------------------------------------------------
+    dnl = os.path.join(reg, "tools", "rt-Neigbourlist")
+    sets = {}
+    for fn in ("unitTest.reference", "testNoNL.reference"):
+        for line in open(os.path.join(dnl, fn)):
+            m = re.match(r"\[(.*), pbc (on|off)\] atom (\d+):(.*)", line)
+            if not m:
+                continue
+            key = "%s|%s" % (m.group(1), m.group(2))
+            sets.setdefault(key, {})[m.group(3)] = [int(x) for x in m.group(4).split()]
+    json.dump({"source": "regtest/tools/rt-Neigbourlist/{unitTest,testNoNL}.reference",
+               "lattice": "sc (AtomDistribution.cpp:205-240): integer sites i,j,k, x fastest; box = ceil(cbrt(N))",
+               "cutoff_factor": 1.999, "sets": sets},
+              open(os.path.join(HERE, "rt_neighbourlist.json"), "w"))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

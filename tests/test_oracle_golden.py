@@ -1,0 +1,140 @@
+"""The C oracle against the reference's own regtest golden outputs.
+
+Every expected number here was printed by the reference (regtest
+``*.reference`` files, extracted by tests/golden/make_golden.py); the
+tolerance is the rounding of the print format that produced it.
+"""
+import numpy as np
+import pytest
+
+from plumed2_gb300.frames import sc_sites
+
+
+def test_rt_make_switch(orc, golden):
+    """regtest/basic/rt-make-switch: value and derivative at 10 points, %.6f."""
+    g = golden("rt_make_switch.json")
+    assert len(g["cases"]) == 24
+    for name, case in g["cases"].items():
+        rows = np.array(case["rows"])
+        f, df = orc.switch_eval(case["definition"], rows[:, 0], squared=False)
+        assert np.all(np.abs(f - rows[:, 1]) <= 5.01e-7), name
+        assert np.all(np.abs(df - rows[:, 2]) <= 5.01e-7), name
+        # calculateSqr agrees with calculate to the printed precision (the
+        # vsq_delta columns of the same file are all +-0.000000)
+        f2, df2 = orc.switch_eval(case["definition"], rows[:, 0] ** 2, squared=True)
+        assert np.all(np.abs(f2 - f) <= 5e-7) and np.all(np.abs(df2 - df) <= 5e-7), name
+
+
+def _two_atom_cv(orc, spec, a, b, box):
+    pos = np.array([a, b], float)
+    return orc.coordination(spec, pos, box, np.array([[0, 1]], np.uint32))
+
+
+def test_rt20_switch(orc, golden):
+    """regtest/basic/rt20-switch-*: COLVAR (%f) and DUMPDERIVATIVES (%8.4f)."""
+    g = golden("rt20_switch.json")
+    assert len(g["cases"]) == 12
+    for name, case in g["cases"].items():
+        colvar = np.array(case["colvar"])
+        deriv = np.array(case["deriv"])
+        for fi, (frame, box) in enumerate(zip(g["traj"], g["box"])):
+            B = np.diag(box) if len(box) == 3 else np.array(box).reshape(3, 3)
+            for col, lab in ((1, "c"), (2, "cs")):
+                s, d, v = _two_atom_cv(orc, case[lab], frame[0], frame[1], B)
+                assert abs(s - colvar[fi, col]) <= 5.01e-7, (name, lab, fi)
+                rows = deriv[deriv[:, 0] == colvar[fi, 0]]
+                got = np.concatenate([d.reshape(-1), v.reshape(-1)])
+                assert np.all(np.abs(got - rows[:, 1 + col]) <= 5.01e-5), (name, lab, fi)
+
+
+def test_rt42_values_forces_virial(orc, golden):
+    """regtest/basic/rt42 (+rt42c): 108 atoms in a triclinic box.
+
+    c, e, g at %8.4f; forces and full virial of RESTRAINT SLOPE=1 on c+d (plus
+    the SLOPE=0.001 restraint on the CUSTOM cross-check combination) at %10.5f.
+    CUSTOM switches are evaluated as the built-in switch with the same formula.
+    """
+    g = golden("rt42.json")
+    for fi in range(len(g["frames"])):
+        pos = np.array(g["frames"][fi])
+        box = np.array(g["box"][fi]).reshape(3, 3)
+        n = len(pos)
+        pos2 = np.concatenate([pos, pos])
+        absi = np.concatenate([np.arange(n), np.arange(n)])
+        pairs = orc.all_pairs(1, n, n)
+
+        def cv(spec):
+            s, d, v = orc.coordination(spec, pos2, box, pairs, abs_index=absi)
+            return s, d[:n] + d[n:], v
+
+        sc, dc, vc = cv("R0SYNTAX 6 0 1.0 0.0")
+        sd, dd, vd = cv("RATIONAL R_0=1")
+        se, de, ve = cv("R0SYNTAX 7 0 1.0 0.1")
+        sf, df, vf = cv("RATIONAL R_0=1 D_0=0.1 NN=7 MM=14")
+        sg, _, _ = cv("EXP R_0=1")
+        s1, _, _ = orc.coordination("R0SYNTAX 6 0 1.0 0.0", pos, box, orc.all_pairs(0, n))
+        assert abs(sc - g["c"][fi]) <= 5.01e-5
+        assert abs(se - g["e"][fi]) <= 5.01e-5
+        assert abs(sg - g["g"][fi]) <= 5.01e-5
+        assert abs(s1 - g["c_single"][fi]) <= 5.01e-5
+        F = -(dc + dd) - 0.001 * (dc - dd + de - df)
+        V = -(vc + vd) - 0.001 * (vc - vd + ve - vf)
+        assert np.abs(F - np.array(g["ff_forces"][fi])).max() <= 5.01e-6
+        assert np.abs(V - np.array(g["ff_virial"][fi]).reshape(3, 3)).max() <= 5.01e-6
+
+
+def _neigh_sets(pairs, nslots):
+    out = [set() for _ in range(nslots)]
+    for a, b in pairs:
+        out[a].add(int(b))
+        out[b].add(int(a))
+    return out
+
+
+@pytest.mark.parametrize("pbc", ["off", "on"])
+def test_rt_neighbourlist(orc, golden, pbc):
+    """regtest/tools/rt-Neigbourlist: exact neighbour sets (sc lattice, cutoff 1.999 spacing)."""
+    g = golden("rt_neighbourlist.json")
+    do_pbc = pbc == "on"
+    # single list, 125 atoms
+    atoms = sc_sites(125)
+    box = np.diag([5.0] * 3)
+    cut = (5.0 / 5) * 1.999
+    pairs = orc.nl_classic(0, 125, 0, atoms, box, do_pbc, cut)
+    sets = _neigh_sets(pairs, 125)
+    exp = g["sets"]["Single list|%s" % pbc]
+    for i in range(125):
+        assert sorted(sets[i]) == exp[str(i)]
+    # two lists / pairs: 124 atoms, A even, B odd
+    atoms = sc_sites(124)
+    A = np.arange(0, 124, 2)[:62]
+    B = np.arange(1, 124, 2)[:62]
+    idx = np.concatenate([A, B])
+    reordered = atoms[idx]
+    for key, mode in (("Two lists", 1), ("List of pairs", 2)):
+        pairs = orc.nl_classic(mode, 62, 62, reordered, box, do_pbc, cut)
+        sets = _neigh_sets(pairs, 124)
+        exp = g["sets"]["%s|%s" % (key, pbc)]
+        for slot in range(124):
+            got = sorted(int(idx[j]) for j in sets[slot])
+            assert got == exp[str(int(idx[slot]))], (key, slot)
+    # no NL: every other atom of 27
+    pairs = orc.all_pairs(0, 27)
+    sets = _neigh_sets(pairs, 27)
+    exp = g["sets"]["NoNL|%s" % pbc]
+    for i in range(27):
+        assert sorted(sets[i]) == exp[str(i)]
+
+
+def test_cell_nl_equals_classic(orc):
+    """The cell-accelerated exact NL returns the classic pair set, sorted."""
+    rng = np.random.default_rng(7)
+    pos = sc_sites(1728) * 0.31 + rng.normal(0, 0.03, (1728, 3))
+    box = np.diag([12 * 0.31] * 3)
+    for mode, n0, n1 in ((0, 1728, 0), (1, 864, 864)):
+        for do_pbc in (True, False):
+            a = orc.nl_classic(mode, n0, n1, pos, box, do_pbc, 0.7)
+            b = orc.nl_classic_cells(mode, n0, n1, pos, box, do_pbc, 0.7)
+            assert len(a) == len(b)
+            a = a[np.lexsort((a[:, 1], a[:, 0]))]
+            assert np.array_equal(a, b)

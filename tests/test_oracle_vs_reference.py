@@ -1,0 +1,94 @@
+"""The C oracle is bit-identical to the reference's own code on the same inputs.
+
+Runs where oracle/_ref (the reference sources compiled by oracle/Makefile)
+exists; skipped elsewhere.  Serial order and -ffp-contract=off on both sides
+make every comparison exact (np.array_equal), not toleranced.
+"""
+import numpy as np
+import pytest
+
+from plumed2_gb300.frames import jittered_lattice
+
+SPECS = [
+    "RATIONAL R_0=0.30 D_0=0.0 NN=6 MM=12 D_MAX=1.0",
+    "RATIONAL R_0=1.3 NN=6 MM=10 D_MAX=2.6",
+    "RATIONAL R_0=1.3 NN=5 MM=11 D_MAX=2.6",
+    "RATIONAL R_0=1.3 NN=5 D_MAX=2.6",
+    "RATIONAL R_0=0.3 NN=8 MM=16 D_MAX=0.9",
+    "RATIONAL R_0=0.3 NN=6 MM=12",
+    "RATIONAL R_0=1.3 NN=6 MM=10 D_MAX=2.6 NOSTRETCH",
+    "EXP R_0=0.8 D_0=0.5 D_MAX=2.6",
+    "GAUSSIAN R_0=1.0 D_0=0.0 D_MAX=2.6",
+    "GAUSSIAN R_0=1.0 D_0=0.3 D_MAX=2.6",
+    "Q R_0=1.0 D_0=0.3 BETA=5.0 LAMBDA=1.0 REF=1.3 D_MAX=2.6",
+    "TANH R_0=1.3 D_MAX=2.6",
+    "SMAP R_0=1.3 A=3 B=2 D_MAX=2.6",
+    "CUBIC D_MAX=2.6 D_0=0.6",
+    "COSINUS R_0=2.6",
+    "R0SYNTAX 6 0 0.3 0.0",
+    "R0SYNTAX 7 0 1.0 0.1",
+    "R0SYNTAX 8 14 0.4 0.05",
+]
+
+
+@pytest.mark.parametrize("spec", SPECS)
+def test_switch_bit_exact(orc, ref, spec):
+    x = np.linspace(0.0, 3.0, 3001)
+    for squared in (True, False):
+        xx = x * x if squared else x
+        f1, d1 = orc.switch_eval(spec, xx, squared)
+        f2, d2 = ref.switch_eval(spec, xx, squared)
+        assert np.array_equal(f1, f2) and np.array_equal(d1, d2)
+
+
+def test_pbc_bit_exact(orc, ref):
+    rng = np.random.default_rng(11)
+    for box in (np.diag([3.0, 3.1, 2.9]),
+                np.array([[3, 0, 0], [0.5, 2.8, 0], [0.3, 0.2, 2.9]], float),
+                np.array([[6, -6, 0], [0, 6, -6], [-6, 6, 6]], float),
+                np.zeros((3, 3))):
+        v1 = rng.uniform(-5, 5, (400, 3))
+        v2 = rng.uniform(-5, 5, (400, 3))
+        d2, _ = ref.pbc_distance(box, v1, v2)
+        assert np.array_equal(orc.pbc_distance(box, v1, v2), d2)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("do_pbc", [True, False])
+def test_neighbour_list_bit_exact(orc, ref, mode, do_pbc):
+    pos = jittered_lattice(1000, 0.30, 0.03, 5)
+    box = np.diag([3.0] * 3)
+    n0, n1 = (1000, 0) if mode == 0 else (500, 500)
+    for cut in (0.45, 0.9, 1.6):
+        a = orc.nl_classic(mode, n0, n1, pos, box, do_pbc, cut)
+        b = ref.nl(mode, n0, n1, pos, box, do_pbc, cut)
+        assert np.array_equal(a, b)
+        if mode != 2:
+            c = orc.nl_linkcells(mode, n0, n1, pos, box, do_pbc, cut)
+            d = ref.nl(mode, n0, n1, pos, box, do_pbc, cut, cells=True)
+            assert np.array_equal(c, d)
+
+
+@pytest.mark.parametrize("spec", ["RATIONAL R_0=0.30 D_0=0.0 NN=6 MM=12 D_MAX=1.0", "R0SYNTAX 6 0 0.3 0.0",
+                                  "RATIONAL R_0=0.3 NN=5 MM=11 D_MAX=1.0", "GAUSSIAN R_0=0.2 D_0=0.1 D_MAX=0.9"])
+def test_coordination_bit_exact(orc, ref, spec):
+    pos = jittered_lattice(1000, 0.30, 0.03, 6)
+    box = np.diag([3.0] * 3)
+    for mode, n0, n1, cut in ((0, 1000, 0, 0.0), (0, 1000, 0, 0.8), (1, 400, 600, 0.0), (1, 400, 600, 0.9),
+                              (2, 500, 500, 0.0)):
+        s2, d2, v2 = ref.coordination(spec, mode, n0, n1, pos, box, nl_cutoff=cut)
+        pairs = orc.all_pairs(mode, n0, n1) if cut == 0 else orc.nl_classic(mode, n0, n1, pos, box, True, cut)
+        s1, d1, v1 = orc.coordination(spec, pos, box, pairs)
+        assert s1 == s2 and np.array_equal(d1, d2) and np.array_equal(v1, v2)
+
+
+def test_coordination_duplicates_and_self_skip(orc, ref):
+    """GROUPA with repeated atoms (cf. regtest/basic/rt-fix-229): pairs of equal absolute index are skipped."""
+    pos0 = jittered_lattice(64, 0.3, 0.03, 8)
+    sel = np.array([0, 1, 1, 2, 5, 5, 5, 9, 30, 31, 63, 0])
+    pos = pos0[sel]
+    box = np.diag([1.2] * 3)
+    spec = "R0SYNTAX 6 0 0.3 0.0"
+    s2, d2, v2 = ref.coordination(spec, 0, len(sel), 0, pos, box, abs_index=sel.astype(np.int64))
+    s1, d1, v1 = orc.coordination(spec, pos, box, orc.all_pairs(0, len(sel)), abs_index=sel)
+    assert s1 == s2 and np.array_equal(d1, d2) and np.array_equal(v1, v2)
