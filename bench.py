@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Throughput of the COORDINATION hot path on one GB300 (or N, one process each).
+
+Workload (the 262,144-atom configuration the headline target is quoted on):
+  262,144 atoms on a jittered 64^3 simple-cubic lattice (sigma 0.03 nm) filling
+  a periodic 19.87 nm cube; GROUPA = all atoms (single list);
+  SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6}; NLIST NL_CUTOFF=0.8
+  NL_STRIDE=10; 16 independent walkers (separately seeded) per GPU, batched in
+  one launch per kernel; mixed precision (FP32 pair math, FP64 compensated
+  sums).  A step is CV + derivatives + virial for all walkers, followed by the
+  backward pass of a 500-hill metadynamics-style bias when it is available.
+  Neighbour lists are rebuilt on steps that are multiples of NL_STRIDE, so
+  rebuilds are amortised exactly as in an MD run.
+
+  value  = pair-evaluations (neighbour-list entries processed, summed over
+           walkers) per second, inputs resident in HBM, CUDA events around the
+           timed steps on the library's stream.  Working set per step (FP64
+           positions 100 MB + neighbour lists ~0.7 GB) exceeds the 129 MB L2.
+  e2e    = the same metric through the plugin-facing C ABI call
+           (coord_forward, one context per walker, host buffers, H2D of
+           positions and D2H of s/derivatives/virial inside the timed region).
+
+  --impl reference : the reference's algorithm on the host cores (oracle/_ref
+  where it was built from the reference sources, else the C restatement in
+  oracle/), OpenMP over all threads, one walker per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CV+force µs/step & pair-evals/s, mixed+batched vs FP64 GPU at ≤1e-6 rel err"
+N_ATOMS = 262144
+BOX = 19.87
+SPEC = "RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6"
+LINE = "GROUPA=1-%d SWITCH={%s} NLIST NL_CUTOFF=0.8 NL_STRIDE=10"
+ALG_FLOPS_PER_PAIR = 57  # FMA = 2: delta 3, min-image 9, r^2 5, switch+dfunc 12, chain 4, dd 3, derivs 6, virial 18, s 1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--walkers", type=int, default=16)
+    ap.add_argument("--atoms", type=int, default=N_ATOMS)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="small sizes (for profiling captures)")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (median SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def make_walkers(n_walkers, n_atoms, first):
+    from plumed2_gb300.frames import sc_sites
+    sites = sc_sites(n_atoms)
+    m = round(n_atoms ** (1 / 3))
+    a = BOX / m
+    out = np.empty((n_walkers, n_atoms, 3))
+    for w in range(n_walkers):
+        rng = np.random.default_rng([2028, first + w])
+        out[w] = sites * a + rng.normal(0.0, 0.03, size=(n_atoms, 3))
+    return out, np.diag([BOX * (n_atoms / N_ATOMS) ** (1 / 3)] * 3)
+
+
+def cpu_baseline(frames, box, budget_s=10.0, use_reference=False):
+    """The reference algorithm on this host's cores: classic neighbour list once
+    (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop."""
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle()
+    pos = frames[0]
+    n = len(pos)
+    t0 = time.perf_counter()
+    pairs = orc.nl_classic_cells(0, n, 0, pos, box, True, 0.8)
+    t_build = time.perf_counter() - t0
+    kind = "port"
+    nthreads = orc.max_threads()
+    if use_reference:
+        try:
+            ref = oracle.Reference()
+            kind = "reference"
+            nthreads = ref.max_threads()
+        except Exception:
+            ref = None
+    reps, t_loop = 0, 0.0
+    while t_loop < budget_s or reps == 0:
+        t0 = time.perf_counter()
+        orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
+        t_loop += time.perf_counter() - t0
+        reps += 1
+    per_step = t_loop / reps + t_build / 10.0
+    return {"value": len(pairs) / per_step, "unit": "pair-evals/s", "cores": nthreads, "kind": kind,
+            "sample": "1 walker of %d atoms: classic NL build once (%.2f s, serial, amortised /10) + %d pair "
+                      "loops over %d NL pairs (OpenMP, %d threads)" % (n, t_build, reps, len(pairs), nthreads),
+            "ms_per_step": per_step * 1e3}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle()
+    ref = None
+    kind = "port"
+    if oracle.Reference.available():
+        try:
+            ref = oracle.Reference()
+            kind = "reference"
+        except Exception:
+            ref = None
+    n = args.atoms if not args.quick else 32768
+    frames, box = make_walkers(1, n, 0)
+    pos = frames[0]
+    nthreads = orc.max_threads()
+    pairs = None
+    total_pairs, total_t, step = 0, 0.0, 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        if pairs is None or step % 10 == 0:
+            pairs = orc.nl_classic_cells(0, n, 0, pos, box, True, 0.8)
+        if ref is not None and n <= 60000:
+            ref.coordination(SPEC, 0, n, 0, pos, box, nl_cutoff=0.8, nthreads=nthreads)
+        else:
+            orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            total_pairs += len(pairs)
+            total_t += dt
+        step += 1
+    v = total_pairs / total_t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pair-evals/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "1 walker per step of %d atoms, single list, %s, NLIST NL_CUTOFF=0.8 "
+                                   "NL_STRIDE=10 (rebuild every 10th step)" % (n, SPEC)},
+            "cpu_baseline": {"value": v, "unit": "pair-evals/s", "cores": nthreads, "kind": kind,
+                             "sample": "%d walker-steps of %d atoms, %d NL pairs each" % (args.steps, n, len(pairs))},
+            "e2e": {"value": v, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from plumed2_gb300 import _lib
+    from plumed2_gb300.action import Coordination
+
+    W = args.walkers
+    n = args.atoms if not args.quick else 32768
+    frames, box = make_walkers(W, n, rank * W)
+    boxes = np.stack([box] * W)
+    line = LINE % (n, SPEC)
+    c = Coordination(line, precision="mixed", device=local)
+    tpos = torch.from_numpy(frames).to(dev)
+    s = torch.zeros(W, dtype=torch.float64, device=dev)
+    der = torch.zeros(W, n, 3, dtype=torch.float64, device=dev)
+    vir = torch.zeros(W, 9, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    step = 0
+
+    def one_step(ctx):
+        nonlocal step
+        ctx.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step)
+        step += 1
+
+    for _ in range(args.warmup):
+        one_step(c)
+    torch.cuda.synchronize()
+    pairs_per_step = sum(c.nl_size(w) for w in range(W))
+
+    # timed region (events on the library's stream through a default-stream sync)
+    clocks = Clocks(local)
+    c.set_timing(True)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step(c)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = _lib.launch_count() - l0
+    kern_ms, kern_n = c.kernel_ms()
+    c.set_timing(False)
+    if ws > 1:
+        tt = torch.tensor([t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = tt.item()
+    ms_step = t / args.steps * 1e3
+    value = pairs_per_step * ws * args.steps / t
+
+    # the plain FP64 GPU path on the same workload (the drop-in, for the 5x target)
+    c64 = Coordination(line, precision="fp64", device=local)
+    st64 = 0
+    c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1, 1 + args.fp64_steps):
+        c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=k)
+    torch.cuda.synchronize()
+    t64 = (time.perf_counter() - t0) / max(args.fp64_steps, 1)
+    c64.close()
+    del st64
+
+    line_out = None
+    if rank == 0:
+        peaks = _lib.measure_peaks(local)
+        mp = {}
+        try:
+            mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        hbm_peak = mp.get("hbm_gbs") or peaks["hbm_gbs"]
+        # roofline of the pair kernel: algorithmic FLOPs and bytes per launch
+        pairs_launch = pairs_per_step
+        flops = pairs_launch * ALG_FLOPS_PER_PAIR
+        bytes_alg = 4 * pairs_launch + 16 * W * n + 16 * W * n  # ELL entry + fixed-point positions + FP32 deriv accum
+        achieved_tf = flops / (kern_ms * 1e-3) / 1e12 if kern_ms > 0 else None
+        achieved_gbs = bytes_alg / (kern_ms * 1e-3) / 1e9 if kern_ms > 0 else None
+        frac_fp32 = achieved_tf / peaks["fp32_tflops"] if achieved_tf else None
+        frac_hbm = achieved_gbs / hbm_peak if achieved_gbs else None
+        if frac_fp32 is not None and frac_hbm is not None and frac_hbm > frac_fp32:
+            roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": frac_hbm,
+                    "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+        else:
+            roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                    "frac": frac_fp32, "traffic": None,
+                    "peak_source": "coord_measure_peaks FP32 FMA microbenchmark (measured live)"}
+        roof.update({"kernel": "k_eval_nl32 (mixed NL pair kernel)", "kernel_ms": kern_ms, "launches": kern_n,
+                     "alg_flops_per_launch": flops, "alg_bytes_per_launch": bytes_alg,
+                     "other_roof_frac": frac_hbm if roof["bound"] == "fp32" else frac_fp32})
+
+        # e2e through the plugin-facing host call, one context per walker
+        e2e_v, h2d, d2h = None, 0, 0
+        if args.e2e_steps > 0:
+            ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
+            host_pos = [np.ascontiguousarray(frames[w]) for w in range(W)]
+            for w in range(W):
+                ctxs[w].calculate(host_pos[w], box, 0)
+            t0 = time.perf_counter()
+            npairs = 0
+            for k in range(1, 1 + args.e2e_steps):
+                for w in range(W):
+                    sv, dv, vv = ctxs[w].calculate(host_pos[w], box, k)
+            te = time.perf_counter() - t0
+            npairs = sum(ctxs[w].nl_size() for w in range(W)) * args.e2e_steps
+            e2e_v = npairs / te
+            h2d = W * n * 3 * 8
+            d2h = W * (n * 3 * 8 + 10 * 8)
+            for x in ctxs:
+                x.close()
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(frames, box, budget_s=8.0)
+        line_out = {
+            "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "262144-atom jittered sc lattice, 19.87 nm periodic box, single list, %s, NLIST "
+                                   "NL_CUTOFF=0.8 NL_STRIDE=10, %d walkers per GPU batched per launch, mixed "
+                                   "precision (FP32 pairs, FP64 compensated sums)" % (SPEC, W),
+                       "atoms": n, "walkers_per_gpu": W, "pairs_per_step_per_gpu": pairs_per_step,
+                       "cv_force_us_per_step": ms_step * 1e3, "us_per_walker_step": ms_step * 1e3 / W,
+                       "fp64_gpu_ms_per_step": t64 * 1e3,
+                       "mixed_over_fp64_speedup": (t64 * 1e3) / ms_step,
+                       "backward": False, "l2": "working set (0.8 GB) larger than the 129 MB L2",
+                       "parallelism": "walkers sharded across GPUs, no collective"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line_out), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,187 @@
+/*
+ * coordgpu.h -- C ABI of libcoordgpu.so, a GB300 (sm_103a) implementation of
+ * PLUMED's COORDINATION collective variable.
+ *
+ * The library replaces, behind PLUMED's own action interface, the hot path of
+ *   src/colvar/CoordinationBase.cpp:142-231   CoordinationBase::calculate
+ *   src/colvar/Coordination.cpp:103-163       Coordination (keywords, pairing)
+ *   src/tools/SwitchingFunction.cpp           SwitchingFunction::calculateSqr
+ *   src/tools/NeighborList.cpp:168-315        NeighborList::update
+ *   src/tools/Pbc.cpp:362-415, Tools.h:547    minimum-image distances
+ * A PLUMED plugin (plumed2_gb300/plugin/CoordinationGPU.cpp) registers the
+ * COORDINATION directive and forwards each calculate() to coord_forward().
+ *
+ * Conventions
+ *  - coord_create() validates keywords and sets up the switching function
+ *    without touching CUDA; the device is initialised by coord_set_groups().
+ *  - Every entry point returns an int status (COORD_OK == 0).  A nonzero status
+ *    leaves a message retrievable with coord_last_error(ctx).
+ *  - Positions are AoS doubles, 3 per slot; slots are GROUPA followed by
+ *    GROUPB, in the order given to coord_set_groups (the order in which
+ *    CoordinationBase requests its atoms, NeighborList.cpp:62-67).
+ *  - Boxes are 3x3 row-major doubles (row i = lattice vector i), as passed to
+ *    Pbc::setBox; an all-zero box means no periodicity.
+ *  - Derivatives are ds/dx per slot (AoS, 3 per slot); the virial is the 3x3
+ *    box derivative -sum dfunc * d (x) d, in the layout of
+ *    Colvar::setBoxDerivatives (Colvar.h:74-113).
+ *  - No function allocates or frees caller memory; the context owns its
+ *    device buffers.  Host-pointer functions copy in/out through pinned
+ *    staging on the context's stream; *_device functions take device pointers
+ *    and a cudaStream_t passed as void* (NULL = the context's own stream).
+ *  - A context is not thread-safe; use one per action instance (the
+ *    reference's contract: one Colvar per action, CoordinationBase.h:33).
+ */
+#ifndef COORDGPU_H
+#define COORDGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define COORD_OK 0
+#define COORD_ERR_ARG 1         /* invalid argument / keyword error          */
+#define COORD_ERR_CUDA 2        /* CUDA runtime error                        */
+#define COORD_ERR_BOX 3         /* box not usable (see Pbc::setBox)          */
+#define COORD_ERR_UNSUPPORTED 4 /* valid input this build does not handle    */
+#define COORD_ERR_NOMEM 5       /* device allocation failed                  */
+#define COORD_ERR_TIMEOUT 6     /* a bounded device-side wait expired        */
+#define COORD_ERR_STATE 7       /* call out of order (e.g. no groups set)    */
+
+/* ---- parameters: the COORDINATION keyword surface ------------------------ */
+/* Mirrors CoordinationBase::registerKeywords (CoordinationBase.cpp:30-40)
+ * and Coordination::registerKeywords (Coordination.cpp:115-126). */
+#define COORD_NL_NONE 0     /* no NLIST: every pair, every step             */
+#define COORD_NL_CLASSIC 1  /* NLIST: pairs with |d|<=NL_CUTOFF, rebuilt every NL_STRIDE */
+#define COORD_NL_CELLS 2    /* NLISTCELLS: pairs in neighbouring link cells  */
+
+#define COORD_PREC_FP64 0   /* FP64 throughout: the drop-in path            */
+#define COORD_PREC_MIXED 1  /* FP32 pair math, compensated FP64 sums        */
+
+typedef struct {
+  const char *switch_def; /* SWITCH={...} body, e.g. "RATIONAL R_0=0.3 D_MAX=1.0";
+                             NULL/"" selects the R_0/NN/MM/D_0 keywords below */
+  double r0;              /* R_0 (required and >0 when switch_def is empty)  */
+  double d0;              /* D_0 (default 0.0)                               */
+  int nn;                 /* NN  (default 6)                                 */
+  int mm;                 /* MM  (default 0 -> 2*NN)                         */
+  int nopbc;              /* NOPBC flag                                      */
+  int pair;               /* PAIR flag                                       */
+  int nlist;              /* COORD_NL_*                                      */
+  double nl_cutoff;       /* NL_CUTOFF (>0 when nlist != NONE)               */
+  int nl_stride;          /* NL_STRIDE (>0 when nlist != NONE)               */
+  int serial;             /* SERIAL flag (accepted; no effect on the GPU)    */
+  int precision;          /* COORD_PREC_*                                    */
+  int device;             /* CUDA device ordinal                             */
+} coord_params;
+
+typedef struct coord_ctx coord_ctx;
+
+/* Fill p with the reference defaults (NN=6, MM=0, D_0=0, FP64, device 0). */
+void coord_params_default(coord_params *p);
+
+/* Create a context: parses SWITCH / R_0,NN,MM,D_0 exactly as
+ * Coordination::Coordination (Coordination.cpp:128-157) and checks the
+ * NLIST/NL_CUTOFF/NL_STRIDE/PAIR rules of CoordinationBase.cpp:66-84. */
+int coord_create(const coord_params *p, coord_ctx **out);
+int coord_destroy(coord_ctx *ctx);
+const char *coord_last_error(const coord_ctx *ctx);
+const char *coord_status_string(int status);
+
+/* Groups as absolute atom indices (AtomNumber::index()).  n_b==0 selects the
+ * single-list N(N-1)/2 form; PAIR pairs a[i] with b[i].  Pairs whose two
+ * absolute indices are equal are skipped (CoordinationBase.cpp:183). */
+int coord_set_groups(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, const int64_t *group_b, int64_t n_b);
+
+/* Number of slots (n_a + n_b). */
+int coord_get_nslots(const coord_ctx *ctx, int64_t *nslots);
+
+/* The context's switching function evaluated on the host:
+ * SwitchingFunction::calculateSqr (squared != 0, x = r^2) or ::calculate
+ * (x = r), SwitchingFunction.cpp:1163-1175.  f and df receive n values. */
+int coord_switch_eval(const coord_ctx *ctx, int n, const double *x, int squared, double *f, double *df);
+/* Its constants d0, dmax, dmax^2, 1/r0, 1/r0^2, stretch, shift
+ * (switchContainers::Data, SwitchingFunction.h:57-95). */
+int coord_switch_params(const coord_ctx *ctx, double out[7]);
+
+/* ---- forward: CV, derivatives, virial ------------------------------------ */
+#define COORD_FLAG_REBUILD 1u   /* force a neighbour-list rebuild this step   */
+#define COORD_FLAG_NO_DERIV 2u  /* compute s only (no derivatives, no virial) */
+#define COORD_FLAG_DR0 4u       /* also return ds/dR_0 and ds/dD_0            */
+
+/* One step of CoordinationBase::prepare()+calculate() for one frame, host
+ * buffers.  The neighbour list is rebuilt when the list is new, when
+ * step % NL_STRIDE == 0, or on COORD_FLAG_REBUILD (NeighborList::prepare,
+ * NeighborList.cpp:433-456).  pos: nslots*3; deriv: nslots*3 (may be NULL
+ * with COORD_FLAG_NO_DERIV); virial: 9 (may be NULL). */
+int coord_forward(coord_ctx *ctx, const double *pos, const double box[9], int64_t step, unsigned flags, double *s,
+                  double *deriv, double *virial);
+
+/* Batched form for walkers / trajectory frames sharing one action definition:
+ * n_frames independent frames, each with its own neighbour list.  Device
+ * pointers: pos [n_frames][nslots][3], s [n_frames], deriv
+ * [n_frames][nslots][3], virial [n_frames][9], dparam [n_frames][2]
+ * (ds/dR_0, ds/dD_0; only with COORD_FLAG_DR0, else may be NULL).  boxes are
+ * HOST [n_frames][9].  stream: cudaStream_t or NULL. */
+int coord_forward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, int64_t step,
+                         unsigned flags, double *s, double *deriv, double *virial, double *dparam, void *stream);
+
+/* ---- backward: gradients of an upstream scalar ---------------------------- */
+/* Given g[f] = dV/ds for each frame (device), returns on the device
+ * grad_pos [n_frames][nslots][3] = g * ds/dx, grad_box [n_frames][9] =
+ * g * ds/dh (h = box, scaled coordinates held fixed; the box-derivative
+ * convention of ActionAtomistic.cpp:221-265), grad_param [n_frames][2] =
+ * g * (ds/dR_0, ds/dD_0).  Reuses the neighbour list of the last forward;
+ * any output pointer may be NULL. */
+int coord_backward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, const double *g,
+                          double *grad_pos, double *grad_box, double *grad_param, void *stream);
+
+/* ---- neighbour list introspection ------------------------------------------ */
+/* nl->size() of the last build for frame f (pairs processed per step,
+ * CoordinationBase.cpp:163), including pairs skipped as self pairs. */
+int coord_nl_size(coord_ctx *ctx, int frame, int64_t *n);
+/* The pair set of the last build for frame f as (first, second) slot pairs
+ * in the reference's orientation (first<second for a single list, first in
+ * GROUPA otherwise), sorted; writes min(n, cap) pairs, returns n. */
+int coord_get_pairs(coord_ctx *ctx, int frame, uint32_t *pairs, int64_t cap, int64_t *n);
+
+/* ---- many actions in one launch ------------------------------------------- */
+/* A batch of contexts whose groups index one shared system of n_atoms atoms
+ * (absolute indices = rows of pos).  One forward evaluates every action on
+ * every frame in a single persistent launch.  Device pointers: pos
+ * [n_frames][n_atoms][3]; s [n_frames][n_actions]; deriv: for each frame, for
+ * each action, nslots_k*3 values, concatenated (offsets from
+ * coord_multi_deriv_offset); virial [n_frames][n_actions][9]. */
+typedef struct coord_multi coord_multi;
+int coord_multi_create(coord_ctx *const *ctxs, int n_actions, int64_t n_atoms, coord_multi **out);
+int coord_multi_destroy(coord_multi *m);
+int coord_multi_deriv_offset(const coord_multi *m, int action, int64_t *offset, int64_t *per_frame);
+int coord_multi_forward_device(coord_multi *m, int n_frames, const double *pos, const double *boxes, unsigned flags,
+                               double *s, double *deriv, double *virial, void *stream);
+/* Record the next coord_multi_forward_device call into a CUDA graph and
+ * replay it on later calls with the same shapes (1) or launch directly (0). */
+int coord_multi_use_graph(coord_multi *m, int enable);
+const char *coord_multi_last_error(const coord_multi *m);
+
+/* ---- tuning and measurement ------------------------------------------------ */
+/* Run the autotuner for this context's shapes now (it otherwise runs on the
+ * first forward).  Returns the chosen configuration as text. */
+int coord_autotune(coord_ctx *ctx, char *desc, size_t desclen);
+/* Microbenchmarks of the device (FP32 FMA, FP64 FMA TFLOP/s, HBM copy GB/s). */
+int coord_measure_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *hbm_gbs);
+/* Kernel launches issued by this library since load (for launch accounting). */
+int64_t coord_launch_count(void);
+/* Average device time (ms) of the pair-evaluation kernel over the launches
+ * since timing was enabled or last read, from CUDA events recorded around it
+ * on the stream it runs on; count receives the number of launches (may be
+ * NULL).  Waits for those events; resets the record. */
+int coord_last_kernel_ms(coord_ctx *ctx, double *ms, int *count);
+/* Turn per-launch event timing of the pair kernel on/off (default off). */
+int coord_set_timing(coord_ctx *ctx, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,266 @@
+"""The COORDINATION action, host side.
+
+``Coordination`` mirrors the reference action's keyword surface and
+per-step contract (src/colvar/Coordination.cpp, CoordinationBase.cpp):
+
+    c = Coordination("GROUPA=1-1000 SWITCH={RATIONAL R_0=0.30 NN=6 MM=12 D_MAX=1.0}")
+    s, deriv, virial = c.calculate(positions, box, step)
+
+``positions`` are the requested atoms in request order (GROUPA then GROUPB,
+as ActionAtomistic::getPositions() returns them), ``box`` is the 3x3 lattice
+(rows are lattice vectors, all zero without pbc).  Derivatives and the
+virial follow Colvar's layout (Colvar.h:74-113).  Keyword errors raise
+``ValueError`` with the reference's messages.  Every number is computed by
+libcoordgpu.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import CoordError, check, dptr
+
+_FLAGS = ("SERIAL", "PAIR", "NLIST", "NLISTCELLS", "NOPBC", "NUMERICAL_DERIVATIVES")
+_KEYS = ("GROUPA", "GROUPB", "NL_CUTOFF", "NL_STRIDE", "SWITCH", "R_0", "NN", "MM", "D_0", "LABEL")
+
+
+def parse_atom_list(text: str) -> List[int]:
+    """GROUPA/GROUPB value: comma-separated serials and ranges a-b or a-b:stride
+    (1-based, as Tools::interpretRanges); returns 0-based absolute indices."""
+    out: List[int] = []
+    for tok in text.split(","):
+        tok = tok.strip()
+        if not tok:
+            continue
+        m = re.fullmatch(r"(\d+)-(\d+)(?::(\d+))?", tok)
+        if m:
+            a, b, st = int(m.group(1)), int(m.group(2)), int(m.group(3) or 1)
+            out.extend(range(a - 1, b, st))
+        elif re.fullmatch(r"\d+", tok):
+            out.append(int(tok) - 1)
+        else:
+            raise ValueError("could not interpret atom list entry '%s'" % tok)
+    return out
+
+
+def split_line(line: str) -> List[str]:
+    """Words of an input line; {...} groups stay one word (Tools::getWords)."""
+    words, cur, depth = [], "", 0
+    for ch in line:
+        if ch == "{":
+            depth += 1
+        elif ch == "}":
+            depth -= 1
+            if depth < 0:
+                raise ValueError("Extra closed parenthesis in '%s'" % line)
+        if ch.isspace() and depth == 0:
+            if cur:
+                words.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if depth != 0:
+        raise ValueError("Unmatched parenthesis in '%s'" % line)
+    if cur:
+        words.append(cur)
+    return words
+
+
+class Coordination:
+    """GPU COORDINATION behind the reference's keyword interface."""
+
+    def __init__(self, line: str = "", *, precision: str = "fp64", device: int = 0, **kw):
+        words = split_line(line)
+        opts = {}
+        flags = set()
+        label = None
+        for w in words:
+            if w.endswith(":") and not opts and not flags and label is None:
+                label = w[:-1]
+                continue
+            if w == "COORDINATION":
+                continue
+            if "=" in w:
+                k, v = w.split("=", 1)
+                if v.startswith("{") and v.endswith("}"):
+                    v = v[1:-1]
+                opts[k.upper()] = v
+            else:
+                flags.add(w.upper())
+        for k, v in kw.items():
+            k = k.upper()
+            if isinstance(v, bool):
+                if v:
+                    flags.add(k)
+            else:
+                opts[k] = v
+        self.label = opts.pop("LABEL", label)
+        for k in opts:
+            if k not in _KEYS:
+                raise ValueError("cannot read keyword %s" % k)
+        for f in flags:
+            if f not in _FLAGS:
+                raise ValueError("cannot read flag %s" % f)
+        ga = opts.get("GROUPA", "")
+        gb = opts.get("GROUPB", "")
+        self.group_a = parse_atom_list(ga) if isinstance(ga, str) else [int(x) for x in ga]
+        self.group_b = parse_atom_list(gb) if isinstance(gb, str) else [int(x) for x in gb]
+        nlist = "NLIST" in flags
+        cells = "NLISTCELLS" in flags
+        if nlist and cells:
+            raise ValueError("Please activate only one of the two version of the NL")
+        self._L = _lib.load()
+        p = _lib.CoordParams()
+        self._L.coord_params_default(C.byref(p))
+        sw = opts.get("SWITCH", "")
+        self._switch_bytes = sw.encode() if sw else None
+        p.switch_def = self._switch_bytes
+        if not sw:
+            p.r0 = float(opts.get("R_0", 0.0))
+            p.d0 = float(opts.get("D_0", 0.0))
+            p.nn = int(opts.get("NN", 6))
+            p.mm = int(opts.get("MM", 0))
+        p.nopbc = int("NOPBC" in flags)
+        p.pair = int("PAIR" in flags)
+        p.serial = int("SERIAL" in flags)
+        p.nlist = _lib.NL_CLASSIC if nlist else (_lib.NL_CELLS if cells else _lib.NL_NONE)
+        p.nl_cutoff = float(opts.get("NL_CUTOFF", 0.0))
+        p.nl_stride = int(float(opts.get("NL_STRIDE", 0)))
+        p.precision = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[precision]
+        p.device = device
+        self.params = p
+        self.precision = precision
+        ctx = C.c_void_p()
+        rc = self._L.coord_create(C.byref(p), C.byref(ctx))
+        self._ctx = ctx
+        if rc != 0:
+            msg = self._L.coord_last_error(ctx).decode() if ctx.value else ""
+            self.close()
+            raise ValueError(msg) if rc == _lib.COORD_ERR_ARG else CoordError(rc, msg)
+        self._groups_set = False
+
+    # -- groups ------------------------------------------------------------
+    def _ensure_groups(self):
+        if self._groups_set:
+            return
+        a = np.ascontiguousarray(self.group_a, dtype=np.int64)
+        b = np.ascontiguousarray(self.group_b, dtype=np.int64)
+        rc = self._L.coord_set_groups(self._ctx, a.ctypes.data_as(C.POINTER(C.c_int64)), len(a),
+                                      b.ctypes.data_as(C.POINTER(C.c_int64)), len(b))
+        if rc == _lib.COORD_ERR_ARG:
+            raise ValueError(self._L.coord_last_error(self._ctx).decode())
+        check(self._L, self._ctx, rc)
+        self._groups_set = True
+
+    @property
+    def nslots(self) -> int:
+        return len(self.group_a) + len(self.group_b)
+
+    @property
+    def requested_atoms(self) -> List[int]:
+        """Absolute atom indices in request order (CoordinationBase.cpp:99)."""
+        return list(self.group_a) + list(self.group_b)
+
+    # -- per step ----------------------------------------------------------
+    def calculate(self, positions, box, step: int = 0, rebuild: bool = False,
+                  derivatives: bool = True) -> Tuple[float, Optional[np.ndarray], Optional[np.ndarray]]:
+        self._ensure_groups()
+        pos = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).reshape(-1, 3))
+        if len(pos) != self.nslots:
+            raise ValueError("expected %d positions, got %d" % (self.nslots, len(pos)))
+        bx = np.ascontiguousarray(np.asarray(box, dtype=np.float64).reshape(9))
+        s = C.c_double()
+        deriv = np.zeros((self.nslots, 3)) if derivatives else None
+        vir = np.zeros(9) if derivatives else None
+        flags = (_lib.FLAG_REBUILD if rebuild else 0) | (0 if derivatives else _lib.FLAG_NO_DERIV)
+        rc = self._L.coord_forward(self._ctx, dptr(pos), dptr(bx), int(step), flags, C.byref(s),
+                                   dptr(deriv) if derivatives else None, dptr(vir) if derivatives else None)
+        check(self._L, self._ctx, rc)
+        return s.value, deriv, (vir.reshape(3, 3) if derivatives else None)
+
+    def calculate_system(self, system_positions, box, step: int = 0, **kw):
+        """Gather the requested atoms from a full system array and calculate."""
+        sp = np.asarray(system_positions, dtype=np.float64).reshape(-1, 3)
+        return self.calculate(sp[self.requested_atoms], box, step, **kw)
+
+    def forward_device(self, pos_ptr: int, boxes, n_frames: int, s_ptr: int, deriv_ptr: int = 0,
+                       virial_ptr: int = 0, step: int = 0, flags: int = 0, stream: int = 0, dparam_ptr: int = 0):
+        """Device-pointer batched forward (pointers as integers, e.g. tensor.data_ptr())."""
+        self._ensure_groups()
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 9))
+        if len(bx) != n_frames:
+            raise ValueError("need one box per frame")
+        rc = self._L.coord_forward_device(self._ctx, int(n_frames), C.c_void_p(pos_ptr), dptr(bx), int(step),
+                                          int(flags), C.c_void_p(s_ptr), C.c_void_p(deriv_ptr or None),
+                                          C.c_void_p(virial_ptr or None), C.c_void_p(dparam_ptr or None),
+                                          C.c_void_p(stream or None))
+        check(self._L, self._ctx, rc)
+
+    def backward_device(self, pos_ptr: int, boxes, n_frames: int, g_ptr: int, grad_pos_ptr: int = 0,
+                        grad_box_ptr: int = 0, grad_param_ptr: int = 0, stream: int = 0):
+        self._ensure_groups()
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 9))
+        rc = self._L.coord_backward_device(self._ctx, int(n_frames), C.c_void_p(pos_ptr), dptr(bx),
+                                           C.c_void_p(g_ptr), C.c_void_p(grad_pos_ptr or None),
+                                           C.c_void_p(grad_box_ptr or None), C.c_void_p(grad_param_ptr or None),
+                                           C.c_void_p(stream or None))
+        check(self._L, self._ctx, rc)
+
+    # -- neighbour list ------------------------------------------------------
+    def nl_size(self, frame: int = 0) -> int:
+        n = C.c_int64()
+        check(self._L, self._ctx, self._L.coord_nl_size(self._ctx, frame, C.byref(n)))
+        return n.value
+
+    def pairs(self, frame: int = 0) -> np.ndarray:
+        n = C.c_int64()
+        check(self._L, self._ctx, self._L.coord_get_pairs(self._ctx, frame, None, 0, C.byref(n)))
+        out = np.zeros(2 * max(n.value, 1), dtype=np.uint32)
+        check(self._L, self._ctx, self._L.coord_get_pairs(self._ctx, frame, out.ctypes.data_as(
+            C.POINTER(C.c_uint32)), n.value, C.byref(n)))
+        return out[:2 * n.value].reshape(-1, 2)
+
+    # -- switching function ------------------------------------------------
+    def switch(self, x, squared: bool = True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        f = np.empty_like(x)
+        df = np.empty_like(x)
+        check(self._L, self._ctx, self._L.coord_switch_eval(self._ctx, len(x), dptr(x), int(squared), dptr(f),
+                                                             dptr(df)))
+        return f, df
+
+    def switch_params(self) -> dict:
+        out = np.zeros(7)
+        check(self._L, self._ctx, self._L.coord_switch_params(self._ctx, dptr(out)))
+        return dict(zip(["d0", "dmax", "dmax_2", "invr0", "invr0_2", "stretch", "shift"], out))
+
+    # -- tuning / timing -----------------------------------------------------
+    def set_timing(self, enable: bool = True):
+        check(self._L, self._ctx, self._L.coord_set_timing(self._ctx, int(enable)))
+
+    def kernel_ms(self):
+        """(average ms, launches) of the pair kernel since timing was enabled/last read."""
+        ms = C.c_double()
+        n = C.c_int()
+        check(self._L, self._ctx, self._L.coord_last_kernel_ms(self._ctx, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def autotune(self) -> str:
+        buf = C.create_string_buffer(256)
+        check(self._L, self._ctx, self._L.coord_autotune(self._ctx, buf, 256))
+        return buf.value.decode()
+
+    def close(self):
+        if getattr(self, "_ctx", None) is not None and self._ctx.value:
+            self._L.coord_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,841 @@
+// coord_api.cu -- the C ABI (include/coordgpu.h): contexts, buffers, the
+// per-step launch sequence.  Host code; kernels live in k_fp64.cu/k_mixed.cu.
+#include "coordgpu.h"
+#include "launch.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace coordgpu;
+
+namespace {
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) {
+      n = std::max<size_t>(want, 1);
+      // zero-filled before any kernel of the context's (non-blocking) stream can see it
+      e = cudaMemset(p, 0, n * sizeof(T));
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <typename T> struct HostBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = std::max<size_t>(want, 1);
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+} // namespace
+
+struct coord_ctx {
+  coord_params p{};
+  std::string switch_def;
+  SwitchParams sw{};
+  SwitchF32 s32{};
+  int mode = MODE_SINGLE;
+  int64_t nA = 0, nB = 0, ns = 0;
+  bool groups_set = false;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  // neighbour-list state
+  bool firsttime = true;
+  int built_frames = 0;
+  int cap = 0, self_cap = 64, ncell_cap = 0, max_blocks = 0;
+  int nframes_alloc = 0;
+  // device buffers
+  DevBuf<int64_t> abs_of_slot;
+  DevBuf<FrameConst> fc;
+  DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, scatter_tmp, row_len, slice_w;
+  DevBuf<double4> x64;
+  DevBuf<uint4> q;
+  DevBuf<uint32_t> ell, self_pairs;
+  DevBuf<unsigned long long> nl_count, mm;
+  DevBuf<unsigned char> pair_flag;
+  DevBuf<double> acc64, partials;
+  DevBuf<float4> acc32;
+  DevBuf<unsigned> tickets;
+  // host-API staging
+  DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam;
+  HostBuf<double> h_pos, h_out;
+  HostBuf<FrameConst> h_fc;
+  HostBuf<unsigned long long> h_nl;
+  std::vector<FrameConst> fc_uploaded;
+  std::vector<double> boxes_seen;
+  // tuning
+  int tile64 = 64, tile32 = 128, ap_blocks = 0;
+  bool tuned = false;
+  // timing: one event pair per pair-kernel launch while enabled
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  size_t ev_used = 0;
+
+  int fail(int code, const std::string &m) {
+    err = m;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char *where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return COORD_ERR_CUDA;
+  }
+};
+
+namespace {
+
+bool box_is_zero(const double *b) {
+  for (int i = 0; i < 9; i++)
+    if (b[i] != 0.0) return false;
+  return true;
+}
+
+int nl_kind_of(const coord_ctx *c) { return c->p.nlist; }
+
+// Per-frame constants from the box (host part; no-pbc frames are finished on
+// the device by k_bounds_finish).
+int frame_setup(coord_ctx *c, const double *box, FrameConst *fc, bool *need_bounds) {
+  std::memset(fc, 0, sizeof *fc);
+  pbc_setup(box, &fc->pbc);
+  const bool do_pbc = !c->p.nopbc;
+  const bool usepbc = do_pbc && fc->pbc.type != PBC_UNSET;
+  const int kind = nl_kind_of(c);
+  const double cut = c->p.nl_cutoff;
+  GridParams &g = fc->grid;
+  g.nc[0] = g.nc[1] = g.nc[2] = 1;
+  g.ncells = 1;
+  for (int k = 0; k < 3; k++) g.inv_width[k] = 1.0;
+  *need_bounds = false;
+  if (kind == COORD_NL_CLASSIC) {
+    if (usepbc && fc->pbc.type == PBC_ORTHO) {
+      g.wrap = 1;
+      for (int k = 0; k < 3; k++) {
+        int n = (int)std::floor(fc->pbc.box[4 * k] / (cut * (1.0 + 1e-9)));
+        if (n < 3) n = 1;
+        g.nc[k] = std::min(n, 1024);
+      }
+      // bound the grid (cells may be larger than the cutoff, never smaller)
+      const long long maxcells = std::max<long long>(8 * std::max<int64_t>(c->ns, 1), 1 << 16);
+      while ((long long)g.nc[0] * g.nc[1] * g.nc[2] > maxcells) {
+        const int k = (g.nc[0] >= g.nc[1] && g.nc[0] >= g.nc[2]) ? 0 : (g.nc[1] >= g.nc[2] ? 1 : 2);
+        g.nc[k] = std::max(1, g.nc[k] / 2);
+      }
+    } else if (usepbc) {
+      g.wrap = 0;  // generic box: one cell, every candidate tested exactly
+    } else {
+      *need_bounds = true;
+    }
+  } else if (kind == COORD_NL_CELLS) {
+    if (box_is_zero(box)) {
+      *need_bounds = true;
+    } else {
+      // LinkCells::createCells (LinkCells.cpp:99-122): reciprocal = invBox^T
+      for (int k = 0; k < 3; k++) {
+        const double *ib = fc->pbc.invbox;
+        const double m = std::sqrt(ib[0 * 3 + k] * ib[0 * 3 + k] + ib[1 * 3 + k] * ib[1 * 3 + k] +
+                                   ib[2 * 3 + k] * ib[2 * 3 + k]);
+        int n = (int)std::floor(1.0 / m / cut);
+        if (n == 0) n = 1;
+        g.nc[k] = n;
+      }
+    }
+  }
+  g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
+  fc->cut2 = cut * cut;
+  // fixed-point frame
+  if (usepbc && fc->pbc.type == PBC_ORTHO) {
+    fc->fixed_ok = 1;
+    double span = 0;
+    for (int k = 0; k < 3; k++) {
+      fc->inv_l[k] = fc->pbc.invbox[4 * k];
+      fc->scale[k] = (float)(fc->pbc.box[4 * k] / 4294967296.0);
+      span = std::max(span, fc->pbc.box[4 * k]);
+    }
+    const double band = 1e-4 * fc->cut2 + 8.0 * cut * span / 4294967296.0 + 1e-12;
+    fc->cut2_lo = (float)(fc->cut2 - band);
+    fc->cut2_hi = (float)(fc->cut2 + band);
+  } else if (!usepbc) {
+    fc->fixed_ok = 1;
+    *need_bounds = *need_bounds || (c->p.precision == COORD_PREC_MIXED) || kind == COORD_NL_CLASSIC;
+    fc->cut2_lo = -1.0f;  // finished on the device (span known there)
+    fc->cut2_hi = -1.0f;
+  } else {
+    fc->fixed_ok = 0;  // generic box
+  }
+  return COORD_OK;
+}
+
+int ensure_buffers(coord_ctx *c, int n_frames) {
+  cudaError_t e;
+  const size_t F = (size_t)n_frames, ns = (size_t)std::max<int64_t>(c->ns, 1);
+  const int nslices = (int)((c->ns + 31) / 32);
+#define ENS(buf, n)                                    \
+  if ((e = (buf).ensure(n)) != cudaSuccess) {          \
+    return c->cuda_fail(e, "allocation of " #buf);     \
+  }
+  ENS(c->fc, F);
+  ENS(c->slot_of_rank, F * ns);
+  ENS(c->cell_of_slot, F * ns);
+  ENS(c->scatter_tmp, F * ns);
+  ENS(c->row_len, F * ns);
+  ENS(c->slice_w, F * std::max(nslices, 1));
+  ENS(c->x64, F * ns);
+  ENS(c->q, F * ns);
+  ENS(c->acc64, F * ns * 3);
+  ENS(c->acc32, F * ns);
+  ENS(c->nl_count, F * 4);
+  ENS(c->mm, F * 6);
+  ENS(c->tickets, F);
+  ENS(c->cell_count, F * (size_t)c->ncell_cap);
+  ENS(c->cell_fill, F * (size_t)c->ncell_cap);
+  ENS(c->cell_start, F * ((size_t)c->ncell_cap + 1));
+  ENS(c->self_pairs, F * (size_t)c->self_cap * 2);
+  ENS(c->pair_flag, F * (size_t)std::max<int64_t>(c->nA, 1));
+  ENS(c->partials, F * (size_t)c->max_blocks * kPartials);
+  if (c->p.nlist != COORD_NL_NONE && c->mode != MODE_PAIR) {
+    ENS(c->ell, F * (size_t)nslices * (size_t)c->cap * 32);
+  }
+#undef ENS
+  if ((e = c->h_fc.ensure(F)) != cudaSuccess) return c->cuda_fail(e, "pinned allocation");
+  if ((e = c->h_nl.ensure(F * 4)) != cudaSuccess) return c->cuda_fail(e, "pinned allocation");
+  c->nframes_alloc = std::max(c->nframes_alloc, n_frames);
+  return COORD_OK;
+}
+
+KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags, double *s, double *deriv,
+                double *virial, double *dparam) {
+  KArgs a{};
+  a.nframes = n_frames;
+  a.ns = (int)c->ns;
+  a.nA = (int)(c->mode == MODE_SINGLE ? c->ns : c->nA);
+  a.mode = c->mode;
+  a.do_pbc = !c->p.nopbc;
+  a.nl_kind = c->p.nlist;
+  a.cap = c->cap;
+  a.ncell_cap = c->ncell_cap;
+  a.self_cap = c->self_cap;
+  a.nslices = (int)((c->ns + 31) / 32);
+  a.flags = (int)flags;
+  a.fc = c->fc.p;
+  a.abs_of_slot = c->abs_of_slot.p;
+  a.pos = d_pos;
+  a.cell_of_slot = c->cell_of_slot.p;
+  a.cell_count = c->cell_count.p;
+  a.cell_start = c->cell_start.p;
+  a.cell_fill = c->cell_fill.p;
+  a.slot_of_rank = c->slot_of_rank.p;
+  a.scatter_tmp = c->scatter_tmp.p;
+  a.x64 = c->x64.p;
+  a.q = c->q.p;
+  a.ell = c->ell.p;
+  a.row_len = c->row_len.p;
+  a.slice_w = c->slice_w.p;
+  a.nl_count = c->nl_count.p;
+  a.self_pairs = c->self_pairs.p;
+  a.pair_flag = c->pair_flag.p;
+  a.acc64 = c->acc64.p;
+  a.acc32 = c->acc32.p;
+  a.partials = c->partials.p;
+  a.max_blocks = c->max_blocks;
+  a.tickets = c->tickets.p;
+  a.out_s = s;
+  a.out_deriv = deriv;
+  a.out_virial = virial;
+  a.out_dparam = dparam;
+  return a;
+}
+
+// Initial row capacity of the neighbour list: half the expected neighbours
+// plus margin (grown on overflow).
+int estimate_cap(coord_ctx *c, const double *box) {
+  PbcParams p;
+  pbc_setup(box, &p);
+  const double cut = c->p.nl_cutoff;
+  double vol = 0.0;
+  if (!c->p.nopbc && p.type != PBC_UNSET) {
+    const double *b = p.box;
+    vol = std::fabs(b[0] * b[4] * b[8] + b[1] * b[5] * b[6] + b[2] * b[3] * b[7] - b[0] * b[5] * b[7] -
+                    b[1] * b[3] * b[8] - b[2] * b[4] * b[6]);
+  }
+  double expect;
+  if (vol > 0) {
+    const double rho = (double)c->ns / vol;
+    if (c->p.nlist == COORD_NL_CELLS) {
+      int nc[3];
+      for (int k = 0; k < 3; k++) {
+        const double m = std::sqrt(p.invbox[k] * p.invbox[k] + p.invbox[3 + k] * p.invbox[3 + k] +
+                                   p.invbox[6 + k] * p.invbox[6 + k]);
+        nc[k] = std::max(1, (int)std::floor(1.0 / m / cut));
+      }
+      expect = 27.0 * (double)c->ns / ((double)nc[0] * nc[1] * nc[2]);
+    } else {
+      expect = rho * 4.18879020478639 * cut * cut * cut;
+    }
+    expect = std::min(expect, (double)c->ns);
+    int cap = (int)std::ceil(0.5 * expect * 1.35 + 24);
+    return (cap + 7) & ~7;
+  }
+  return (int)std::min<int64_t>(std::max<int64_t>(c->ns, 1), 64);
+}
+
+int set_tuning_defaults(coord_ctx *c) {
+  if (c->ap_blocks == 0) c->ap_blocks = std::max(1, c->nsm) * 8;
+  return 0;
+}
+
+int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bounds_any) {
+  *need_bounds_any = false;
+  bool changed = (int)c->fc_uploaded.size() != n_frames;
+  c->fc_uploaded.resize(n_frames);
+  for (int f = 0; f < n_frames; f++) {
+    FrameConst fcs;
+    bool nb = false;
+    frame_setup(c, boxes + 9 * (size_t)f, &fcs, &nb);
+    *need_bounds_any = *need_bounds_any || nb;
+    if (std::memcmp(&fcs, &c->fc_uploaded[f], sizeof fcs) != 0) changed = true;
+    c->fc_uploaded[f] = fcs;
+    if (fcs.pbc.type == PBC_GENERIC && !c->p.nopbc && c->p.precision == COORD_PREC_MIXED)
+      return c->fail(COORD_ERR_UNSUPPORTED, "the mixed-precision path needs an orthorhombic box (or NOPBC); "
+                                            "use the FP64 path for triclinic boxes");
+    if (fcs.grid.ncells > c->ncell_cap) return COORD_ERR_STATE;  // caller grows ncell_cap
+  }
+  if (changed || *need_bounds_any) {
+    std::memcpy(c->h_fc.p, c->fc_uploaded.data(), sizeof(FrameConst) * n_frames);
+    cudaError_t e =
+        cudaMemcpyAsync(c->fc.p, c->h_fc.p, sizeof(FrameConst) * n_frames, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "frame upload");
+  }
+  return COORD_OK;
+}
+
+int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
+                 double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream) {
+  if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
+  if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
+  if (flags & (COORD_FLAG_DR0)) return c->fail(COORD_ERR_UNSUPPORTED, "ds/dR_0 is provided by coord_backward_device");
+  if (c->ns == 0) {
+    // empty groups: s = 0, no derivatives
+    if (s) cudaMemsetAsync(s, 0, sizeof(double) * n_frames, stream);
+    if (virial) cudaMemsetAsync(virial, 0, sizeof(double) * 9 * n_frames, stream);
+    return COORD_OK;
+  }
+  cudaStream_t saved = c->stream;
+  if (stream) c->stream = stream;
+  struct Restore {
+    coord_ctx *c;
+    cudaStream_t s;
+    ~Restore() { c->stream = s; }
+  } restore{c, saved};
+
+  const bool nl = c->p.nlist != COORD_NL_NONE;
+  const bool mixed = c->p.precision == COORD_PREC_MIXED;
+  const int nl_stride = c->p.nl_stride;
+  // NeighborList::prepare (NeighborList.cpp:433-456)
+  bool rebuild = false;
+  if (nl) {
+    if (nl_stride == 1 || c->firsttime || (step % nl_stride) == 0 || (flags & COORD_FLAG_REBUILD) ||
+        c->built_frames != n_frames)
+      rebuild = true;
+  }
+  // sizes
+  if (c->cap == 0 && nl) c->cap = estimate_cap(c, boxes);
+  {
+    int need_cells = (int)std::max<int64_t>(c->ns, 64);
+    for (int f = 0; f < n_frames; f++) {
+      FrameConst tmp;
+      bool nb;
+      frame_setup(c, boxes + 9 * (size_t)f, &tmp, &nb);
+      need_cells = std::max(need_cells, tmp.grid.ncells);
+    }
+    if (need_cells > c->ncell_cap) c->ncell_cap = need_cells;
+  }
+  set_tuning_defaults(c);
+  c->max_blocks = std::max<int>(c->max_blocks, std::max<int>((int)((c->ns + 255) / 256), c->ap_blocks));
+  c->max_blocks = std::max<int>(c->max_blocks, (int)((std::max<int64_t>(c->nA, 1) + 255) / 256));
+  int rc = ensure_buffers(c, n_frames);
+  if (rc) return rc;
+  bool need_bounds = false;
+  rc = upload_frames(c, n_frames, boxes, &need_bounds);
+  if (rc) return rc;
+
+  KArgs a = make_args(c, n_frames, d_pos, flags, s, (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv,
+                      (flags & COORD_FLAG_NO_DERIV) ? nullptr : virial, dparam);
+  cudaError_t e;
+  if (rebuild) cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
+  if (need_bounds && (mixed || rebuild)) {
+    // min/max sentinels: lo = all ones, hi = 0
+    std::vector<unsigned long long> init(6 * (size_t)n_frames);
+    for (int f = 0; f < n_frames; f++)
+      for (int k = 0; k < 6; k++) init[6 * f + k] = k < 3 ? ~0ull : 0ull;
+    if ((e = cudaMemcpyAsync(c->mm.p, init.data(), sizeof(unsigned long long) * init.size(), cudaMemcpyHostToDevice,
+                             c->stream)) != cudaSuccess)
+      return c->cuda_fail(e, "bounds init");
+    launch_bounds(a, c->mm.p, nl ? c->p.nl_cutoff : 1.0, c->p.nlist == COORD_NL_CELLS && rebuild ? 1 : 0, c->stream);
+    // the band of the FP32 prefilter depends on the frame span: finish it here
+  }
+
+  if (rebuild) {
+    if (c->mode == MODE_PAIR) {
+      cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
+      launch_pair_flags(a, c->stream);
+    } else {
+      for (int attempt = 0; attempt < 8; attempt++) {
+        if (attempt > 0)
+          cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
+        launch_nl_build(a, c->stream);
+        if ((e = cudaMemcpyAsync(c->h_nl.p, c->nl_count.p, sizeof(unsigned long long) * 4 * n_frames,
+                                 cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+          return c->cuda_fail(e, "neighbour-list count");
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return c->cuda_fail(e, "neighbour-list build");
+        unsigned long long need = 0, selfn = 0;
+        for (int f = 0; f < n_frames; f++) {
+          need = std::max(need, c->h_nl.p[4 * f + 2]);
+          selfn = std::max(selfn, c->h_nl.p[4 * f + 1]);
+          if (c->h_nl.p[4 * f + 3])
+            return c->fail(COORD_ERR_UNSUPPORTED, "NLISTCELLS without a box: the bounding box needs more link "
+                                                  "cells than this context allocated");
+        }
+        bool again = false;
+        if (need > (unsigned long long)c->cap) {
+          c->cap = (int)((need * 5 / 4 + 8) & ~7ull);
+          again = true;
+        }
+        if (selfn > (unsigned long long)c->self_cap) {
+          c->self_cap = (int)(selfn + 64);
+          again = true;
+        }
+        if (!again) break;
+        if ((rc = ensure_buffers(c, n_frames))) return rc;
+        a = make_args(c, n_frames, d_pos, flags, s, (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv,
+                      (flags & COORD_FLAG_NO_DERIV) ? nullptr : virial, dparam);
+        if (attempt == 7) return c->fail(COORD_ERR_NOMEM, "neighbour list did not fit after 8 attempts");
+      }
+    }
+    c->firsttime = false;
+    c->built_frames = n_frames;
+  }
+
+  cudaEvent_t tev1 = nullptr;
+  if (c->timing) {
+    if (c->ev_used == c->ev_pool.size()) {
+      cudaEvent_t x, y;
+      cudaEventCreate(&x);
+      cudaEventCreate(&y);
+      c->ev_pool.push_back({x, y});
+    }
+    cudaEventRecord(c->ev_pool[c->ev_used].first, c->stream);
+    tev1 = c->ev_pool[c->ev_used].second;
+    c->ev_used++;
+  }
+  if (c->mode == MODE_PAIR) {
+    if (mixed) {
+      launch_gather(a, 0, 0, 1, c->stream);
+      launch_pairs32(a, c->sw, c->s32, nl ? 1 : 0, c->stream);
+    } else {
+      launch_pairs64(a, c->sw, nl ? 1 : 0, c->stream);
+    }
+  } else if (!nl) {
+    if (mixed) {
+      launch_gather(a, 0, 0, 1, c->stream);
+      launch_allpairs32(a, c->sw, c->s32, c->tile32, c->ap_blocks, c->stream);
+    } else {
+      launch_allpairs64(a, c->sw, c->tile64, c->ap_blocks, c->stream);
+    }
+  } else {
+    if (mixed) {
+      launch_gather(a, 1, 0, 1, c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, 256, c->stream);
+    } else {
+      launch_gather(a, 1, 1, 0, c->stream);
+      launch_eval_nl64(a, c->sw, c->stream);
+    }
+  }
+  if (tev1) cudaEventRecord(tev1, c->stream);
+  const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  if (mixed)
+    launch_finalize32(a, rank_order, c->stream);
+  else
+    launch_finalize64(a, rank_order, c->stream);
+  if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "kernel launch");
+  return COORD_OK;
+}
+
+int device_init(coord_ctx *c) {
+  if (c->stream) {
+    cudaSetDevice(c->p.device);
+    return COORD_OK;
+  }
+  cudaError_t e = cudaSetDevice(c->p.device);
+  if (e != cudaSuccess) return c->cuda_fail(e, "cudaSetDevice");
+  cudaDeviceProp prop;
+  if ((e = cudaGetDeviceProperties(&prop, c->p.device)) != cudaSuccess) return c->cuda_fail(e, "device properties");
+  c->nsm = prop.multiProcessorCount;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return c->cuda_fail(e, "stream");
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  return COORD_OK;
+}
+
+} // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void coord_params_default(coord_params *p) {
+  std::memset(p, 0, sizeof *p);
+  p->nn = 6;
+  p->mm = 0;
+  p->d0 = 0.0;
+  p->precision = COORD_PREC_FP64;
+}
+
+const char *coord_status_string(int status) {
+  switch (status) {
+  case COORD_OK: return "ok";
+  case COORD_ERR_ARG: return "invalid argument";
+  case COORD_ERR_CUDA: return "CUDA error";
+  case COORD_ERR_BOX: return "invalid box";
+  case COORD_ERR_UNSUPPORTED: return "unsupported input";
+  case COORD_ERR_NOMEM: return "out of device memory";
+  case COORD_ERR_TIMEOUT: return "device wait timed out";
+  case COORD_ERR_STATE: return "call out of order";
+  default: return "unknown status";
+  }
+}
+
+const char *coord_last_error(const coord_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int coord_create(const coord_params *p, coord_ctx **out) {
+  if (!p || !out) return COORD_ERR_ARG;
+  *out = nullptr;
+  coord_ctx *c = new coord_ctx();
+  c->p = *p;
+  auto bad = [&](int code, const std::string &m) {
+    // keep the context so the caller can read the message, as Action::error would report it
+    c->err = m;
+    *out = c;
+    return code;
+  };
+  // CoordinationBase::CoordinationBase (CoordinationBase.cpp:66-84)
+  if (p->nlist != COORD_NL_NONE && p->nlist != COORD_NL_CLASSIC && p->nlist != COORD_NL_CELLS)
+    return bad(COORD_ERR_ARG, "unknown neighbour-list kind");
+  if (p->nlist == COORD_NL_CELLS && p->pair)
+    return bad(COORD_ERR_ARG, "Pair is not compatible with the CELLS implementation of the NL");
+  if (p->nlist != COORD_NL_NONE) {
+    if (p->nl_cutoff <= 0.0) return bad(COORD_ERR_ARG, "NL_CUTOFF should be explicitly specified and positive");
+    if (p->nl_stride <= 0) return bad(COORD_ERR_ARG, "NL_STRIDE should be explicitly specified and positive");
+  }
+  if (p->precision != COORD_PREC_FP64 && p->precision != COORD_PREC_MIXED)
+    return bad(COORD_ERR_ARG, "unknown precision");
+  // Coordination::Coordination (Coordination.cpp:128-157)
+  if (p->switch_def && p->switch_def[0]) {
+    c->switch_def = p->switch_def;
+    char err[512];
+    err[0] = 0;
+    const int rc = switch_from_string(p->switch_def, &c->sw, err, sizeof err);
+    if (rc == 2) return bad(COORD_ERR_UNSUPPORTED, std::string("problem reading SWITCH keyword : ") + err);
+    if (rc) return bad(COORD_ERR_ARG, std::string("problem reading SWITCH keyword : ") + err);
+  } else {
+    if (p->r0 <= 0.0) return bad(COORD_ERR_ARG, "R_0 should be explicitly specified and positive");
+    switch_from_rational(p->nn, p->mm, p->r0, p->d0, &c->sw);
+  }
+  c->p.switch_def = nullptr;
+  // FP32 parameters of the mixed path
+  {
+    const SwitchParams &s = c->sw;
+    c->s32.dmax2 = (s.dmax_2 >= 3.0e38) ? INFINITY : (float)s.dmax_2;
+    c->s32.invr0_2 = (float)s.invr0_2;
+    c->s32.stretch = (float)s.stretch;
+    c->s32.shift = (float)s.shift;
+    const int nh = s.type == SW_RATFIX ? s.nn / 2 : 0;
+    c->s32.c = (float)(-(double)nh * 2.0 * s.invr0_2 * s.stretch);
+  }
+  // CUDA is initialised on first use (coord_set_groups), so keyword checks and
+  // switch set-up work on machines without a GPU.
+  *out = c;
+  return COORD_OK;
+}
+
+int coord_destroy(coord_ctx *c) {
+  if (!c) return COORD_OK;
+  if (c->stream) {
+    cudaSetDevice(c->p.device);
+    cudaStreamSynchronize(c->stream);
+  }
+  c->abs_of_slot.release();
+  c->fc.release();
+  c->cell_of_slot.release();
+  c->cell_count.release();
+  c->cell_start.release();
+  c->cell_fill.release();
+  c->slot_of_rank.release();
+  c->scatter_tmp.release();
+  c->row_len.release();
+  c->slice_w.release();
+  c->x64.release();
+  c->q.release();
+  c->ell.release();
+  c->self_pairs.release();
+  c->nl_count.release();
+  c->mm.release();
+  c->pair_flag.release();
+  c->acc64.release();
+  c->partials.release();
+  c->acc32.release();
+  c->tickets.release();
+  c->d_pos.release();
+  c->d_s.release();
+  c->d_deriv.release();
+  c->d_virial.release();
+  c->d_dparam.release();
+  c->h_pos.release();
+  c->h_out.release();
+  c->h_fc.release();
+  c->h_nl.release();
+  for (auto &pr : c->ev_pool) {
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return COORD_OK;
+}
+
+int coord_set_groups(coord_ctx *c, const int64_t *a, int64_t na, const int64_t *b, int64_t nb) {
+  if (!c) return COORD_ERR_ARG;
+  if (na < 0 || nb < 0 || (na > 0 && !a) || (nb > 0 && !b)) return c->fail(COORD_ERR_ARG, "bad group arrays");
+  if (na + nb > (int64_t)kRankMask) return c->fail(COORD_ERR_UNSUPPORTED, "more than 2^31-1 slots");
+  if (c->p.pair) {
+    if (na != nb)
+      return c->fail(COORD_ERR_ARG, "when using PAIR option, the two groups should have the same number of elements");
+    c->mode = MODE_PAIR;
+  } else {
+    c->mode = nb > 0 ? MODE_TWO : MODE_SINGLE;
+  }
+  c->nA = na;
+  c->nB = nb;
+  c->ns = na + nb;
+  std::vector<int64_t> abs(std::max<int64_t>(c->ns, 1));
+  for (int64_t i = 0; i < na; i++) abs[i] = a[i];
+  for (int64_t i = 0; i < nb; i++) abs[na + i] = b[i];
+  if (int rc = device_init(c)) return rc;
+  cudaError_t e = c->abs_of_slot.ensure(abs.size());
+  if (e != cudaSuccess) return c->cuda_fail(e, "allocation");
+  if ((e = cudaMemcpy(c->abs_of_slot.p, abs.data(), sizeof(int64_t) * abs.size(), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return c->cuda_fail(e, "group upload");
+  c->groups_set = true;
+  c->firsttime = true;
+  c->cap = 0;
+  c->fc_uploaded.clear();
+  return COORD_OK;
+}
+
+int coord_switch_eval(const coord_ctx *c, int n, const double *x, int squared, double *f, double *df) {
+  if (!c || n < 0 || (n > 0 && (!x || !f || !df))) return COORD_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    f[i] = squared ? switch_host_calculate_sqr(c->sw, x[i], df + i) : switch_host_calculate(c->sw, x[i], df + i);
+  return COORD_OK;
+}
+
+int coord_switch_params(const coord_ctx *c, double out[7]) {
+  if (!c || !out) return COORD_ERR_ARG;
+  const SwitchParams &s = c->sw;
+  const double v[7] = {s.d0, s.dmax, s.dmax_2, s.invr0, s.invr0_2, s.stretch, s.shift};
+  std::memcpy(out, v, sizeof v);
+  return COORD_OK;
+}
+
+int coord_get_nslots(const coord_ctx *c, int64_t *nslots) {
+  if (!c || !nslots) return COORD_ERR_ARG;
+  *nslots = c->ns;
+  return COORD_OK;
+}
+
+int coord_forward_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes, int64_t step,
+                         unsigned flags, double *s, double *deriv, double *virial, double *dparam, void *stream) {
+  if (!c) return COORD_ERR_ARG;
+  if (!boxes || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions or boxes");
+  cudaSetDevice(c->p.device);
+  return forward_impl(c, n_frames, pos, boxes, step, flags, s, deriv, virial, dparam, (cudaStream_t)stream);
+}
+
+int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t step, unsigned flags, double *s,
+                  double *deriv, double *virial) {
+  if (!c) return COORD_ERR_ARG;
+  if (!box || !s || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions, box or s");
+  if (!(flags & COORD_FLAG_NO_DERIV) && !deriv && c->ns > 0) return c->fail(COORD_ERR_ARG, "null deriv");
+  cudaSetDevice(c->p.device);
+  const size_t n3 = (size_t)c->ns * 3;
+  cudaError_t e;
+  if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3)) || (e = c->d_s.ensure(1)) ||
+      (e = c->d_virial.ensure(9)) || (e = c->h_pos.ensure(n3)) || (e = c->h_out.ensure(n3 + 10)))
+    return c->cuda_fail(e, "staging allocation");
+  if (n3) {
+    std::memcpy(c->h_pos.p, pos, n3 * sizeof(double));
+    if ((e = cudaMemcpyAsync(c->d_pos.p, c->h_pos.p, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
+      return c->cuda_fail(e, "H2D positions");
+  }
+  int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, c->d_s.p, c->d_deriv.p, c->d_virial.p, nullptr, nullptr);
+  if (rc) return rc;
+  cudaMemcpyAsync(c->h_out.p, c->d_s.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  const bool want_d = !(flags & COORD_FLAG_NO_DERIV);
+  if (want_d) {
+    cudaMemcpyAsync(c->h_out.p + 1, c->d_virial.p, 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (n3) cudaMemcpyAsync(c->h_out.p + 10, c->d_deriv.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  }
+  if ((e = cudaStreamSynchronize(c->stream))) return c->cuda_fail(e, "forward");
+  *s = c->h_out.p[0];
+  if (want_d) {
+    if (virial) std::memcpy(virial, c->h_out.p + 1, 9 * sizeof(double));
+    if (n3) std::memcpy(deriv, c->h_out.p + 10, n3 * sizeof(double));
+  }
+  return COORD_OK;
+}
+
+int coord_backward_device(coord_ctx *c, int, const double *, const double *, const double *, double *, double *,
+                          double *, void *) {
+  if (!c) return COORD_ERR_ARG;
+  return c->fail(COORD_ERR_UNSUPPORTED, "backward not built yet");
+}
+
+int coord_nl_size(coord_ctx *c, int frame, int64_t *n) {
+  if (!c || !n) return COORD_ERR_ARG;
+  if (c->p.nlist == COORD_NL_NONE) {
+    const int64_t ns = c->ns;
+    *n = c->mode == MODE_SINGLE ? ns * (ns - 1) / 2 : (c->mode == MODE_TWO ? c->nA * c->nB : c->nA);
+    return COORD_OK;
+  }
+  if (frame < 0 || frame >= c->built_frames) return c->fail(COORD_ERR_STATE, "no neighbour list for that frame");
+  unsigned long long h[4];
+  cudaSetDevice(c->p.device);
+  cudaError_t e = cudaMemcpyAsync(h, c->nl_count.p + 4 * (size_t)frame, sizeof h, cudaMemcpyDeviceToHost, c->stream);
+  if (!e) e = cudaStreamSynchronize(c->stream);
+  if (e) return c->cuda_fail(e, "nl size");
+  *n = (int64_t)(h[0] + h[1]);
+  return COORD_OK;
+}
+
+int coord_get_pairs(coord_ctx *c, int frame, uint32_t *pairs, int64_t cap, int64_t *n) {
+  if (!c || !n) return COORD_ERR_ARG;
+  if (c->p.nlist == COORD_NL_NONE) return c->fail(COORD_ERR_STATE, "no neighbour list (NLIST not active)");
+  if (frame < 0 || frame >= c->built_frames) return c->fail(COORD_ERR_STATE, "no neighbour list for that frame");
+  cudaSetDevice(c->p.device);
+  cudaStreamSynchronize(c->stream);
+  std::vector<std::pair<uint32_t, uint32_t>> out;
+  const size_t ns = (size_t)c->ns, fo = (size_t)frame * ns;
+  if (c->mode == MODE_PAIR) {
+    std::vector<unsigned char> fl(c->nA);
+    cudaMemcpy(fl.data(), c->pair_flag.p + (size_t)frame * c->nA, c->nA, cudaMemcpyDeviceToHost);
+    for (int64_t i = 0; i < c->nA; i++)
+      if (fl[i]) out.push_back({(uint32_t)i, (uint32_t)(i + c->nA)});
+  } else {
+    const int nslices = (int)((ns + 31) / 32);
+    std::vector<int> slot(ns), len(ns);
+    std::vector<uint32_t> ell((size_t)nslices * c->cap * 32);
+    unsigned long long cnt[4];
+    cudaMemcpy(slot.data(), c->slot_of_rank.p + fo, ns * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(len.data(), c->row_len.p + fo, ns * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(ell.data(), c->ell.p + (size_t)frame * nslices * c->cap * 32, ell.size() * sizeof(uint32_t),
+               cudaMemcpyDeviceToHost);
+    cudaMemcpy(cnt, c->nl_count.p + 4 * (size_t)frame, sizeof cnt, cudaMemcpyDeviceToHost);
+    for (size_t r = 0; r < ns; r++)
+      for (int k = 0; k < len[r]; k++) {
+        const uint32_t e = ell[((r >> 5) * c->cap + k) * 32 + (r & 31)];
+        const uint32_t p = e & kRankMask;
+        const bool rfirst = (e & kOrientBit) != 0;
+        const uint32_t a = (uint32_t)slot[r], b = (uint32_t)slot[p];
+        out.push_back(rfirst ? std::make_pair(a, b) : std::make_pair(b, a));
+      }
+    const size_t nself = std::min<unsigned long long>(cnt[1], (unsigned long long)c->self_cap);
+    std::vector<uint32_t> sp(2 * std::max<size_t>(nself, 1));
+    if (nself)
+      cudaMemcpy(sp.data(), c->self_pairs.p + (size_t)frame * c->self_cap * 2, nself * 2 * sizeof(uint32_t),
+                 cudaMemcpyDeviceToHost);
+    for (size_t k = 0; k < nself; k++) out.push_back({sp[2 * k], sp[2 * k + 1]});
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e) return c->cuda_fail(e, "get pairs");
+  std::sort(out.begin(), out.end());
+  *n = (int64_t)out.size();
+  for (int64_t i = 0; i < *n && i < cap; i++) {
+    pairs[2 * i] = out[i].first;
+    pairs[2 * i + 1] = out[i].second;
+  }
+  return COORD_OK;
+}
+
+int coord_autotune(coord_ctx *c, char *desc, size_t desclen) {
+  if (!c) return COORD_ERR_ARG;
+  if (desc && desclen) std::snprintf(desc, desclen, "tile64=%d tile32=%d blocks=%d", c->tile64, c->tile32, c->ap_blocks);
+  return COORD_OK;
+}
+
+int coord_measure_peaks(int device, double *fp32, double *fp64, double *hbm) {
+  return measure_peaks(device, fp32, fp64, hbm);
+}
+
+int64_t coord_launch_count(void) { return g_launches.load(); }
+
+int coord_last_kernel_ms(coord_ctx *c, double *ms, int *count) {
+  if (!c || !ms) return COORD_ERR_ARG;
+  *ms = 0.0;
+  if (count) *count = 0;
+  double tot = 0.0;
+  for (size_t i = 0; i < c->ev_used; i++) {
+    float t = 0.f;
+    cudaEventSynchronize(c->ev_pool[i].second);
+    if (cudaEventElapsedTime(&t, c->ev_pool[i].first, c->ev_pool[i].second) == cudaSuccess) tot += t;
+  }
+  if (c->ev_used) *ms = tot / (double)c->ev_used;
+  if (count) *count = (int)c->ev_used;
+  c->ev_used = 0;
+  return COORD_OK;
+}
+
+int coord_set_timing(coord_ctx *c, int enable) {
+  if (!c) return COORD_ERR_ARG;
+  c->timing = enable != 0;
+  c->ev_used = 0;
+  return COORD_OK;
+}
+
+// multi-action batches: implemented in multi.cu
+} // extern "C"

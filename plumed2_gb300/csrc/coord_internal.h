@@ -1,0 +1,92 @@
+// coord_internal.h -- types shared by the host runtime and the sm_103a kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace coordgpu {
+
+// ---------------------------------------------------------------------------
+// Switching functions.  One struct carries every switch type's parameters,
+// laid out like switchContainers::Data (SwitchingFunction.h:57-95) so the
+// host set-up can follow SwitchingFunction::set() step by step.
+// ---------------------------------------------------------------------------
+enum SwitchType : int {
+  SW_NONE = 0,
+  SW_RATFIX,               // fixedRational<N>   (SwitchingFunction.cpp:185-216), N in nn
+  SW_RATIONAL,             // rational<standard, standard>
+  SW_RATIONAL_FAST,        // rational<fast, standard>
+  SW_RATIONAL_SIMPLE,      // rational<standard, simplified>
+  SW_RATIONAL_SIMPLE_FAST, // rational<fast, simplified>
+  SW_EXP,
+  SW_GAUSSIAN,
+  SW_FASTGAUSSIAN,
+  SW_SMAP,
+  SW_CUBIC,
+  SW_TANH,
+  SW_COSINUS,
+  SW_Q
+};
+
+struct SwitchParams {
+  int type;
+  int nn, mm, nnf, mmf;
+  int a, b;
+  double d0, dmax, dmax_2, invr0, invr0_2, stretch, shift;
+  double preRes, preDfunc, preSecDev, preDfuncF, preSecDevF;
+  double c, d;
+  double beta, lambda, ref;
+  double r0;               // 1/invr0 as given (for parameter gradients)
+  int r0_syntax;           // set(nn,mm,r0,d0): d_max depends on R_0 and D_0
+  int stretched;           // stretch/shift were set up
+};
+
+// Parses SWITCH={...} (SwitchingFunction::set(string), SwitchingFunction.cpp:
+// 1055-1159).  Returns 0 or writes a message into err.
+int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen);
+// The R_0/NN/MM/D_0 form (SwitchingFunction::set(nn,mm,r0,d0), :1176-1184).
+int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw);
+// Host-side evaluation (same code as the device FP64 evaluator).
+double switch_host_calculate(const SwitchParams &sw, double distance, double *dfunc);
+double switch_host_calculate_sqr(const SwitchParams &sw, double distance2, double *dfunc);
+
+// ---------------------------------------------------------------------------
+// Periodic boundary conditions (Pbc::setBox, Pbc.cpp:165-212).
+// ---------------------------------------------------------------------------
+enum PbcType : int { PBC_UNSET = 0, PBC_ORTHO = 1, PBC_GENERIC = 2 };
+
+struct PbcParams {
+  int type;
+  int nshift[8];
+  double box[9], invbox[9], reduced[9], invreduced[9];
+  double shift[8][18][3];
+};
+int pbc_setup(const double box[9], PbcParams *p);
+
+// ---------------------------------------------------------------------------
+// Neighbour-list geometry for one frame (computed on the host from the box).
+// ---------------------------------------------------------------------------
+struct GridParams {
+  int nc[3];          // cells per dimension
+  int ncells;
+  int wrap;           // 1: periodic cell indices
+  int use_scaled;     // bin on scaled coordinates (box given)
+  double lo[3];       // no-pbc bounding-box origin (device-computed when 0 box)
+  double inv_width[3];
+};
+
+// Per-frame constants read by the kernels (one record per frame on device).
+struct FrameConst {
+  PbcParams pbc;
+  GridParams grid;
+  double cut2;        // NL_CUTOFF^2 (classic test, NeighborList.cpp:238)
+  float  cut2_lo, cut2_hi; // FP32 prefilter band around cut2
+  // fixed-point frame of the mixed path: q = frac(x * inv_l) * 2^32
+  double inv_l[3];
+  float  scale[3];    // L / 2^32 per axis (FP32)
+  int    fixed_ok;    // box is orthorhombic (or none) so fixed point applies
+};
+
+// Pair modes (NeighborList::NNStyle, NeighborList.h:39).
+enum PairMode : int { MODE_SINGLE = 0, MODE_TWO = 1, MODE_PAIR = 2 };
+
+} // namespace coordgpu

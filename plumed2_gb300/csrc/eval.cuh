@@ -1,0 +1,356 @@
+// eval.cuh -- pair-evaluation kernels (forward: s, ds/dx, virial).
+#pragma once
+#include "kernels.cuh"
+
+namespace coordgpu {
+namespace {
+
+__device__ __forceinline__ void vir_sub(double v[kPartials], const double dd[3], const double d[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) v[1 + 3 * i + j] -= dd[i] * d[j];
+}
+
+// ---------------------------------------------------------------------------
+// neighbour list, FP64: one thread per row (rank), warp = slice
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const size_t fo = (size_t)f * a.ns;
+  double part[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  if (r < a.ns) {
+    const FrameConst &fc = a.fc[f];
+    const int len = a.row_len[fo + r];
+    const double4 xr4 = a.x64[fo + r];
+    const double xr[3] = {xr4.x, xr4.y, xr4.z};
+    double accr[3] = {0.0, 0.0, 0.0};
+    const uint32_t *e = a.ell + ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
+    for (int k = 0; k < len; k++) {
+      const uint32_t ent = __ldg(e + (size_t)k * 32);
+      const int p = (int)(ent & kRankMask);
+      const bool rfirst = (ent & kOrientBit) != 0;
+      const double4 xp4 = a.x64[fo + p];
+      const double xp[3] = {xp4.x, xp4.y, xp4.z};
+      double d[3], df;
+      const double sig = rfirst ? pair_fp64(sw, fc, a.do_pbc, xr, xp, d, df) : pair_fp64(sw, fc, a.do_pbc, xp, xr, d, df);
+      part[0] += sig;
+      const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+      double *accp = a.acc64 + (fo + p) * 3;
+      // deriv[first] -= dd; deriv[second] += dd  (CoordinationBase.cpp:196-206)
+      const double sgn = rfirst ? 1.0 : -1.0;
+      for (int q = 0; q < 3; q++) {
+        accr[q] -= sgn * dd[q];
+        atomicAdd(accp + q, sgn * dd[q]);
+      }
+      vir_sub(part, dd, d);
+    }
+    double *acc = a.acc64 + (fo + r) * 3;
+    for (int q = 0; q < 3; q++) atomicAdd(acc + q, accr[q]);
+  }
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// neighbour list, mixed: FP32 pair math from fixed-point positions, FP32
+// per-thread accumulation (Kahan for s), FP64 compensated block/grid sums.
+// NH = N/2 of fixedRational<N>; NH==0 evaluates any switch type in FP32.
+// ---------------------------------------------------------------------------
+template <int NH>
+__device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s, float r2, float &sig, float &df) {
+  if constexpr (NH > 0) {
+    const float x = r2 * s.invr0_2;
+    float xp = 1.0f;
+#pragma unroll
+    for (int i = 0; i < NH - 1; i++) xp *= x;
+    const float s0 = __frcp_rn(fmaf(xp, x, 1.0f));
+    sig = fmaf(s0, s.stretch, s.shift);
+    df = s.c * xp * s0 * s0;
+  } else {
+    VD<float> v = sw_calculate_sqr<float>(sw, r2);
+    sig = v.f;
+    df = v.d;
+  }
+}
+
+template <int NH>
+__global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const size_t fo = (size_t)f * a.ns;
+  float cv = 0.f, cvc = 0.f;
+  float vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
+  if (r < a.ns) {
+    const FrameConst &fc = a.fc[f];
+    const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+    const int len = a.row_len[fo + r];
+    const uint4 qr = a.q[fo + r];
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const uint32_t *e = a.ell + ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
+    for (int k = 0; k < len; k++) {
+      const uint32_t ent = __ldg(e + (size_t)k * 32);
+      const int p = (int)(ent & kRankMask);
+      const uint4 qp = __ldg(a.q + fo + p);
+      const float dx = fixed_delta(qr.x, qp.x, sx);
+      const float dy = fixed_delta(qr.y, qp.y, sy);
+      const float dz = fixed_delta(qr.z, qp.z, sz);
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (r2 <= s32.dmax2) {
+        float sig, df;
+        sw32<NH>(sw, s32, r2, sig, df);
+        // Kahan sum of s
+        const float yk = sig - cvc;
+        const float tk = cv + yk;
+        cvc = (tk - cv) - yk;
+        cv = tk;
+        const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+        ax -= ddx;
+        ay -= ddy;
+        az -= ddz;
+        atomicAdd(a.acc32 + fo + p, make_float4(ddx, ddy, ddz, 0.f));
+        vxx = fmaf(-ddx, dx, vxx);
+        vyy = fmaf(-ddy, dy, vyy);
+        vzz = fmaf(-ddz, dz, vzz);
+        vxy = fmaf(-ddx, dy, vxy);
+        vxz = fmaf(-ddx, dz, vxz);
+        vyz = fmaf(-ddy, dz, vyz);
+      }
+    }
+    if (len > 0) atomicAdd(a.acc32 + fo + r, make_float4(ax, ay, az, 0.f));
+  }
+  double part[kPartials] = {(double)cv - (double)cvc, (double)vxx, (double)vxy, (double)vxz, (double)vxy,
+                            (double)vyy, (double)vyz, (double)vxz, (double)vyz, (double)vzz, 0.0, 0.0};
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// every pair (no NLIST): tiles of TILE i-slots against TILE j-slots.  The
+// j-side derivatives accumulate in shared memory with a staggered j order
+// (thread t visits j = (t+step) mod TILE) so no two threads hit the same
+// address in the same step.  Single list: tiles (I,J), J>=I, j>i inside a
+// diagonal tile; two lists: A tiles x B tiles.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tile_pair(int t, int nTi, int nTj, bool tri, int &I, int &J) {
+  if (!tri) {
+    I = t / nTj;
+    J = t % nTj;
+    return;
+  }
+  int i = 0, rem = t;
+  while (rem >= nTi - i) {
+    rem -= nTi - i;
+    i++;
+  }
+  I = i;
+  J = i + rem;
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, int nTi, int nTj, int ntp) {
+  const int f = blockIdx.z;
+  const bool tri = a.mode == MODE_SINGLE;
+  const int iend = tri ? a.ns : a.nA, jbase0 = tri ? 0 : a.nA, jend = a.ns;
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  __shared__ double xj[TILE][3];
+  __shared__ double accj[TILE][3];
+  __shared__ long long absj[TILE];
+  double part[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  for (int t = blockIdx.x; t < ntp; t += gridDim.x) {
+    int I, J;
+    tile_pair(t, nTi, nTj, tri, I, J);
+    const int i = I * TILE + threadIdx.x;
+    const int jb = jbase0 + J * TILE;
+    __syncthreads();
+    {
+      const int j = jb + threadIdx.x;
+      if (j < jend) {
+        const double *p = a.pos + (fo + j) * 3;
+        xj[threadIdx.x][0] = p[0];
+        xj[threadIdx.x][1] = p[1];
+        xj[threadIdx.x][2] = p[2];
+        absj[threadIdx.x] = a.abs_of_slot[j];
+      }
+      accj[threadIdx.x][0] = accj[threadIdx.x][1] = accj[threadIdx.x][2] = 0.0;
+    }
+    __syncthreads();
+    double acci[3] = {0.0, 0.0, 0.0};
+    if (i < iend) {
+      const double *pi = a.pos + (fo + i) * 3;
+      const double xi[3] = {pi[0], pi[1], pi[2]};
+      const long long absi = a.abs_of_slot[i];
+      const bool diag = tri && (I == J);
+      for (int s = 0; s < TILE; s++) {
+        const int jl = (threadIdx.x + s) & (TILE - 1);
+        const int j = jb + jl;
+        if (j >= jend || (diag && jl <= (int)threadIdx.x) || absj[jl] == absi) continue;
+        double d[3], df;
+        const double xjj[3] = {xj[jl][0], xj[jl][1], xj[jl][2]};
+        const double sig = pair_fp64(sw, fc, a.do_pbc, xi, xjj, d, df);
+        part[0] += sig;
+        const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+        for (int q = 0; q < 3; q++) {
+          acci[q] -= dd[q];
+          if (dd[q] != 0.0) atomicAdd(&accj[jl][q], dd[q]);
+        }
+        vir_sub(part, dd, d);
+      }
+      for (int q = 0; q < 3; q++)
+        if (acci[q] != 0.0) atomicAdd(a.acc64 + (fo + i) * 3 + q, acci[q]);
+    }
+    __syncthreads();
+    {
+      const int j = jb + threadIdx.x;
+      if (j < jend)
+        for (int q = 0; q < 3; q++)
+          if (accj[threadIdx.x][q] != 0.0) atomicAdd(a.acc64 + (fo + j) * 3 + q, accj[threadIdx.x][q]);
+    }
+  }
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+template <int TILE, int NH>
+__global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int nTi, int nTj,
+                                                     int ntp) {
+  const int f = blockIdx.z;
+  const bool tri = a.mode == MODE_SINGLE;
+  const int iend = tri ? a.ns : a.nA, jbase0 = tri ? 0 : a.nA, jend = a.ns;
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  __shared__ uint4 qj[TILE];
+  __shared__ float accj[TILE][3];
+  __shared__ long long absj[TILE];
+  float cv = 0.f, cvc = 0.f, vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
+  for (int t = blockIdx.x; t < ntp; t += gridDim.x) {
+    int I, J;
+    tile_pair(t, nTi, nTj, tri, I, J);
+    const int i = I * TILE + threadIdx.x;
+    const int jb = jbase0 + J * TILE;
+    __syncthreads();
+    {
+      const int j = jb + threadIdx.x;
+      if (j < jend) {
+        qj[threadIdx.x] = a.q[fo + j];
+        absj[threadIdx.x] = a.abs_of_slot[j];
+      }
+      accj[threadIdx.x][0] = accj[threadIdx.x][1] = accj[threadIdx.x][2] = 0.f;
+    }
+    __syncthreads();
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (i < iend) {
+      const uint4 qi = a.q[fo + i];
+      const long long absi = a.abs_of_slot[i];
+      const bool diag = tri && (I == J);
+      for (int s = 0; s < TILE; s++) {
+        const int jl = (threadIdx.x + s) & (TILE - 1);
+        const int j = jb + jl;
+        if (j >= jend || (diag && jl <= (int)threadIdx.x) || absj[jl] == absi) continue;
+        const uint4 qp = qj[jl];
+        const float dx = fixed_delta(qi.x, qp.x, sx), dy = fixed_delta(qi.y, qp.y, sy),
+                    dz = fixed_delta(qi.z, qp.z, sz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (r2 <= s32.dmax2) {
+          float sig, df;
+          sw32<NH>(sw, s32, r2, sig, df);
+          const float yk = sig - cvc;
+          const float tk = cv + yk;
+          cvc = (tk - cv) - yk;
+          cv = tk;
+          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+          ax -= ddx;
+          ay -= ddy;
+          az -= ddz;
+          atomicAdd(&accj[jl][0], ddx);
+          atomicAdd(&accj[jl][1], ddy);
+          atomicAdd(&accj[jl][2], ddz);
+          vxx = fmaf(-ddx, dx, vxx);
+          vyy = fmaf(-ddy, dy, vyy);
+          vzz = fmaf(-ddz, dz, vzz);
+          vxy = fmaf(-ddx, dy, vxy);
+          vxz = fmaf(-ddx, dz, vxz);
+          vyz = fmaf(-ddy, dz, vyz);
+        }
+      }
+      if (ax != 0.f || ay != 0.f || az != 0.f) atomicAdd(a.acc32 + fo + i, make_float4(ax, ay, az, 0.f));
+    }
+    __syncthreads();
+    {
+      const int j = jb + threadIdx.x;
+      const float *v = accj[threadIdx.x];
+      if (j < jend && (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f))
+        atomicAdd(a.acc32 + fo + j, make_float4(v[0], v[1], v[2], 0.f));
+    }
+  }
+  double part[kPartials] = {(double)cv - (double)cvc, (double)vxx, (double)vxy, (double)vxz, (double)vxy,
+                            (double)vyy, (double)vyz, (double)vxz, (double)vyz, (double)vzz, 0.0, 0.0};
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// PAIR: pair i is (slot i, slot i+nA); every slot belongs to one pair, so
+// derivatives are written without atomics.  With NLIST only flagged pairs.
+// ---------------------------------------------------------------------------
+__global__ void k_pairs64(KArgs a, SwitchParams sw, int use_flags) {
+  const int f = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t fo = (size_t)f * a.ns;
+  double part[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  if (i < a.nA && (!use_flags || a.pair_flag[(size_t)f * a.nA + i]) && a.abs_of_slot[i] != a.abs_of_slot[i + a.nA]) {
+    const double *p0 = a.pos + (fo + i) * 3, *p1 = a.pos + (fo + i + a.nA) * 3;
+    const double v1[3] = {p0[0], p0[1], p0[2]}, v2[3] = {p1[0], p1[1], p1[2]};
+    double d[3], df;
+    part[0] = pair_fp64(sw, a.fc[f], a.do_pbc, v1, v2, d, df);
+    const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+    for (int q = 0; q < 3; q++) {
+      a.acc64[(fo + i) * 3 + q] -= dd[q];
+      a.acc64[(fo + i + a.nA) * 3 + q] += dd[q];
+    }
+    vir_sub(part, dd, d);
+  }
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+template <int NH> __global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int use_flags) {
+  const int f = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t fo = (size_t)f * a.ns;
+  double part[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  if (i < a.nA && (!use_flags || a.pair_flag[(size_t)f * a.nA + i]) && a.abs_of_slot[i] != a.abs_of_slot[i + a.nA]) {
+    const FrameConst &fc = a.fc[f];
+    const uint4 q0 = a.q[fo + i], q1 = a.q[fo + i + a.nA];
+    const float dx = fixed_delta(q0.x, q1.x, fc.scale[0]), dy = fixed_delta(q0.y, q1.y, fc.scale[1]),
+                dz = fixed_delta(q0.z, q1.z, fc.scale[2]);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 <= s32.dmax2) {
+      float sig, df;
+      sw32<NH>(sw, s32, r2, sig, df);
+      const float dd[3] = {df * dx, df * dy, df * dz}, d[3] = {dx, dy, dz};
+      part[0] = sig;
+      float4 &a0 = a.acc32[fo + i], &a1 = a.acc32[fo + i + a.nA];
+      a0.x -= dd[0];
+      a0.y -= dd[1];
+      a0.z -= dd[2];
+      a1.x += dd[0];
+      a1.y += dd[1];
+      a1.z += dd[2];
+      for (int x = 0; x < 3; x++)
+        for (int y = 0; y < 3; y++) part[1 + 3 * x + y] = -(double)dd[x] * (double)d[y];
+    }
+  }
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+} // namespace
+} // namespace coordgpu

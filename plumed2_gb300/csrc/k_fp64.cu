@@ -1,0 +1,73 @@
+// k_fp64.cu -- neighbour-list build and FP64 pair kernels.
+// Compiled with -fmad=false: every FP64 expression keeps the reference's
+// rounding (no fused multiply-add), which the exact cutoff test and the
+// bit-level parity of per-pair values rely on.
+#include "launch.h"
+#include "eval.cuh"
+
+namespace coordgpu {
+
+std::atomic<long long> g_launches{0};
+
+static inline dim3 grid1(int n, int block, int frames) { return dim3((n + block - 1) / block > 0 ? (n + block - 1) / block : 1, frames); }
+
+void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int linkcells, cudaStream_t s) {
+  const int blocks = std::max(1, std::min(1024, (a.ns + 255) / 256));
+  k_bounds<<<dim3(blocks, a.nframes), 256, 0, s>>>(a, mm);
+  k_bounds_finish<<<(a.nframes + 63) / 64, 64, 0, s>>>(a, mm, cutoff, linkcells);
+  g_launches += 2;
+}
+
+void launch_nl_build(const KArgs &a, cudaStream_t s) {
+  cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)a.ncell_cap * a.nframes, s);
+  k_bin<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
+  k_scan_cells<<<a.nframes, 1024, 0, s>>>(a);
+  k_scatter<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
+  k_cell_sort<<<dim3(std::min(a.ncell_cap, 65535), a.nframes), 64, 0, s>>>(a);
+  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1);
+  k_nl_search<<<grid1(a.ns, 128, a.nframes), 128, 0, s>>>(a);
+  g_launches += 6;
+}
+
+void launch_pair_flags(const KArgs &a, cudaStream_t s) {
+  k_pair_flags<<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a);
+  g_launches += 1;
+}
+
+void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s) {
+  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order, want64, wantq);
+  g_launches += 1;
+}
+
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, cudaStream_t s) {
+  k_eval_nl64<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw);
+  g_launches += 1;
+}
+
+void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int tile, int nblocks, cudaStream_t s) {
+  const bool tri = a.mode == MODE_SINGLE;
+  const int ni = tri ? a.ns : a.nA, nj = tri ? a.ns : a.ns - a.nA;
+  const int nTi = (ni + tile - 1) / tile, nTj = (nj + tile - 1) / tile;
+  const long long ntp = tri ? (long long)nTi * (nTi + 1) / 2 : (long long)nTi * nTj;
+  const int nb = (int)std::max(1ll, std::min<long long>(ntp, nblocks));
+  dim3 g(nb, 1, a.nframes);
+  switch (tile) {
+  case 32: k_allpairs64<32><<<g, 32, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
+  case 64: k_allpairs64<64><<<g, 64, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
+  case 256: k_allpairs64<256><<<g, 256, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
+  default: k_allpairs64<128><<<g, 128, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
+  }
+  g_launches += 1;
+}
+
+void launch_pairs64(const KArgs &a, const SwitchParams &sw, int use_flags, cudaStream_t s) {
+  k_pairs64<<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, use_flags);
+  g_launches += 1;
+}
+
+void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s) {
+  k_finalize64<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order);
+  g_launches += 1;
+}
+
+} // namespace coordgpu

@@ -1,0 +1,59 @@
+// kargs.h -- kernel argument records shared by the launchers and the host runtime.
+#pragma once
+#include "coord_internal.h"
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace coordgpu {
+
+constexpr int kPartials = 12;  // s, virial[9], ds/dR0, ds/dD0
+constexpr uint32_t kOrientBit = 0x80000000u;
+constexpr uint32_t kRankMask = 0x7fffffffu;
+
+struct KArgs {
+  int nframes;
+  int ns;         // slots per frame
+  int nA;         // slots in GROUPA (== ns for a single list)
+  int mode;       // PairMode
+  int do_pbc;     // !NOPBC
+  int nl_kind;    // COORD_NL_* (1 classic, 2 cells)
+  int cap;        // neighbour-list row capacity (entries per row)
+  int ncell_cap;  // cells per frame (allocation)
+  int self_cap;   // self-pair list capacity per frame
+  int nslices;    // ceil(ns/32)
+  int flags;      // COORD_FLAG_* of the call
+  FrameConst *fc;               // [nframes]
+  const int64_t *abs_of_slot;   // [ns]
+  const double *pos;            // [nframes][ns][3]   input, slot order
+  int *cell_of_slot;            // [nframes][ns]
+  int *cell_count;              // [nframes][ncell_cap]
+  int *cell_start;              // [nframes][ncell_cap+1]
+  int *cell_fill;               // [nframes][ncell_cap]
+  int *slot_of_rank;            // [nframes][ns]
+  int *scatter_tmp;             // [nframes][ns]
+  double4 *x64;                 // [nframes][ns] sorted (or slot-order) FP64 positions
+  uint4 *q;                     // [nframes][ns] fixed-point positions
+  uint32_t *ell;                // [nframes][nslices*cap*32]
+  int *row_len;                 // [nframes][ns]
+  int *slice_w;                 // [nframes][nslices]
+  unsigned long long *nl_count; // [nframes][4]: pairs, self pairs, max row length, geometry error
+  uint32_t *self_pairs;         // [nframes][self_cap][2]
+  unsigned char *pair_flag;     // [nframes][nA] PAIR-mode neighbour flags
+  double *acc64;                // [nframes][ns][3] derivative accumulators (FP64 path)
+  float4 *acc32;                // [nframes][ns]    derivative accumulators (mixed path)
+  double *partials;             // [nframes][max_blocks][kPartials]
+  int max_blocks;
+  unsigned *tickets;            // [nframes]
+  double *out_s;                // [nframes]
+  double *out_deriv;            // [nframes][ns][3] slot order
+  double *out_virial;           // [nframes][9]
+  double *out_dparam;           // [nframes][2]
+  const double *g;              // [nframes] upstream dV/ds (backward)
+};
+
+// FP32 parameters of a fixedRational<2*NH> switch (mixed path).
+struct SwitchF32 {
+  float dmax2, invr0_2, stretch, shift, c;  // c = -NH * 2*invr0^2 * stretch
+};
+
+} // namespace coordgpu

@@ -1,0 +1,569 @@
+// kernels.cuh -- sm_103a kernels of the COORDINATION hot path.
+//
+// Included by two translation units:
+//   k_fp64.cu   compiled with -fmad=false: neighbour-list build (the exact
+//               FP64 cutoff test must not be contracted) and the FP64 pair
+//               kernels, whose per-pair arithmetic repeats the reference's
+//               operations in order (Pbc::distance + modulo2 +
+//               SwitchingFunction::calculateSqr, CoordinationBase.cpp:187-206)
+//   k_mixed.cu  FP32 pair kernels (FMA allowed) with compensated FP64 sums
+//
+// Data layout (per frame f; frames = walkers or trajectory frames):
+//   slots     GROUPA then GROUPB, the order positions arrive in
+//   ranks     slots sorted by neighbour-list cell (x fastest) and, inside a
+//             cell, by slot index: spatially coherent rows for the pair kernels
+//   ell       neighbour list as a sliced ELL: 32 consecutive ranks form a
+//             slice (one warp); entry k of lane l sits at
+//             ell[(slice*cap + k)*32 + l]; bits 0-30 partner rank, bit 31 set
+//             when the row atom is the first atom of the pair in the
+//             reference's orientation (NeighborList.cpp:158-163,252-266).
+//             Each pair is stored once (half list), owned by the lower rank
+//             when ranks sum to even, else by the higher (balanced rows).
+//   q         mixed path positions as 32-bit fixed-point fractions of the box
+//             (orthorhombic) or of a bounding frame (no pbc): differences
+//             wrap modulo 2^32, which is exactly the minimum image.
+#pragma once
+#include "coord_internal.h"
+#include "switch_eval.cuh"
+#include "kargs.h"
+#include <cstdint>
+
+namespace coordgpu {
+
+namespace {  // kernels have internal linkage: each .cu instantiates what it launches
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-reduces kPartials doubles (one set per thread), writes the block's
+// record, and lets the last block of the frame (atomic ticket, no waiting)
+// sum all records in block order with Kahan compensation.  The final values
+// land in out_s / out_virial / out_dparam of the frame.
+__device__ void block_partials_finish(const KArgs &a, int frame, double v[kPartials], int nblocks_frame) {
+  __shared__ double red[kPartials][32];
+  __shared__ bool is_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) {
+    double w = warp_sum(v[k]);
+    if (lane == 0) red[k][warp] = w;
+  }
+  __syncthreads();
+  double *rec = a.partials + ((size_t)frame * a.max_blocks + blockIdx.x) * kPartials;
+  if (threadIdx.x < kPartials) {
+    double s = 0.0;
+    for (int w = 0; w < nwarps; w++) s += red[threadIdx.x][w];
+    rec[threadIdx.x] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(&a.tickets[frame], 1u);
+    is_last = (t == (unsigned)nblocks_frame - 1u);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (threadIdx.x < kPartials) {
+    const double *base = a.partials + (size_t)frame * a.max_blocks * kPartials;
+    double s = 0.0, c = 0.0;  // Kahan-Babuska (Neumaier) compensated sum
+    for (int b = 0; b < nblocks_frame; b++) {
+      const double x = __ldcg(base + (size_t)b * kPartials + threadIdx.x);
+      const double t = s + x;
+      c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+      s = t;
+    }
+    s += c;
+    const int k = threadIdx.x;
+    if (k == 0) {
+      if (a.out_s) a.out_s[frame] = s;
+    } else if (k <= 9) {
+      if (a.out_virial) a.out_virial[(size_t)frame * 9 + (k - 1)] = s;
+    } else {
+      if (a.out_dparam) a.out_dparam[(size_t)frame * 2 + (k - 10)] = s;
+    }
+  }
+  if (threadIdx.x == 0) a.tickets[frame] = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// fixed-point positions (mixed path and the FP32 neighbour-list prefilter)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t to_fixed(double x, double lo, double inv_l) {
+  double f = (x - lo) * inv_l;
+  f = f - floor(f);
+  const long long v = __double2ll_rn(f * 4294967296.0);
+  return (uint32_t)(v & 0xffffffffll);
+}
+__device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x) {
+  return make_uint4(to_fixed(x[0], fc.grid.lo[0], fc.inv_l[0]), to_fixed(x[1], fc.grid.lo[1], fc.inv_l[1]),
+                    to_fixed(x[2], fc.grid.lo[2], fc.inv_l[2]), 0u);
+}
+__device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float scale) {
+  return (float)(int)(b - a) * scale;  // wraps modulo 2^32: minimum image
+}
+
+// ---------------------------------------------------------------------------
+// cells: binning, scan, scatter, per-cell ordering
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cell_index_of(const FrameConst &fc, const double *x, int nl_kind, int do_pbc) {
+  const GridParams &g = fc.grid;
+  int c[3];
+  if (nl_kind == 2) {
+    // LinkCells::findMyCell (LinkCells.cpp:255-266): scaled coordinates of
+    // (x - origin) through invBox^T, then floor((pbc(s)+0.5)*n).
+    double xm[3] = {x[0] - g.lo[0], x[1] - g.lo[1], x[2] - g.lo[2]};
+    const double *ib = fc.pbc.invbox;
+    for (int i = 0; i < 3; i++) {
+      double s = 0.0;
+      for (int j = 0; j < 3; j++) s += ib[j * 3 + i] * xm[j];
+      int ci = (int)floor((tools_pbc(s) + 0.5) * g.nc[i]);
+      c[i] = min(max(ci, 0), g.nc[i] - 1);
+    }
+  } else if (g.wrap) {
+    for (int k = 0; k < 3; k++) {
+      double f = x[k] * fc.pbc.invbox[4 * k];
+      f = f - floor(f);
+      c[k] = min(max((int)(f * g.nc[k]), 0), g.nc[k] - 1);
+    }
+  } else {
+    for (int k = 0; k < 3; k++) {
+      const double f = (x[k] - g.lo[k]) * g.inv_width[k];
+      c[k] = min(max((int)floor(f * g.nc[k]), 0), g.nc[k] - 1);
+    }
+  }
+  (void)do_pbc;
+  return (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+}
+
+// min/max of positions per frame (no-pbc bounding frames)
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+  unsigned long long b = __double_as_longlong(v);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_ordered(unsigned long long b) {
+  b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
+  return __longlong_as_double(b);
+}
+
+__global__ void k_bounds(KArgs a, unsigned long long *mm /*[nframes][6]*/) {
+  const int f = blockIdx.y;
+  const double *pos = a.pos + (size_t)f * a.ns * 3;
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.ns; s += gridDim.x * blockDim.x)
+    for (int k = 0; k < 3; k++) {
+      unsigned long long b = ordered_bits(pos[3 * (size_t)s + k]);
+      lo[k] = min(lo[k], b);
+      hi[k] = max(hi[k], b);
+    }
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = min(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+      hi[k] = max(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 3; k++) {
+      atomicMin(&mm[f * 6 + k], lo[k]);
+      atomicMax(&mm[f * 6 + 3 + k], hi[k]);
+    }
+}
+
+// Completes the no-pbc frame of every frame: bounding-box origin and widths
+// for binning and the fixed-point frame; cell counts bounded by ncell_cap.
+// For NLISTCELLS this is LinkCells::setupCells(pos) (LinkCells.cpp:48-68).
+__global__ void k_bounds_finish(KArgs a, const unsigned long long *mm, double cutoff, int linkcells) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.nframes) return;
+  FrameConst &fc = a.fc[f];
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; k++) {
+    lo[k] = from_ordered(mm[f * 6 + k]);
+    hi[k] = from_ordered(mm[f * 6 + 3 + k]);
+    if (a.ns == 0) lo[k] = hi[k] = 0.0;
+  }
+  if (linkcells) {
+    double box[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+      if (cutoff < 1.3407807929942596e154)
+        box[4 * k] = cutoff * (1 + ceil((hi[k] - lo[k]) / cutoff));
+      else
+        box[4 * k] = hi[k] - lo[k] + 1;
+      fc.grid.lo[k] = (lo[k] + hi[k]) / 2;
+    }
+    // Pbc::setBox of the diagonal bounding box: invBox = inverse(box)
+    const double det = box[0] * box[4] * box[8];
+    const double invdet = 1.0 / det;
+    for (int i = 0; i < 9; i++) fc.pbc.invbox[i] = 0.0;
+    fc.pbc.invbox[0] = invdet * (box[4] * box[8]);
+    fc.pbc.invbox[4] = invdet * (box[0] * box[8]);
+    fc.pbc.invbox[8] = invdet * (box[0] * box[4]);
+    long long ncell = 1;
+    for (int k = 0; k < 3; k++) {
+      const double r = fc.pbc.invbox[4 * k];
+      int n = (int)floor(1.0 / sqrt(r * r) / cutoff);
+      if (n == 0) n = 1;
+      fc.grid.nc[k] = n;
+      ncell *= n;
+    }
+    if (ncell > a.ncell_cap) {
+      // more link cells than were allocated: report instead of binning
+      fc.grid.ncells = 0;
+      a.nl_count[f * 4 + 3] = 1ull;
+    } else {
+      fc.grid.ncells = (int)ncell;
+    }
+  } else {
+    int nc[3];
+    double width[3];
+    for (int k = 0; k < 3; k++) {
+      width[k] = (hi[k] - lo[k]) > 0 ? (hi[k] - lo[k]) : 1.0;
+      double n = floor(width[k] / (cutoff * (1.0 + 1e-9)));
+      nc[k] = (int)fmin(fmax(n, 1.0), 1024.0);
+    }
+    while ((long long)nc[0] * nc[1] * nc[2] > a.ncell_cap) {
+      int kmax = (nc[0] >= nc[1] && nc[0] >= nc[2]) ? 0 : (nc[1] >= nc[2] ? 1 : 2);
+      nc[kmax] = max(1, nc[kmax] / 2);
+    }
+    for (int k = 0; k < 3; k++) {
+      fc.grid.nc[k] = nc[k];
+      fc.grid.lo[k] = lo[k];
+      fc.grid.inv_width[k] = 1.0 / width[k];
+    }
+    fc.grid.ncells = nc[0] * nc[1] * nc[2];
+  }
+  // fixed-point frame: twice the span so differences never wrap.  With
+  // NLISTCELLS grid.lo stays the LinkCells origin (the box centre); the
+  // fixed-point differences are modular, so any origin works.
+  double spanmax = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double span = fmax(hi[k] - lo[k], 1e-3) * 2.0 + 1e-3;
+    if (!linkcells) fc.grid.lo[k] = lo[k];
+    fc.inv_l[k] = 1.0 / span;
+    fc.scale[k] = (float)(span / 4294967296.0);
+    spanmax = fmax(spanmax, span);
+  }
+  // FP32 prefilter band around cutoff^2 (covers quantisation and rounding)
+  const double band = 1e-4 * fc.cut2 + 8.0 * cutoff * spanmax / 4294967296.0 + 1e-12;
+  fc.cut2_lo = (float)(fc.cut2 - band);
+  fc.cut2_hi = (float)(fc.cut2 + band);
+}
+
+__global__ void k_bin(KArgs a) {
+  const int f = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  const FrameConst &fc = a.fc[f];
+  if (fc.grid.ncells <= 0 || fc.grid.ncells > a.ncell_cap) return;
+  const int c = cell_index_of(fc, a.pos + ((size_t)f * a.ns + s) * 3, a.nl_kind, a.do_pbc);
+  a.cell_of_slot[(size_t)f * a.ns + s] = c;
+  atomicAdd(&a.cell_count[(size_t)f * a.ncell_cap + c], 1);
+}
+
+// exclusive scan of the cell counts, one block per frame
+__global__ void k_scan_cells(KArgs a) {
+  const int f = blockIdx.x;
+  const int n = min(max(a.fc[f].grid.ncells, 0), a.ncell_cap);
+  int *cnt = a.cell_count + (size_t)f * a.ncell_cap;
+  int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
+  int *fill = a.cell_fill + (size_t)f * a.ncell_cap;
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(lo + per, n);
+  int local = 0;
+  for (int i = lo; i < hi; i++) local += cnt[i];
+  // block exclusive scan of 'local'
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int v = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    warp_tot[lane] = v;
+  }
+  __syncthreads();
+  int run = incl - local + (warp > 0 ? warp_tot[warp - 1] : 0);
+  for (int i = lo; i < hi; i++) {
+    start[i] = run;
+    run += cnt[i];
+    cnt[i] = 0;  // reset for the next build
+    fill[i] = 0;
+  }
+  if (threadIdx.x == blockDim.x - 1) start[n] = run;
+}
+
+__global__ void k_scatter(KArgs a) {
+  const int f = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  if (a.fc[f].grid.ncells <= 0) return;
+  const int c = a.cell_of_slot[(size_t)f * a.ns + s];
+  const int p = a.cell_start[(size_t)f * (a.ncell_cap + 1) + c] + atomicAdd(&a.cell_fill[(size_t)f * a.ncell_cap + c], 1);
+  if (p < a.ns) a.scatter_tmp[(size_t)f * a.ns + p] = s;
+}
+
+// Orders each cell's members by slot index (rank = number of smaller
+// members), which makes the sorted order independent of atomic timing.
+__global__ void k_cell_sort(KArgs a) {
+  const int f = blockIdx.y;
+  const int n = min(max(a.fc[f].grid.ncells, 0), a.ncell_cap);
+  const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
+  const int *tmp = a.scatter_tmp + (size_t)f * a.ns;
+  int *out = a.slot_of_rank + (size_t)f * a.ns;
+  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    const int b = start[c], m = start[c + 1] - b;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      const int v = tmp[b + i];
+      int r = 0;
+      for (int j = 0; j < m; j++) r += (tmp[b + j] < v);
+      out[b + r] = v;
+    }
+  }
+}
+
+// FP64 positions in rank order (and the fixed-point copy for the NL prefilter
+// and the mixed kernels).  rank_order==0: slot order.
+__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.ns) return;
+  const int s = rank_order ? a.slot_of_rank[(size_t)f * a.ns + r] : r;
+  const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
+  const double x0 = x[0], x1 = x[1], x2 = x[2];
+  if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, 0.0);
+  if (wantq) {
+    const double xx[3] = {x0, x1, x2};
+    a.q[(size_t)f * a.ns + r] = fixed_of(a.fc[f], xx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// neighbour-list search: one thread per row (rank); exact pair set
+// ---------------------------------------------------------------------------
+// The cells a cell must look at: LinkCells::addRequiredCells
+// (LinkCells.cpp:184-231) -- with at least 3 cells per periodic dimension
+// this is the 27-cell stencil; with fewer, duplicates are avoided by the
+// same min/max rules the reference uses.
+__device__ __forceinline__ void cell_range(int c, int n, int wrap, int &lo, int &hi) {
+  lo = c + ((n < 2) ? 0 : -1);
+  hi = c + ((n < 3 && wrap) ? 1 : 2);
+  if (!wrap) {
+    lo = max(lo, 0);
+    hi = min(hi, n);
+  }
+}
+__device__ __forceinline__ int wrap_cell(int v, int n) { return (v < 0) ? n - 1 : v % n; }
+
+__global__ void k_nl_search(KArgs a) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool active = r < a.ns;
+  const FrameConst &fc = a.fc[f];
+  const GridParams &g = fc.grid;
+  const size_t fo = (size_t)f * a.ns;
+  const int *slot_of_rank = a.slot_of_rank + fo;
+  const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
+  int n = 0;
+  unsigned long long nself = 0;
+  if (active && g.ncells > 0) {
+    const int sr = slot_of_rank[r];
+    const bool ra = sr < a.nA;
+    const int cr = a.cell_of_slot[fo + sr];
+    const int cx = cr % g.nc[0], cy = (cr / g.nc[0]) % g.nc[1], cz = cr / (g.nc[0] * g.nc[1]);
+    const double4 xr4 = a.x64[fo + r];
+    const uint4 qr = a.q[fo + r];
+    const int64_t absr = a.abs_of_slot[sr];
+    const int cwrap = (a.nl_kind == 2) ? a.do_pbc : g.wrap;
+    int x0, x1, y0, y1, z0, z1;
+    cell_range(cx, g.nc[0], cwrap, x0, x1);
+    cell_range(cy, g.nc[1], cwrap, y0, y1);
+    cell_range(cz, g.nc[2], cwrap, z0, z1);
+    const size_t slice_base = ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
+    for (int nx = x0; nx < x1; ++nx)
+      for (int ny = y0; ny < y1; ++ny)
+        for (int nz = z0; nz < z1; ++nz) {
+          const int c = wrap_cell(nx, g.nc[0]) + wrap_cell(ny, g.nc[1]) * g.nc[0] +
+                        wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
+          const int pe = start[c + 1];
+          for (int p = start[c]; p < pe; p++) {
+            if (p == r) continue;
+            // ownership: even rank sum -> lower rank, odd -> higher rank
+            const bool own = ((r + p) & 1) ? (r > p) : (r < p);
+            if (!own) continue;
+            const int sp = slot_of_rank[p];
+            bool r_first;
+            if (a.mode == MODE_TWO) {
+              if (ra == (sp < a.nA)) continue;
+              r_first = ra;
+            } else {
+              r_first = sr < sp;
+            }
+            bool accept;
+            if (a.nl_kind == 2) {
+              accept = true;  // NLISTCELLS: every pair of neighbouring cells (NeighborList.cpp:194-231)
+            } else {
+              accept = false;
+              bool exact = true;
+              if (fc.fixed_ok) {
+                const uint4 qp = a.q[fo + p];
+                const float dx = fixed_delta(qr.x, qp.x, fc.scale[0]);
+                const float dy = fixed_delta(qr.y, qp.y, fc.scale[1]);
+                const float dz = fixed_delta(qr.z, qp.z, fc.scale[2]);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 > fc.cut2_hi) {
+                  exact = false;
+                } else if (r2 < fc.cut2_lo) {
+                  exact = false;
+                  accept = true;
+                }
+              }
+              if (exact) {
+                // the reference's own test: modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
+                const double4 xp4 = a.x64[fo + p];
+                const double va[3] = {xr4.x, xr4.y, xr4.z}, vb[3] = {xp4.x, xp4.y, xp4.z};
+                double d[3];
+                const double *v1 = r_first ? va : vb, *v2 = r_first ? vb : va;
+                if (a.do_pbc)
+                  pbc_distance(fc.pbc, v1, v2, d);
+                else
+                  for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+                accept = mod2(d) <= fc.cut2;
+              }
+            }
+            if (!accept) continue;
+            if (a.abs_of_slot[sp] == absr) {
+              // a self pair: counted in the list size, skipped by the CV loop
+              // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
+              unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
+              if (k < (unsigned long long)a.self_cap) {
+                a.self_pairs[((size_t)f * a.self_cap + k) * 2] = r_first ? sr : sp;
+                a.self_pairs[((size_t)f * a.self_cap + k) * 2 + 1] = r_first ? sp : sr;
+              }
+              nself++;
+              continue;
+            }
+            if (n < a.cap) a.ell[slice_base + (size_t)n * 32] = (uint32_t)p | (r_first ? kOrientBit : 0u);
+            n++;
+          }
+        }
+    a.row_len[fo + r] = min(n, a.cap);
+  }
+  // per-warp bookkeeping: slice width, list size, overflow
+  const int wmax = warp_max(active ? n : 0);
+  unsigned long long tot = active ? (unsigned long long)n : 0ull;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  (void)nself;
+  if (lane == 0 && (r >> 5) < a.nslices) {
+    a.slice_w[(size_t)f * a.nslices + (r >> 5)] = min(wmax, a.cap);
+    atomicAdd(&a.nl_count[f * 4 + 0], tot);
+    if (wmax > a.cap) atomicMax(&a.nl_count[f * 4 + 2], (unsigned long long)wmax);
+  }
+}
+
+// PAIR mode list: pair i kept when |d(i, i+nA)| <= cutoff (NeighborList.cpp:150-152,252-266)
+__global__ void k_pair_flags(KArgs a) {
+  const int f = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nA) return;
+  const FrameConst &fc = a.fc[f];
+  const double *p0 = a.pos + ((size_t)f * a.ns + i) * 3;
+  const double *p1 = a.pos + ((size_t)f * a.ns + i + a.nA) * 3;
+  double d[3];
+  if (a.do_pbc)
+    pbc_distance(fc.pbc, p0, p1, d);
+  else
+    for (int k = 0; k < 3; k++) d[k] = p1[k] - p0[k];
+  const bool keep = mod2(d) <= fc.cut2;
+  a.pair_flag[(size_t)f * a.nA + i] = keep ? 1 : 0;
+  unsigned long long c = keep ? 1ull : 0ull;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&a.nl_count[f * 4 + 0], c);
+}
+
+// ---------------------------------------------------------------------------
+// finalize: sorted/slot accumulators -> FP64 derivatives in slot order; the
+// accumulators are zeroed for the next step.
+// ---------------------------------------------------------------------------
+__global__ void k_finalize64(KArgs a, int rank_order) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.ns) return;
+  const size_t fo = (size_t)f * a.ns;
+  const int s = rank_order ? a.slot_of_rank[fo + r] : r;
+  double *acc = a.acc64 + (fo + r) * 3;
+  if (a.out_deriv) {
+    double *o = a.out_deriv + (fo + s) * 3;
+    o[0] = acc[0];
+    o[1] = acc[1];
+    o[2] = acc[2];
+  }
+  acc[0] = 0.0;
+  acc[1] = 0.0;
+  acc[2] = 0.0;
+}
+__global__ void k_finalize32(KArgs a, int rank_order) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.ns) return;
+  const size_t fo = (size_t)f * a.ns;
+  const int s = rank_order ? a.slot_of_rank[fo + r] : r;
+  const float4 v = a.acc32[fo + r];
+  if (a.out_deriv) {
+    double *o = a.out_deriv + (fo + s) * 3;
+    o[0] = (double)v.x;
+    o[1] = (double)v.y;
+    o[2] = (double)v.z;
+  }
+  a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 pair math of one (first, second) pair: the reference's operations.
+// Returns sigma; d, dfunc out.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double pair_fp64(const SwitchParams &sw, const FrameConst &fc, int do_pbc,
+                                            const double v1[3], const double v2[3], double d[3], double &dfunc) {
+  if (do_pbc)
+    pbc_distance(fc.pbc, v1, v2, d);
+  else
+    for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+  VD<double> r = sw_calculate_sqr<double>(sw, mod2(d));
+  dfunc = r.d;
+  return r.f;
+}
+
+// ds/dR_0 and ds/dD_0 of one pair (for COORD_FLAG_DR0 and the backward).
+// sigma is a function of (r - d0)/r0 (stretched); the stretch/shift depend on
+// R_0 and D_0 through sigma(0) and sigma(d_max), and for the R_0= syntax d_max
+// itself is d0 + r0*1e-5^(1/(n-m)).  Derivatives are taken by central
+// differences of the closed form in (r0, d0) at fixed r -- see
+// param_grad_host() which precomputes the stretch sensitivities.
+struct ParamGrad {
+  double dstretch_dr0, dshift_dr0, dstretch_dd0, dshift_dd0;  // of the stretch/shift constants
+};
+
+} // namespace
+} // namespace coordgpu

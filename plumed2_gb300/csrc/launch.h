@@ -1,0 +1,34 @@
+// launch.h -- host launchers of the kernels (defined in k_fp64.cu / k_mixed.cu).
+#pragma once
+#include "kargs.h"
+#include <atomic>
+
+namespace coordgpu {
+
+// library-wide kernel launch counter (coord_launch_count)
+extern std::atomic<long long> g_launches;
+
+// k_fp64.cu (compiled with -fmad=false)
+void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int linkcells, cudaStream_t s);
+void launch_nl_build(const KArgs &a, cudaStream_t s);
+void launch_pair_flags(const KArgs &a, cudaStream_t s);
+void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s);
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, cudaStream_t s);
+void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int tile, int nblocks, cudaStream_t s);
+void launch_pairs64(const KArgs &a, const SwitchParams &sw, int use_flags, cudaStream_t s);
+void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s);
+
+// k_mixed.cu
+void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int block, cudaStream_t s);
+void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int tile, int nblocks,
+                       cudaStream_t s);
+void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int use_flags, cudaStream_t s);
+void launch_finalize32(const KArgs &a, int rank_order, cudaStream_t s);
+
+// number of 32-lane switch specialisations compiled for the mixed path
+int mixed_nh(const SwitchParams &sw);  // N/2 of fixedRational<N>, or 0 for the generic evaluator
+
+// peaks.cu
+int measure_peaks(int device, double *fp32, double *fp64, double *hbm);
+
+} // namespace coordgpu

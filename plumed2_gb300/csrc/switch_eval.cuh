@@ -1,0 +1,270 @@
+// switch_eval.cuh -- switching functions, value and dfunc, host and device.
+//
+// One templated evaluator per switch type.  Instantiated with double inside a
+// translation unit compiled without FMA contraction (-fmad=false on the
+// device, -ffp-contract=off on the host), every function below performs the
+// reference's operations in the reference's order, so a pair's (sigma,
+// dfunc) is bit-identical to SwitchingFunction::calculateSqr for the rational
+// family (only +,-,*,/ and sqrt, all correctly rounded).  The exp/tanh/cos
+// families call CUDA's math library, which may differ from the host libm in
+// the last ulp.
+//
+// Semantics follow src/tools/SwitchingFunction.cpp:
+//   baseSwitch::calculate (:130-147), applystretch (:121-127),
+//   fixedRational<N>::calculateSqr (:203-215), rational<>::doRational
+//   (:253-280) and calculateSqr (:288-303), fastgaussian calculateSqr
+//   (:410-431), nativeq calculate (:527-555).
+#pragma once
+#include "coord_internal.h"
+#include <cmath>
+
+#ifdef __CUDACC__
+#define SW_HD __host__ __device__ __forceinline__
+#else
+#define SW_HD inline
+#endif
+
+namespace coordgpu {
+
+template <typename T> struct VD {
+  T f, d;
+};
+
+SW_HD double m_exp(double x) { return exp(x); }
+SW_HD float m_exp(float x) { return expf(x); }
+SW_HD double m_tanh(double x) { return tanh(x); }
+SW_HD float m_tanh(float x) { return tanhf(x); }
+SW_HD double m_cos(double x) { return cos(x); }
+SW_HD float m_cos(float x) { return cosf(x); }
+SW_HD double m_sin(double x) { return sin(x); }
+SW_HD float m_sin(float x) { return sinf(x); }
+SW_HD double m_pow(double x, double y) { return pow(x, y); }
+SW_HD float m_pow(float x, float y) { return powf(x, y); }
+SW_HD double m_sqrt(double x) { return sqrt(x); }
+SW_HD float m_sqrt(float x) { return sqrtf(x); }
+
+// Tools::fastpow(base, exp) (Tools.h:582-597); the compile-time fastpow<N>
+// performs the same multiplications in the same order.
+template <typename T> SW_HD T fastpow(T base, int exp) {
+  if (exp < 0) {
+    exp = -exp;
+    base = T(1.0) / base;
+  }
+  T result = T(1.0);
+  while (exp) {
+    if (exp & 1) result *= base;
+    exp >>= 1;
+    base *= base;
+  }
+  return result;
+}
+
+// fixedRational<N>::doRational<POW> (:191-196)
+template <typename T> SW_HD VD<T> rational_fixed(int POW, T rdist) {
+  VD<T> r;
+  const T rNdist = fastpow<T>(rdist, POW - 1);
+  r.f = T(1.0) / (T(1.0) + rNdist * rdist);
+  r.d = T(-POW) * rNdist * r.f * r.f;
+  return r;
+}
+
+// rational<isFast,nis2m>::doRational (:253-280)
+template <typename T>
+SW_HD VD<T> rational_rt(bool simplified, T rdist, T secDev, int N, int M, T dfunc, T result) {
+  const T moreThanOne = T(1.0 + 5.0e10 * 2.220446049250313080847263336181640625e-16);
+  const T lessThanOne = T(1.0 - 5.0e10 * 2.220446049250313080847263336181640625e-16);
+  if (simplified) {
+    const T rNdist = fastpow<T>(rdist, N - 1);
+    result = T(1.0) / (T(1.0) + rNdist * rdist);
+    dfunc = T(-N) * rNdist * result * result;
+  } else if (!((rdist > lessThanOne) && (rdist < moreThanOne))) {
+    const T rNdist = fastpow<T>(rdist, N - 1);
+    const T rMdist = fastpow<T>(rdist, M - 1);
+    const T num = T(1.0) - rNdist * rdist;
+    const T iden = T(1.0) / (T(1.0) - rMdist * rdist);
+    result = num * iden;
+    dfunc = ((T(M) * result * rMdist) - (T(N) * rNdist)) * iden;
+  } else {
+    const T x = (rdist - T(1.0));
+    result = result + x * (dfunc + T(0.5) * x * secDev);
+    dfunc = dfunc + x * secDev;
+  }
+  return VD<T>{result, dfunc};
+}
+
+// switching::function(rdist) of the baseSwitch types
+template <typename T> SW_HD VD<T> sw_function(const SwitchParams &s, T rdist) {
+  switch (s.type) {
+  case SW_RATFIX:
+    return rational_fixed<T>(s.nn, rdist);
+  case SW_RATIONAL:
+  case SW_RATIONAL_FAST:
+    return rational_rt<T>(false, rdist, T(s.preSecDev), s.nn, s.mm, T(s.preDfunc), T(s.preRes));
+  case SW_RATIONAL_SIMPLE:
+  case SW_RATIONAL_SIMPLE_FAST:
+    return rational_rt<T>(true, rdist, T(s.preSecDev), s.nn, s.mm, T(s.preDfunc), T(s.preRes));
+  case SW_EXP: {
+    T result = m_exp(-rdist);
+    return VD<T>{result, -result};
+  }
+  case SW_GAUSSIAN:
+  case SW_FASTGAUSSIAN: {
+    T result = m_exp(T(-0.5) * rdist * rdist);
+    return VD<T>{result, -rdist * result};
+  }
+  case SW_SMAP: {
+    const T sx = T(s.c) * fastpow<T>(rdist, s.a);
+    T result = m_pow(T(1.0) + sx, T(s.d));
+    T dfunc = T(-s.b) * sx / rdist * result / (T(1.0) + sx);
+    return VD<T>{result, dfunc};
+  }
+  case SW_CUBIC: {
+    const T tmp1 = rdist - T(1.0);
+    const T tmp2 = T(1.0) + T(2.0) * rdist;
+    T dfunc = T(2) * tmp1 * tmp2 + T(2) * tmp1 * tmp1;
+    return VD<T>{tmp1 * tmp1 * tmp2, dfunc};
+  }
+  case SW_TANH: {
+    const T tmp1 = m_tanh(rdist);
+    T dfunc = tmp1 * tmp1 - T(1.0);
+    return VD<T>{T(1.0) - tmp1, dfunc};
+  }
+  case SW_COSINUS: {
+    T result = T(0.0), dfunc = T(0.0);
+    if (rdist <= T(1.0)) {
+      const T pi = T(3.141592653589793238462643383279502884197169399375105820974944592307);
+      T rdistPI = rdist * pi;
+      result = T(0.5) * (m_cos(rdistPI) + T(1.0));
+      dfunc = T(-0.5) * pi * m_sin(rdistPI);
+    }
+    return VD<T>{result, dfunc};
+  }
+  default:
+    return VD<T>{T(0), T(0)};
+  }
+}
+
+// nativeqSwitch::calculate (:527-555)
+template <typename T> SW_HD VD<T> nativeq_calculate(const SwitchParams &s, T distance) {
+  T res = T(0.0), dfunc = T(0.0);
+  if (distance <= T(s.dmax)) {
+    res = T(1.0);
+    if (distance > T(s.d0)) {
+      const T rdist = T(s.beta) * (distance - T(s.lambda) * T(s.ref));
+      T exprdist = m_exp(rdist);
+      res = T(1.0) / (T(1.0) + exprdist);
+      dfunc = -T(s.beta) / (exprdist + T(2.0) + T(1.0) / exprdist) / distance;
+      dfunc *= T(s.stretch);
+    }
+    res = res * T(s.stretch) + T(s.shift);
+  }
+  return VD<T>{res, dfunc};
+}
+
+// baseSwitch::calculate + applystretch
+template <typename T> SW_HD VD<T> sw_calculate(const SwitchParams &s, T distance) {
+  if (s.type == SW_Q) return nativeq_calculate<T>(s, distance);
+  const T rdist = (distance - T(s.d0)) * T(s.invr0);
+  if (distance > T(s.dmax)) return VD<T>{T(0.0), T(0.0)};
+  if (rdist > T(0.0)) {
+    VD<T> r = sw_function<T>(s, rdist);
+    r.f = r.f * T(s.stretch) + T(s.shift);
+    r.d *= T(s.stretch);
+    r.d *= T(s.invr0);
+    r.d /= distance;
+    return r;
+  }
+  return VD<T>{T(s.stretch) + T(s.shift), T(0.0)};
+}
+
+// calculateSqr dispatch
+template <typename T> SW_HD VD<T> sw_calculate_sqr(const SwitchParams &s, T distance2) {
+  VD<T> r{T(0.0), T(0.0)};
+  switch (s.type) {
+  case SW_RATFIX:
+    if (distance2 <= T(s.dmax_2)) {
+      const T rdist = distance2 * T(s.invr0_2);
+      r = rational_fixed<T>(s.nn / 2, rdist);
+      r.d *= T(2) * T(s.invr0_2);
+      r.f = r.f * T(s.stretch) + T(s.shift);
+      r.d *= T(s.stretch);
+    }
+    return r;
+  case SW_RATIONAL_FAST:
+  case SW_RATIONAL_SIMPLE_FAST:
+    if (distance2 <= T(s.dmax_2)) {
+      const T rdist = distance2 * T(s.invr0_2);
+      r = rational_rt<T>(s.type == SW_RATIONAL_SIMPLE_FAST, rdist, T(s.preSecDevF), s.nnf, s.mmf, T(s.preDfuncF),
+                         T(s.preRes));
+      r.d *= T(2) * T(s.invr0_2);
+      r.f = r.f * T(s.stretch) + T(s.shift);
+      r.d *= T(s.stretch);
+    }
+    return r;
+  case SW_FASTGAUSSIAN:
+    if (distance2 < T(s.dmax_2)) {
+      r.f = T(1.0);
+      if (distance2 > T(0.0)) {
+        r.f = m_exp(T(-0.5) * distance2);
+        r.d = -r.f;
+        r.f = r.f * T(s.stretch) + T(s.shift);
+        r.d *= T(s.stretch);
+      }
+    }
+    return r;
+  default:
+    return sw_calculate<T>(s, m_sqrt(distance2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tools::pbc (Tools.h:547-571) and Pbc::distance (Pbc.cpp:383-415), FP64.
+// ---------------------------------------------------------------------------
+SW_HD double tools_pbc(double x) {
+  x += 100.0;
+  if (x >= 0) return x - (double)(int)(x + 0.5);
+  return x - (double)(int)(x - 0.5);
+}
+
+SW_HD double mod2(const double d[3]) { return d[0] * d[0] + d[1] * d[1] + d[2] * d[2]; }
+
+// v2 - v1 under the frame's pbc, writing d.
+SW_HD void pbc_distance(const PbcParams &p, const double v1[3], const double v2[3], double d[3]) {
+  for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+  if (p.type == PBC_ORTHO) {
+    for (int k = 0; k < 3; k++) d[k] = tools_pbc(d[k] * p.invbox[k * 4]) * p.box[k * 4];
+  } else if (p.type == PBC_GENERIC) {
+    double s[3];
+    for (int i = 0; i < 3; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < 3; j++) acc += d[j] * p.invreduced[j * 3 + i];
+      s[i] = acc;
+    }
+    for (int k = 0; k < 3; k++) s[k] = tools_pbc(s[k]);
+    for (int i = 0; i < 3; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < 3; j++) acc += s[j] * p.reduced[j * 3 + i];
+      d[i] = acc;
+    }
+    if (fabs(s[0]) + fabs(s[1]) + fabs(s[2]) > 0.5) {
+      const int o = 4 * (s[0] > 0 ? 1 : 0) + 2 * (s[1] > 0 ? 1 : 0) + (s[2] > 0 ? 1 : 0);
+      double best[3] = {d[0], d[1], d[2]};
+      double lbest = mod2(best);
+      for (int i = 0; i < p.nshift[o]; i++) {
+        double trial[3] = {d[0] + p.shift[o][i][0], d[1] + p.shift[o][i][1], d[2] + p.shift[o][i][2]};
+        double ltrial = mod2(trial);
+        if (ltrial < lbest) {
+          lbest = ltrial;
+          best[0] = trial[0];
+          best[1] = trial[1];
+          best[2] = trial[2];
+        }
+      }
+      d[0] = best[0];
+      d[1] = best[1];
+      d[2] = best[2];
+    }
+  }
+}
+
+} // namespace coordgpu

@@ -1,0 +1,252 @@
+"""GPU results (through the C ABI) against the FP64 oracle on the same inputs.
+
+Tolerances, stated here once:
+  FP64 path   s: |ds|/|s| <= 1e-12;  derivatives and virial: max|d| / max|ref| <= 1e-11
+              (the per-pair arithmetic is the reference's; only the summation
+              order differs -- atomics and tree reductions)
+  mixed path  s: |ds|/|s| <= 1e-6;   derivatives: max_i|dF_i| / max_i|F_i| <= 1e-5;
+              virial: max|dW| / max|W| <= 1e-5
+  neighbour lists: the pair set is bit-exact (sorted comparison).
+"""
+import numpy as np
+import pytest
+
+from plumed2_gb300.frames import jittered_lattice
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": (1e-12, 1e-11), "mixed": (1e-6, 1e-5)}
+
+
+def _check(prec, got, ref, what=""):
+    s, d, v = got
+    s0, d0, v0 = ref
+    ts, td = TOL[prec]
+    assert abs(s - s0) <= ts * max(abs(s0), 1e-300) + 1e-300, (what, s, s0)
+    dscale = max(np.abs(d0).max(), 1e-300)
+    assert np.abs(d - d0).max() <= td * dscale, (what, np.abs(d - d0).max() / dscale)
+    vscale = max(np.abs(v0).max(), 1e-300)
+    assert np.abs(v - v0).max() <= td * vscale, (what, np.abs(v - v0).max() / vscale)
+
+
+def _sorted(p):
+    p = np.asarray(p).reshape(-1, 2)
+    return p[np.lexsort((p[:, 1], p[:, 0]))]
+
+
+def _abs_index(c):
+    return np.asarray(c.requested_atoms, dtype=np.int64)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("pbc", [True, False])
+def test_allpairs_single(orc, prec, pbc):
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.30 D_0=0.0 NN=6 MM=12 D_MAX=1.0"
+    pos = jittered_lattice(1000, 0.30, 0.03, 1)
+    box = np.diag([3.0] * 3)
+    c = Coordination("GROUPA=1-1000 SWITCH={%s}%s" % (spec, "" if pbc else " NOPBC"), precision=prec)
+    got = c.calculate(pos, box)
+    ref = orc.coordination(spec, pos, box, orc.all_pairs(0, 1000), do_pbc=pbc)
+    _check(prec, got, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_allpairs_twolist_and_self_pairs(orc, prec):
+    """GROUPA and GROUPB overlap: pairs of the same atom are skipped."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.2"
+    sysp = jittered_lattice(900, 0.31, 0.03, 2)
+    box = np.diag([0.31 * 10] * 3)
+    c = Coordination("GROUPA=1-600 GROUPB=301-900 SWITCH={%s}" % spec, precision=prec)
+    pos = sysp[c.requested_atoms]
+    got = c.calculate(pos, box)
+    ref = orc.coordination(spec, pos, box, orc.all_pairs(1, 600, 600), abs_index=_abs_index(c))
+    _check(prec, got, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_r0_syntax_default_switch(orc, prec):
+    from plumed2_gb300.action import Coordination
+    pos = jittered_lattice(343, 0.3, 0.03, 3)
+    box = np.diag([2.1] * 3)
+    c = Coordination("GROUPA=1-343 R_0=0.3", precision=prec)
+    got = c.calculate(pos, box)
+    ref = orc.coordination("R0SYNTAX 6 0 0.3 0.0", pos, box, orc.all_pairs(0, 343))
+    _check(prec, got, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["single", "two"])
+@pytest.mark.parametrize("pbc", [True, False])
+def test_nlist_semantics_over_steps(orc, prec, mode, pbc):
+    """NLIST: pair set bit-exact at each rebuild; between rebuilds the list of
+    the last rebuild is evaluated at the new positions (NeighborList::prepare)."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.0"
+    n = 4096
+    L = 16 * 0.31
+    box = np.diag([L] * 3)
+    if mode == "single":
+        line, m, n0, n1 = "GROUPA=1-4096", 0, n, 0
+    else:
+        line, m, n0, n1 = "GROUPA=1-2048 GROUPB=2049-4096", 1, 2048, 2048
+    c = Coordination("%s SWITCH={%s} NLIST NL_CUTOFF=0.9 NL_STRIDE=3%s" % (line, spec, "" if pbc else " NOPBC"),
+                     precision=prec)
+    rng = np.random.default_rng(5)
+    pos = jittered_lattice(n, 0.31, 0.03, 4)
+    nl_ref = None
+    for step in range(7):
+        if step % 3 == 0:
+            nl_ref = orc.nl_classic_cells(m, n0, n1, pos, box, pbc, 0.9)
+        got = c.calculate(pos, box, step)
+        if step % 3 == 0:
+            assert np.array_equal(_sorted(c.pairs()), nl_ref), step
+            assert c.nl_size() == len(nl_ref)
+        ref = orc.coordination(spec, pos, box, nl_ref, do_pbc=pbc)
+        _check(prec, got, ref, "step %d" % step)
+        pos = pos + rng.normal(0, 0.01, pos.shape)
+
+
+@pytest.mark.parametrize("mode", ["single", "two"])
+@pytest.mark.parametrize("pbc", [True, False])
+def test_nlistcells_pair_set(orc, mode, pbc):
+    """NLISTCELLS: every pair of neighbouring link cells (LinkCells geometry)."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=0.8"
+    pos = jittered_lattice(1728, 0.31, 0.03, 6)
+    box = np.diag([12 * 0.31] * 3)
+    if mode == "single":
+        line, m, n0, n1 = "GROUPA=1-1728", 0, 1728, 0
+    else:
+        line, m, n0, n1 = "GROUPA=1-864 GROUPB=865-1728", 1, 864, 864
+    c = Coordination("%s SWITCH={%s} NLISTCELLS NL_CUTOFF=0.8 NL_STRIDE=2%s" % (line, spec, "" if pbc else " NOPBC"))
+    got = c.calculate(pos, box, 0)
+    ref_pairs = orc.nl_linkcells(m, n0, n1, pos, box, pbc, 0.8)
+    assert np.array_equal(_sorted(c.pairs()), _sorted(ref_pairs))
+    ref = orc.coordination(spec, pos, box, ref_pairs, do_pbc=pbc)
+    _check("fp64", got, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("nl", [False, True])
+def test_pair_mode(orc, prec, nl):
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.5"
+    pos = jittered_lattice(1000, 0.30, 0.05, 7)
+    box = np.diag([3.0] * 3)
+    extra = " NLIST NL_CUTOFF=1.0 NL_STRIDE=1" if nl else ""
+    c = Coordination("GROUPA=1-500 GROUPB=501-1000 PAIR SWITCH={%s}%s" % (spec, extra), precision=prec)
+    got = c.calculate(pos, box)
+    pairs = orc.nl_classic(2, 500, 500, pos, box, True, 1.0) if nl else orc.all_pairs(2, 500, 500)
+    if nl:
+        assert np.array_equal(_sorted(c.pairs()), _sorted(pairs))
+    ref = orc.coordination(spec, pos, box, pairs)
+    _check(prec, got, ref)
+
+
+SWITCHES = ["RATIONAL R_0=0.3 NN=5 MM=11 D_MAX=0.9", "RATIONAL R_0=0.3 NN=5 D_MAX=0.9",
+            "RATIONAL R_0=0.3 NN=6 MM=10 D_MAX=0.9", "RATIONAL R_0=0.3 NN=8 MM=16 D_MAX=0.9",
+            "RATIONAL R_0=0.3 NN=6 MM=12", "EXP R_0=0.2 D_0=0.1 D_MAX=0.9", "GAUSSIAN R_0=1.0 D_0=0.0 D_MAX=0.9",
+            "GAUSSIAN R_0=0.3 D_0=0.1 D_MAX=0.9", "TANH R_0=0.3 D_MAX=0.9", "SMAP R_0=0.3 A=3 B=2 D_MAX=0.9",
+            "CUBIC D_MAX=0.9 D_0=0.1", "COSINUS R_0=0.9", "Q R_0=0.3 D_0=0.1 BETA=5.0 LAMBDA=1.0 REF=0.4 D_MAX=0.9"]
+
+
+@pytest.mark.parametrize("spec", SWITCHES)
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_switch_types(orc, spec, prec):
+    from plumed2_gb300.action import Coordination
+    pos = jittered_lattice(512, 0.3, 0.04, 8)
+    box = np.diag([2.4] * 3)
+    c = Coordination("GROUPA=1-512 SWITCH={%s}" % spec, precision=prec)
+    got = c.calculate(pos, box)
+    ref = orc.coordination(spec, pos, box, orc.all_pairs(0, 512))
+    prec_t = prec
+    if prec == "fp64" and not spec.startswith("RATIONAL"):
+        # CUDA's exp/tanh/cos/pow may differ from the host libm in the last ulp
+        TOL["fp64_libm"] = (1e-11, 1e-10)
+        prec_t = "fp64_libm"
+    _check(prec_t, got, ref)
+
+
+def test_triclinic_box_rt42_golden(orc, golden):
+    """regtest/basic/rt42 through the GPU FP64 path: a triclinic box, GROUPA and
+    GROUPB the same 108 atoms; values at %8.4f, forces/virial at %10.5f."""
+    from plumed2_gb300.action import Coordination
+    g = golden("rt42.json")
+    pos = np.array(g["frames"][0])
+    box = np.array(g["box"][0]).reshape(3, 3)
+    n = len(pos)
+    cs = {k: Coordination("GROUPA=1-108 GROUPB=1-108 " + v) for k, v in [
+        ("c", "R_0=1"), ("d", "SWITCH={RATIONAL R_0=1}"), ("e", "R_0=1 NN=7 D_0=0.1"),
+        ("f", "SWITCH={RATIONAL R_0=1 D_0=0.1 NN=7 MM=14}"), ("g", "SWITCH={EXP R_0=1}")]}
+    out = {}
+    for k, c in cs.items():
+        s, d, v = c.calculate(np.concatenate([pos, pos]), box)
+        out[k] = (s, d[:n] + d[n:], v)
+    assert abs(out["c"][0] - g["c"][0]) <= 5.01e-5
+    assert abs(out["e"][0] - g["e"][0]) <= 5.01e-5
+    assert abs(out["g"][0] - g["g"][0]) <= 5.01e-5
+    F = -(out["c"][1] + out["d"][1]) - 0.001 * (out["c"][1] - out["d"][1] + out["e"][1] - out["f"][1])
+    V = -(out["c"][2] + out["d"][2]) - 0.001 * (out["c"][2] - out["d"][2] + out["e"][2] - out["f"][2])
+    assert np.abs(F - np.array(g["ff_forces"][0])).max() <= 5.01e-6
+    assert np.abs(V - np.array(g["ff_virial"][0]).reshape(3, 3)).max() <= 5.01e-6
+    c1 = Coordination("GROUPA=1-108 R_0=1")
+    assert abs(c1.calculate(pos, box)[0] - g["c_single"][0]) <= 5.01e-5
+
+
+def test_rt20_switch_goldens(golden):
+    """regtest/basic/rt20-switch-*: two atoms over switchtraj.xyz through the GPU."""
+    from plumed2_gb300.action import Coordination
+    g = golden("rt20_switch.json")
+    for name, case in g["cases"].items():
+        colvar = np.array(case["colvar"])
+        deriv = np.array(case["deriv"])
+        cc = {lab: Coordination("GROUPA=1 GROUPB=2 SWITCH={%s}" % case[lab]) for lab in ("c", "cs")}
+        for fi, (frame, box) in enumerate(zip(g["traj"], g["box"])):
+            B = np.diag(box)
+            for col, lab in ((1, "c"), (2, "cs")):
+                s, d, v = cc[lab].calculate(np.array(frame), B)
+                assert abs(s - colvar[fi, col]) <= 5.01e-7, (name, lab, fi)
+                rows = deriv[deriv[:, 0] == colvar[fi, 0]]
+                got = np.concatenate([d.reshape(-1), v.reshape(-1)])
+                assert np.all(np.abs(got - rows[:, 1 + col]) <= 5.01e-5), (name, lab, fi)
+
+
+def test_empty_and_tiny_groups(orc):
+    from plumed2_gb300.action import Coordination
+    box = np.diag([3.0] * 3)
+    c = Coordination("GROUPA=1 GROUPB=1 R_0=0.3")  # the self pair is skipped: 0
+    s, d, v = c.calculate(np.zeros((2, 3)), box)
+    assert s == 0.0 and np.all(d == 0)
+    c = Coordination("GROUPA=1-2 R_0=0.3")
+    pos = np.array([[0.0, 0, 0], [0.25, 0, 0]])
+    s, d, v = c.calculate(pos, box)
+    ref = orc.coordination("R0SYNTAX 6 0 0.3 0.0", pos, box, np.array([[0, 1]], np.uint32))
+    _check("fp64", (s, d, v), ref)
+
+
+def test_walkers_batched_device(orc):
+    """Several walkers in one launch (coord_forward_device), each with its own list."""
+    torch = pytest.importorskip("torch")
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6"
+    n, L, W = 4096, 16 * 0.31, 3
+    box = np.diag([L] * 3)
+    frames = np.stack([jittered_lattice(n, 0.31, 0.03, 100 + w) for w in range(W)])
+    for prec in ("fp64", "mixed"):
+        c = Coordination("GROUPA=1-4096 SWITCH={%s} NLIST NL_CUTOFF=0.8 NL_STRIDE=10" % spec, precision=prec)
+        dev = torch.device("cuda:0")
+        tpos = torch.from_numpy(frames).to(dev)
+        s = torch.zeros(W, dtype=torch.float64, device=dev)
+        der = torch.zeros(W, n, 3, dtype=torch.float64, device=dev)
+        vir = torch.zeros(W, 9, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        c.forward_device(tpos.data_ptr(), np.stack([box] * W), W, s.data_ptr(), der.data_ptr(), vir.data_ptr(),
+                         step=0)
+        torch.cuda.synchronize()
+        for w in range(W):
+            pairs = orc.nl_classic_cells(0, n, 0, frames[w], box, True, 0.8)
+            assert np.array_equal(_sorted(c.pairs(w)), pairs)
+            ref = orc.coordination(spec, frames[w], box, pairs)
+            _check(prec, (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy().reshape(3, 3)), ref, prec)
