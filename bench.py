@@ -309,6 +309,7 @@ def run_ours(args):
                     "frac": frac_fp32, "traffic": None,
                     "peak_source": "coord_measure_peaks FP32 FMA microbenchmark (measured live)"}
         roof.update({"kernel": "k_eval_nl32 (mixed NL pair kernel)", "kernel_ms": kern_ms, "launches": kern_n,
+                     "fp64_peak_tflops": peaks["fp64_tflops"], "hbm_microbench_gbs": peaks["hbm_gbs"],
                      "alg_flops_per_launch": flops, "alg_bytes_per_launch": bytes_alg,
                      "other_roof_frac": frac_hbm if roof["bound"] == "fp32" else frac_fp32})
 

@@ -89,7 +89,7 @@ struct coord_ctx {
   DevBuf<float4> acc32;
   DevBuf<unsigned> tickets;
   // host-API staging
-  DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam;
+  DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam, d_bvir, d_bpar;
   HostBuf<double> h_pos, h_out;
   HostBuf<FrameConst> h_fc;
   HostBuf<unsigned long long> h_nl;
@@ -340,11 +340,58 @@ int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bo
   return COORD_OK;
 }
 
+// The pair pass and its finalize kernel (derivatives to slot order, scaled
+// by a.g when set).
+void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
+  const bool nl = c->p.nlist != COORD_NL_NONE;
+  const bool mixed = c->p.precision == COORD_PREC_MIXED;
+  cudaEvent_t tev1 = nullptr;
+  if (c->timing) {
+    if (c->ev_used == c->ev_pool.size()) {
+      cudaEvent_t x, y;
+      cudaEventCreate(&x);
+      cudaEventCreate(&y);
+      c->ev_pool.push_back({x, y});
+    }
+    cudaEventRecord(c->ev_pool[c->ev_used].first, c->stream);
+    tev1 = c->ev_pool[c->ev_used].second;
+    c->ev_used++;
+  }
+  if (c->mode == MODE_PAIR) {
+    if (mixed) {
+      launch_gather(a, 0, 0, 1, c->stream);
+      launch_pairs32(a, c->sw, c->s32, mode, nl ? 1 : 0, c->stream);
+    } else {
+      launch_pairs64(a, c->sw, mode, nl ? 1 : 0, c->stream);
+    }
+  } else if (!nl) {
+    if (mixed) {
+      launch_gather(a, 0, 0, 1, c->stream);
+      launch_allpairs32(a, c->sw, c->s32, mode, c->tile32, c->ap_blocks, c->stream);
+    } else {
+      launch_allpairs64(a, c->sw, mode, c->tile64, c->ap_blocks, c->stream);
+    }
+  } else {
+    if (mixed) {
+      launch_gather(a, 1, 0, 1, c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, mode, c->stream);
+    } else {
+      launch_gather(a, 1, 1, 0, c->stream);
+      launch_eval_nl64(a, c->sw, mode, c->stream);
+    }
+  }
+  if (tev1) cudaEventRecord(tev1, c->stream);
+  const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  if (mixed)
+    launch_finalize32(a, rank_order, c->stream);
+  else
+    launch_finalize64(a, rank_order, c->stream);
+}
+
 int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
                  double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream) {
   if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
   if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
-  if (flags & (COORD_FLAG_DR0)) return c->fail(COORD_ERR_UNSUPPORTED, "ds/dR_0 is provided by coord_backward_device");
   if (c->ns == 0) {
     // empty groups: s = 0, no derivatives
     if (s) cudaMemsetAsync(s, 0, sizeof(double) * n_frames, stream);
@@ -447,47 +494,10 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     c->built_frames = n_frames;
   }
 
-  cudaEvent_t tev1 = nullptr;
-  if (c->timing) {
-    if (c->ev_used == c->ev_pool.size()) {
-      cudaEvent_t x, y;
-      cudaEventCreate(&x);
-      cudaEventCreate(&y);
-      c->ev_pool.push_back({x, y});
-    }
-    cudaEventRecord(c->ev_pool[c->ev_used].first, c->stream);
-    tev1 = c->ev_pool[c->ev_used].second;
-    c->ev_used++;
-  }
-  if (c->mode == MODE_PAIR) {
-    if (mixed) {
-      launch_gather(a, 0, 0, 1, c->stream);
-      launch_pairs32(a, c->sw, c->s32, nl ? 1 : 0, c->stream);
-    } else {
-      launch_pairs64(a, c->sw, nl ? 1 : 0, c->stream);
-    }
-  } else if (!nl) {
-    if (mixed) {
-      launch_gather(a, 0, 0, 1, c->stream);
-      launch_allpairs32(a, c->sw, c->s32, c->tile32, c->ap_blocks, c->stream);
-    } else {
-      launch_allpairs64(a, c->sw, c->tile64, c->ap_blocks, c->stream);
-    }
-  } else {
-    if (mixed) {
-      launch_gather(a, 1, 0, 1, c->stream);
-      launch_eval_nl32(a, c->sw, c->s32, 256, c->stream);
-    } else {
-      launch_gather(a, 1, 1, 0, c->stream);
-      launch_eval_nl64(a, c->sw, c->stream);
-    }
-  }
-  if (tev1) cudaEventRecord(tev1, c->stream);
-  const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
-  if (mixed)
-    launch_finalize32(a, rank_order, c->stream);
-  else
-    launch_finalize64(a, rank_order, c->stream);
+  const int mode = (flags & COORD_FLAG_NO_DERIV) ? EVAL_S : ((flags & COORD_FLAG_DR0) ? EVAL_PARAM : EVAL_DERIV);
+  if (mode == EVAL_PARAM && !c->sw.grad_ok)
+    return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
+  launch_evaluation(c, a, mode);
   if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "kernel launch");
   return COORD_OK;
 }
@@ -584,6 +594,10 @@ int coord_create(const coord_params *p, coord_ctx **out) {
     c->s32.shift = (float)s.shift;
     const int nh = s.type == SW_RATFIX ? s.nn / 2 : 0;
     c->s32.c = (float)(-(double)nh * 2.0 * s.invr0_2 * s.stretch);
+    c->s32.d0 = (float)s.d0;
+    c->s32.invr0 = (float)s.invr0;
+    c->s32.c_r0 = (float)s.c_r0;
+    c->s32.c_d0 = (float)s.c_d0;
   }
   // CUDA is initialised on first use (coord_set_groups), so keyword checks and
   // switch set-up work on machines without a GPU.
@@ -623,6 +637,8 @@ int coord_destroy(coord_ctx *c) {
   c->d_deriv.release();
   c->d_virial.release();
   c->d_dparam.release();
+  c->d_bvir.release();
+  c->d_bpar.release();
   c->h_pos.release();
   c->h_out.release();
   c->h_fc.release();
@@ -730,10 +746,52 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   return COORD_OK;
 }
 
-int coord_backward_device(coord_ctx *c, int, const double *, const double *, const double *, double *, double *,
-                          double *, void *) {
+int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes, const double *g,
+                          double *grad_pos, double *grad_box, double *grad_param, void *stream) {
   if (!c) return COORD_ERR_ARG;
-  return c->fail(COORD_ERR_UNSUPPORTED, "backward not built yet");
+  if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
+  if (!boxes || !g || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions, boxes or g");
+  if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
+  if (grad_param && !c->sw.grad_ok)
+    return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
+  cudaSetDevice(c->p.device);
+  if (c->ns == 0) {
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (grad_box) cudaMemsetAsync(grad_box, 0, sizeof(double) * 9 * n_frames, st);
+    if (grad_param) cudaMemsetAsync(grad_param, 0, sizeof(double) * 2 * n_frames, st);
+    return COORD_OK;
+  }
+  const bool nl = c->p.nlist != COORD_NL_NONE;
+  if (nl && c->built_frames != n_frames)
+    return c->fail(COORD_ERR_STATE, "backward needs the neighbour lists of a forward call with the same frames");
+  cudaStream_t saved = c->stream;
+  if (stream) c->stream = (cudaStream_t)stream;
+  struct Restore {
+    coord_ctx *c;
+    cudaStream_t s;
+    ~Restore() { c->stream = s; }
+  } restore{c, saved};
+  cudaError_t e;
+  if ((e = c->d_bvir.ensure((size_t)9 * n_frames)) || (e = c->d_bpar.ensure((size_t)2 * n_frames)))
+    return c->cuda_fail(e, "allocation");
+  bool need_bounds = false;
+  int rc = upload_frames(c, n_frames, boxes, &need_bounds);
+  if (rc) return rc;
+  KArgs a = make_args(c, n_frames, pos, COORD_FLAG_DR0, nullptr, grad_pos, c->d_bvir.p, c->d_bpar.p);
+  a.g = g;
+  if (need_bounds && c->p.precision == COORD_PREC_MIXED) {
+    std::vector<unsigned long long> init(6 * (size_t)n_frames);
+    for (int f = 0; f < n_frames; f++)
+      for (int k = 0; k < 6; k++) init[6 * f + k] = k < 3 ? ~0ull : 0ull;
+    if ((e = cudaMemcpyAsync(c->mm.p, init.data(), sizeof(unsigned long long) * init.size(), cudaMemcpyHostToDevice,
+                             c->stream)))
+      return c->cuda_fail(e, "bounds init");
+    launch_bounds(a, c->mm.p, nl ? c->p.nl_cutoff : 1.0, 0, c->stream);
+  }
+  launch_evaluation(c, a, c->sw.grad_ok ? EVAL_PARAM : EVAL_DERIV);
+  if (grad_box || grad_param) launch_grad_post(a, c->d_bvir.p, c->d_bpar.p, grad_box, grad_param, c->stream);
+  if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "backward launch");
+  return COORD_OK;
 }
 
 int coord_nl_size(coord_ctx *c, int frame, int64_t *n) {

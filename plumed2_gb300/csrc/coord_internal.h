@@ -38,6 +38,12 @@ struct SwitchParams {
   double r0;               // 1/invr0 as given (for parameter gradients)
   int r0_syntax;           // set(nn,mm,r0,d0): d_max depends on R_0 and D_0
   int stretched;           // stretch/shift were set up
+  // parameter gradients: dsigma/dp = (first term) + c_p * (sigma - 1) for a
+  // pair inside d_max, c_p = stretch * d sigma_raw(d_max)/dp (zero when the
+  // stretch constants do not depend on p); grad_ok = 0 for types whose
+  // R_0/D_0 do not enter as (r - d0)/r0 (CUBIC, Q).
+  double c_r0, c_d0;
+  int grad_ok;
 };
 
 // Parses SWITCH={...} (SwitchingFunction::set(string), SwitchingFunction.cpp:

@@ -1,4 +1,16 @@
-// eval.cuh -- pair-evaluation kernels (forward: s, ds/dx, virial).
+// eval.cuh -- pair-evaluation kernels: s, ds/dx, virial, ds/dR_0, ds/dD_0.
+//
+// Each kernel is templated on an EvalMode (kargs.h): EVAL_S accumulates s
+// only (the cheap forward under autograd), EVAL_DERIV adds the per-atom
+// derivatives and the virial (CoordinationBase::calculate), EVAL_PARAM also
+// the switching-parameter gradients.  The backward pass is EVAL_PARAM with the
+// derivatives scaled by dV/ds in the finalize kernel.
+//
+// Parameter gradient of one pair inside d_max (x = (r - d0)/r0, S = stretch):
+//   dsigma/dR_0 = -dfunc r (r - d0) / r0 + c_r0 (sigma - 1)
+//   dsigma/dD_0 = -dfunc r               + c_d0 (sigma - 1)
+// with dfunc = S f'(x)/(r0 r) the reference's dfunc and c_p the dependence of
+// the stretch constants on p (host_setup.cpp).
 #pragma once
 #include "kernels.cuh"
 
@@ -12,9 +24,18 @@ __device__ __forceinline__ void vir_sub(double v[kPartials], const double dd[3],
     for (int j = 0; j < 3; j++) v[1 + 3 * i + j] -= dd[i] * d[j];
 }
 
+__device__ __forceinline__ void param_acc64(const SwitchParams &sw, double r2, double sig, double df, double part[]) {
+  if (r2 <= sw.dmax_2) {
+    const double r = sqrt(r2);
+    part[10] += -df * r * (r - sw.d0) * sw.invr0 + sw.c_r0 * (sig - 1.0);
+    part[11] += -df * r + sw.c_d0 * (sig - 1.0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // neighbour list, FP64: one thread per row (rank), warp = slice
 // ---------------------------------------------------------------------------
+template <int MODE>
 __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
   const int f = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,26 +60,31 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
       double d[3], df;
       const double sig = rfirst ? pair_fp64(sw, fc, a.do_pbc, xr, xp, d, df) : pair_fp64(sw, fc, a.do_pbc, xp, xr, d, df);
       part[0] += sig;
-      const double dd[3] = {df * d[0], df * d[1], df * d[2]};
-      double *accp = a.acc64 + (fo + p) * 3;
-      // deriv[first] -= dd; deriv[second] += dd  (CoordinationBase.cpp:196-206)
-      const double sgn = rfirst ? 1.0 : -1.0;
-      for (int q = 0; q < 3; q++) {
-        accr[q] -= sgn * dd[q];
-        atomicAdd(accp + q, sgn * dd[q]);
+      if (MODE >= EVAL_DERIV) {
+        const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+        double *accp = a.acc64 + (fo + p) * 3;
+        // deriv[first] -= dd; deriv[second] += dd  (CoordinationBase.cpp:196-206)
+        const double sgn = rfirst ? 1.0 : -1.0;
+        for (int q = 0; q < 3; q++) {
+          accr[q] -= sgn * dd[q];
+          atomicAdd(accp + q, sgn * dd[q]);
+        }
+        vir_sub(part, dd, d);
       }
-      vir_sub(part, dd, d);
+      if (MODE == EVAL_PARAM) param_acc64(sw, mod2(d), sig, df, part);
     }
-    double *acc = a.acc64 + (fo + r) * 3;
-    for (int q = 0; q < 3; q++) atomicAdd(acc + q, accr[q]);
+    if (MODE >= EVAL_DERIV) {
+      double *acc = a.acc64 + (fo + r) * 3;
+      for (int q = 0; q < 3; q++) atomicAdd(acc + q, accr[q]);
+    }
   }
   block_partials_finish(a, f, part, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
-// neighbour list, mixed: FP32 pair math from fixed-point positions, FP32
-// per-thread accumulation (Kahan for s), FP64 compensated block/grid sums.
-// NH = N/2 of fixedRational<N>; NH==0 evaluates any switch type in FP32.
+// mixed precision: FP32 pair math from fixed-point positions, FP32 per-thread
+// accumulation (Kahan for s), FP64 compensated block/grid sums.  NH = N/2 of
+// fixedRational<N>; NH == 0 evaluates any switch type in FP32.
 // ---------------------------------------------------------------------------
 template <int NH>
 __device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s, float r2, float &sig, float &df) {
@@ -77,14 +103,53 @@ __device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s,
   }
 }
 
-template <int NH>
+// Per-thread FP32 accumulators of one pair kernel.
+struct Acc32 {
+  float cv = 0.f, cvc = 0.f;
+  float vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
+  float pr0 = 0.f, pd0 = 0.f;
+  __device__ __forceinline__ void add_s(float sig) {
+    const float yk = sig - cvc;
+    const float tk = cv + yk;
+    cvc = (tk - cv) - yk;
+    cv = tk;
+  }
+  __device__ __forceinline__ void add_vir(float ddx, float ddy, float ddz, float dx, float dy, float dz) {
+    vxx = fmaf(-ddx, dx, vxx);
+    vyy = fmaf(-ddy, dy, vyy);
+    vzz = fmaf(-ddz, dz, vzz);
+    vxy = fmaf(-ddx, dy, vxy);
+    vxz = fmaf(-ddx, dz, vxz);
+    vyz = fmaf(-ddy, dz, vyz);
+  }
+  __device__ __forceinline__ void add_param(const SwitchF32 &s, float r2, float sig, float df) {
+    const float r = sqrtf(r2);
+    pr0 = fmaf(-df * r, (r - s.d0) * s.invr0, fmaf(s.c_r0, sig - 1.f, pr0));
+    pd0 = fmaf(-df, r, fmaf(s.c_d0, sig - 1.f, pd0));
+  }
+  __device__ __forceinline__ void to_partials(double part[kPartials]) const {
+    part[0] = (double)cv - (double)cvc;
+    part[1] = vxx;
+    part[2] = vxy;
+    part[3] = vxz;
+    part[4] = vxy;
+    part[5] = vyy;
+    part[6] = vyz;
+    part[7] = vxz;
+    part[8] = vyz;
+    part[9] = vzz;
+    part[10] = pr0;
+    part[11] = pd0;
+  }
+};
+
+template <int NH, int MODE>
 __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const size_t fo = (size_t)f * a.ns;
-  float cv = 0.f, cvc = 0.f;
-  float vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
+  Acc32 acc;
   if (r < a.ns) {
     const FrameConst &fc = a.fc[f];
     const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
@@ -103,37 +168,32 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
       if (r2 <= s32.dmax2) {
         float sig, df;
         sw32<NH>(sw, s32, r2, sig, df);
-        // Kahan sum of s
-        const float yk = sig - cvc;
-        const float tk = cv + yk;
-        cvc = (tk - cv) - yk;
-        cv = tk;
-        const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
-        ax -= ddx;
-        ay -= ddy;
-        az -= ddz;
-        atomicAdd(a.acc32 + fo + p, make_float4(ddx, ddy, ddz, 0.f));
-        vxx = fmaf(-ddx, dx, vxx);
-        vyy = fmaf(-ddy, dy, vyy);
-        vzz = fmaf(-ddz, dz, vzz);
-        vxy = fmaf(-ddx, dy, vxy);
-        vxz = fmaf(-ddx, dz, vxz);
-        vyz = fmaf(-ddy, dz, vyz);
+        acc.add_s(sig);
+        if (MODE >= EVAL_DERIV) {
+          // d = x_p - x_r: deriv[r] -= df d, deriv[p] += df d (either orientation)
+          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+          ax -= ddx;
+          ay -= ddy;
+          az -= ddz;
+          atomicAdd(a.acc32 + fo + p, make_float4(ddx, ddy, ddz, 0.f));
+          acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+        }
+        if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
       }
     }
-    if (len > 0) atomicAdd(a.acc32 + fo + r, make_float4(ax, ay, az, 0.f));
+    if (MODE >= EVAL_DERIV && len > 0) atomicAdd(a.acc32 + fo + r, make_float4(ax, ay, az, 0.f));
   }
-  double part[kPartials] = {(double)cv - (double)cvc, (double)vxx, (double)vxy, (double)vxz, (double)vxy,
-                            (double)vyy, (double)vyz, (double)vxz, (double)vyz, (double)vzz, 0.0, 0.0};
+  double part[kPartials];
+  acc.to_partials(part);
   block_partials_finish(a, f, part, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
-// every pair (no NLIST): tiles of TILE i-slots against TILE j-slots.  The
-// j-side derivatives accumulate in shared memory with a staggered j order
-// (thread t visits j = (t+step) mod TILE) so no two threads hit the same
-// address in the same step.  Single list: tiles (I,J), J>=I, j>i inside a
-// diagonal tile; two lists: A tiles x B tiles.
+// every pair (no NLIST): tiles of TILE i-slots against TILE j-slots, a
+// persistent grid striding over tile pairs.  j-side derivatives accumulate in
+// shared memory with a staggered order (thread t visits j = (t+step) mod
+// TILE) so no two threads hit one address in the same step.  Single list:
+// tiles (I,J), J>=I, j>i inside a diagonal tile; two lists: A x B tiles.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void tile_pair(int t, int nTi, int nTj, bool tri, int &I, int &J) {
   if (!tri) {
@@ -150,7 +210,7 @@ __device__ __forceinline__ void tile_pair(int t, int nTi, int nTj, bool tri, int
   J = i + rem;
 }
 
-template <int TILE>
+template <int TILE, int MODE>
 __global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, int nTi, int nTj, int ntp) {
   const int f = blockIdx.z;
   const bool tri = a.mode == MODE_SINGLE;
@@ -195,18 +255,22 @@ __global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, i
         const double xjj[3] = {xj[jl][0], xj[jl][1], xj[jl][2]};
         const double sig = pair_fp64(sw, fc, a.do_pbc, xi, xjj, d, df);
         part[0] += sig;
-        const double dd[3] = {df * d[0], df * d[1], df * d[2]};
-        for (int q = 0; q < 3; q++) {
-          acci[q] -= dd[q];
-          if (dd[q] != 0.0) atomicAdd(&accj[jl][q], dd[q]);
+        if (MODE >= EVAL_DERIV) {
+          const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+          for (int q = 0; q < 3; q++) {
+            acci[q] -= dd[q];
+            if (dd[q] != 0.0) atomicAdd(&accj[jl][q], dd[q]);
+          }
+          vir_sub(part, dd, d);
         }
-        vir_sub(part, dd, d);
+        if (MODE == EVAL_PARAM) param_acc64(sw, mod2(d), sig, df, part);
       }
-      for (int q = 0; q < 3; q++)
-        if (acci[q] != 0.0) atomicAdd(a.acc64 + (fo + i) * 3 + q, acci[q]);
+      if (MODE >= EVAL_DERIV)
+        for (int q = 0; q < 3; q++)
+          if (acci[q] != 0.0) atomicAdd(a.acc64 + (fo + i) * 3 + q, acci[q]);
     }
     __syncthreads();
-    {
+    if (MODE >= EVAL_DERIV) {
       const int j = jb + threadIdx.x;
       if (j < jend)
         for (int q = 0; q < 3; q++)
@@ -216,7 +280,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, i
   block_partials_finish(a, f, part, gridDim.x);
 }
 
-template <int TILE, int NH>
+template <int TILE, int NH, int MODE>
 __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int nTi, int nTj,
                                                      int ntp) {
   const int f = blockIdx.z;
@@ -228,7 +292,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
   __shared__ uint4 qj[TILE];
   __shared__ float accj[TILE][3];
   __shared__ long long absj[TILE];
-  float cv = 0.f, cvc = 0.f, vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
+  Acc32 acc;
   for (int t = blockIdx.x; t < ntp; t += gridDim.x) {
     int I, J;
     tile_pair(t, nTi, nTj, tri, I, J);
@@ -260,37 +324,33 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
         if (r2 <= s32.dmax2) {
           float sig, df;
           sw32<NH>(sw, s32, r2, sig, df);
-          const float yk = sig - cvc;
-          const float tk = cv + yk;
-          cvc = (tk - cv) - yk;
-          cv = tk;
-          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
-          ax -= ddx;
-          ay -= ddy;
-          az -= ddz;
-          atomicAdd(&accj[jl][0], ddx);
-          atomicAdd(&accj[jl][1], ddy);
-          atomicAdd(&accj[jl][2], ddz);
-          vxx = fmaf(-ddx, dx, vxx);
-          vyy = fmaf(-ddy, dy, vyy);
-          vzz = fmaf(-ddz, dz, vzz);
-          vxy = fmaf(-ddx, dy, vxy);
-          vxz = fmaf(-ddx, dz, vxz);
-          vyz = fmaf(-ddy, dz, vyz);
+          acc.add_s(sig);
+          if (MODE >= EVAL_DERIV) {
+            const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+            ax -= ddx;
+            ay -= ddy;
+            az -= ddz;
+            atomicAdd(&accj[jl][0], ddx);
+            atomicAdd(&accj[jl][1], ddy);
+            atomicAdd(&accj[jl][2], ddz);
+            acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+          }
+          if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
         }
       }
-      if (ax != 0.f || ay != 0.f || az != 0.f) atomicAdd(a.acc32 + fo + i, make_float4(ax, ay, az, 0.f));
+      if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f))
+        atomicAdd(a.acc32 + fo + i, make_float4(ax, ay, az, 0.f));
     }
     __syncthreads();
-    {
+    if (MODE >= EVAL_DERIV) {
       const int j = jb + threadIdx.x;
       const float *v = accj[threadIdx.x];
       if (j < jend && (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f))
         atomicAdd(a.acc32 + fo + j, make_float4(v[0], v[1], v[2], 0.f));
     }
   }
-  double part[kPartials] = {(double)cv - (double)cvc, (double)vxx, (double)vxy, (double)vxz, (double)vxy,
-                            (double)vyy, (double)vyz, (double)vxz, (double)vyz, (double)vzz, 0.0, 0.0};
+  double part[kPartials];
+  acc.to_partials(part);
   block_partials_finish(a, f, part, gridDim.x);
 }
 
@@ -298,7 +358,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
 // PAIR: pair i is (slot i, slot i+nA); every slot belongs to one pair, so
 // derivatives are written without atomics.  With NLIST only flagged pairs.
 // ---------------------------------------------------------------------------
-__global__ void k_pairs64(KArgs a, SwitchParams sw, int use_flags) {
+template <int MODE> __global__ void k_pairs64(KArgs a, SwitchParams sw, int use_flags) {
   const int f = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const size_t fo = (size_t)f * a.ns;
@@ -310,23 +370,24 @@ __global__ void k_pairs64(KArgs a, SwitchParams sw, int use_flags) {
     const double v1[3] = {p0[0], p0[1], p0[2]}, v2[3] = {p1[0], p1[1], p1[2]};
     double d[3], df;
     part[0] = pair_fp64(sw, a.fc[f], a.do_pbc, v1, v2, d, df);
-    const double dd[3] = {df * d[0], df * d[1], df * d[2]};
-    for (int q = 0; q < 3; q++) {
-      a.acc64[(fo + i) * 3 + q] -= dd[q];
-      a.acc64[(fo + i + a.nA) * 3 + q] += dd[q];
+    if (MODE >= EVAL_DERIV) {
+      const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+      for (int q = 0; q < 3; q++) {
+        a.acc64[(fo + i) * 3 + q] -= dd[q];
+        a.acc64[(fo + i + a.nA) * 3 + q] += dd[q];
+      }
+      vir_sub(part, dd, d);
     }
-    vir_sub(part, dd, d);
+    if (MODE == EVAL_PARAM) param_acc64(sw, mod2(d), part[0], df, part);
   }
   block_partials_finish(a, f, part, gridDim.x);
 }
 
-template <int NH> __global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int use_flags) {
+template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int use_flags) {
   const int f = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const size_t fo = (size_t)f * a.ns;
-  double part[kPartials];
-#pragma unroll
-  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  Acc32 acc;
   if (i < a.nA && (!use_flags || a.pair_flag[(size_t)f * a.nA + i]) && a.abs_of_slot[i] != a.abs_of_slot[i + a.nA]) {
     const FrameConst &fc = a.fc[f];
     const uint4 q0 = a.q[fo + i], q1 = a.q[fo + i + a.nA];
@@ -336,20 +397,51 @@ template <int NH> __global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 
     if (r2 <= s32.dmax2) {
       float sig, df;
       sw32<NH>(sw, s32, r2, sig, df);
-      const float dd[3] = {df * dx, df * dy, df * dz}, d[3] = {dx, dy, dz};
-      part[0] = sig;
-      float4 &a0 = a.acc32[fo + i], &a1 = a.acc32[fo + i + a.nA];
-      a0.x -= dd[0];
-      a0.y -= dd[1];
-      a0.z -= dd[2];
-      a1.x += dd[0];
-      a1.y += dd[1];
-      a1.z += dd[2];
-      for (int x = 0; x < 3; x++)
-        for (int y = 0; y < 3; y++) part[1 + 3 * x + y] = -(double)dd[x] * (double)d[y];
+      acc.add_s(sig);
+      if (MODE >= EVAL_DERIV) {
+        const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+        float4 &a0 = a.acc32[fo + i], &a1 = a.acc32[fo + i + a.nA];
+        a0.x -= ddx;
+        a0.y -= ddy;
+        a0.z -= ddz;
+        a1.x += ddx;
+        a1.y += ddy;
+        a1.z += ddz;
+        acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+      }
+      if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
     }
   }
+  double part[kPartials];
+  acc.to_partials(part);
   block_partials_finish(a, f, part, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// backward epilogue: box and parameter gradients of V from this pass's virial
+// B and parameter sums: dV/dh = g * (-(h^T)^{-1} B)  (scaled coordinates held
+// fixed; the box-derivative convention of ActionAtomistic.cpp:221-265).
+// ---------------------------------------------------------------------------
+__global__ void k_grad_post(KArgs a, const double *vir, const double *dpar, double *grad_box, double *grad_param) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.nframes) return;
+  const double g = a.g[f];
+  const FrameConst &fc = a.fc[f];
+  if (grad_box) {
+    const double *B = vir + (size_t)f * 9;
+    const double *ib = fc.pbc.invbox;
+    const bool has_box = fc.pbc.type != PBC_UNSET;
+    for (int k = 0; k < 3; k++)
+      for (int b = 0; b < 3; b++) {
+        double s = 0.0;
+        for (int q = 0; q < 3; q++) s += ib[q * 3 + k] * B[q * 3 + b];
+        grad_box[(size_t)f * 9 + k * 3 + b] = has_box ? -g * s : 0.0;
+      }
+  }
+  if (grad_param) {
+    grad_param[(size_t)f * 2] = g * dpar[(size_t)f * 2];
+    grad_param[(size_t)f * 2 + 1] = g * dpar[(size_t)f * 2 + 1];
+  }
 }
 
 } // namespace

@@ -156,6 +156,23 @@ Words split(const char *def) {
   return W;
 }
 
+// Constants of the parameter gradients (see SwitchParams::c_r0).  With the
+// stretch set up from a fixed D_MAX, sigma = S*(f(x) - f(xd)), S = 1/(1 -
+// f(xd)), xd = (d_max - d0)/r0, so d sigma/dp = S f'(x) dx/dp + S dsd/dp
+// (sigma - 1) with dsd/dr0 = -f'(xd) xd/r0 and dsd/dd0 = -f'(xd)/r0.  In the
+// R_0= syntax xd is constant (d_max moves with r0 and d0): no second term.
+void setup_param_grad(SwitchParams *s) {
+  s->c_r0 = 0.0;
+  s->c_d0 = 0.0;
+  s->grad_ok = !(s->type == SW_CUBIC || s->type == SW_Q);
+  if (!s->grad_ok || !s->stretched || s->r0_syntax) return;
+  const double xd = (s->dmax - s->d0) * s->invr0;
+  if (!(xd > 0.0)) return;
+  const double fpd = sw_function<double>(*s, xd).d;
+  s->c_r0 = s->stretch * (-fpd * xd * s->invr0);
+  s->c_d0 = s->stretch * (-fpd * s->invr0);
+}
+
 } // namespace
 
 int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw) {
@@ -165,6 +182,7 @@ int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw)
   setup_stretch(sw);
   sw->r0 = r0;
   sw->r0_syntax = 1;
+  setup_param_grad(sw);
   return 0;
 }
 
@@ -250,6 +268,7 @@ int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen)
     return 1;
   }
   if (dostretch && dmax != DBL_MAX) setup_stretch(sw);
+  setup_param_grad(sw);
   return 0;
 }
 

@@ -39,29 +39,53 @@ void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaSt
   g_launches += 1;
 }
 
-void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, cudaStream_t s) {
-  k_eval_nl64<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw);
+#define MODE_DISPATCH(M, CALL) \
+  switch (M) {                   \
+  case EVAL_S: CALL(EVAL_S); break; \
+  case EVAL_PARAM: CALL(EVAL_PARAM); break; \
+  default: CALL(EVAL_DERIV); break; \
+  }
+
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStream_t s) {
+#define CALL(M) k_eval_nl64<M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw)
+  MODE_DISPATCH(mode, CALL)
+#undef CALL
   g_launches += 1;
 }
 
-void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int tile, int nblocks, cudaStream_t s) {
+void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int mode, int tile, int nblocks, cudaStream_t s) {
   const bool tri = a.mode == MODE_SINGLE;
   const int ni = tri ? a.ns : a.nA, nj = tri ? a.ns : a.ns - a.nA;
   const int nTi = (ni + tile - 1) / tile, nTj = (nj + tile - 1) / tile;
   const long long ntp = tri ? (long long)nTi * (nTi + 1) / 2 : (long long)nTi * nTj;
   const int nb = (int)std::max(1ll, std::min<long long>(ntp, nblocks));
   dim3 g(nb, 1, a.nframes);
-  switch (tile) {
-  case 32: k_allpairs64<32><<<g, 32, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
-  case 64: k_allpairs64<64><<<g, 64, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
-  case 256: k_allpairs64<256><<<g, 256, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
-  default: k_allpairs64<128><<<g, 128, 0, s>>>(a, sw, nTi, nTj, (int)ntp); break;
+  if (tile == 32) {
+#define CALL(M) k_allpairs64<32, M><<<g, 32, 0, s>>>(a, sw, nTi, nTj, (int)ntp)
+    MODE_DISPATCH(mode, CALL)
+#undef CALL
+  } else if (tile == 128) {
+#define CALL(M) k_allpairs64<128, M><<<g, 128, 0, s>>>(a, sw, nTi, nTj, (int)ntp)
+    MODE_DISPATCH(mode, CALL)
+#undef CALL
+  } else {
+#define CALL(M) k_allpairs64<64, M><<<g, 64, 0, s>>>(a, sw, nTi, nTj, (int)ntp)
+    MODE_DISPATCH(mode, CALL)
+#undef CALL
   }
   g_launches += 1;
 }
 
-void launch_pairs64(const KArgs &a, const SwitchParams &sw, int use_flags, cudaStream_t s) {
-  k_pairs64<<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, use_flags);
+void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_flags, cudaStream_t s) {
+#define CALL(M) k_pairs64<M><<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, use_flags)
+  MODE_DISPATCH(mode, CALL)
+#undef CALL
+  g_launches += 1;
+}
+
+void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, double *grad_box, double *grad_param,
+                      cudaStream_t s) {
+  k_grad_post<<<(a.nframes + 63) / 64, 64, 0, s>>>(a, vir, dpar, grad_box, grad_param);
   g_launches += 1;
 }
 

@@ -12,26 +12,45 @@ int mixed_nh(const SwitchParams &sw) {
   return 0;
 }
 
-#define NH_DISPATCH(NHV, CALL) \
-  switch (NHV) {               \
-  case 1: CALL(1); break;      \
-  case 2: CALL(2); break;      \
-  case 3: CALL(3); break;      \
-  case 4: CALL(4); break;      \
-  case 5: CALL(5); break;      \
-  case 6: CALL(6); break;      \
-  default: CALL(0); break;     \
-  }
+// N/2 of fixedRational<N> compiled as its own kernel; other N and every other
+// switch type use the generic FP32 evaluator (NH = 0).
+#define NH_MODE_DISPATCH(NHV, M, CALL)       \
+  do {                                       \
+    const int nh_ = (NHV), m_ = (M);         \
+    if (m_ == EVAL_S) {                      \
+      if (nh_ == 3) CALL(3, EVAL_S);         \
+      else if (nh_ == 2) CALL(2, EVAL_S);    \
+      else if (nh_ == 4) CALL(4, EVAL_S);    \
+      else if (nh_ == 6) CALL(6, EVAL_S);    \
+      else CALL(0, EVAL_S);                  \
+    } else if (m_ == EVAL_PARAM) {           \
+      if (nh_ == 3) CALL(3, EVAL_PARAM);     \
+      else if (nh_ == 2) CALL(2, EVAL_PARAM); \
+      else if (nh_ == 4) CALL(4, EVAL_PARAM); \
+      else if (nh_ == 6) CALL(6, EVAL_PARAM); \
+      else CALL(0, EVAL_PARAM);              \
+    } else {                                 \
+      if (nh_ == 3) CALL(3, EVAL_DERIV);     \
+      else if (nh_ == 2) CALL(2, EVAL_DERIV); \
+      else if (nh_ == 4) CALL(4, EVAL_DERIV); \
+      else if (nh_ == 6) CALL(6, EVAL_DERIV); \
+      else CALL(0, EVAL_DERIV);              \
+    }                                        \
+  } while (0)
 
-void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int block, cudaStream_t s) {
-  (void)block;
-#define CALL(N) k_eval_nl32<N><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw, s32)
-  NH_DISPATCH(mixed_nh(sw), CALL)
+static int nh_compiled(const SwitchParams &sw) {
+  const int nh = mixed_nh(sw);
+  return (nh == 2 || nh == 3 || nh == 4 || nh == 6) ? nh : 0;
+}
+
+void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s) {
+#define CALL(N, M) k_eval_nl32<N, M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw, s32)
+  NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL
   g_launches += 1;
 }
 
-void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int tile, int nblocks,
+void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s) {
   const bool tri = a.mode == MODE_SINGLE;
   const int ni = tri ? a.ns : a.nA, nj = tri ? a.ns : a.ns - a.nA;
@@ -39,27 +58,22 @@ void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &
   const long long ntp = tri ? (long long)nTi * (nTi + 1) / 2 : (long long)nTi * nTj;
   const int nb = (int)std::max(1ll, std::min<long long>(ntp, nblocks));
   dim3 g(nb, 1, a.nframes);
-#define CALLT(T, N) k_allpairs32<T, N><<<g, T, 0, s>>>(a, sw, s32, nTi, nTj, (int)ntp)
   if (tile == 64) {
-#define CALL(N) CALLT(64, N)
-    NH_DISPATCH(mixed_nh(sw), CALL)
-#undef CALL
-  } else if (tile == 256) {
-#define CALL(N) CALLT(256, N)
-    NH_DISPATCH(mixed_nh(sw), CALL)
+#define CALL(N, M) k_allpairs32<64, N, M><<<g, 64, 0, s>>>(a, sw, s32, nTi, nTj, (int)ntp)
+    NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL
   } else {
-#define CALL(N) CALLT(128, N)
-    NH_DISPATCH(mixed_nh(sw), CALL)
+#define CALL(N, M) k_allpairs32<128, N, M><<<g, 128, 0, s>>>(a, sw, s32, nTi, nTj, (int)ntp)
+    NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL
   }
-#undef CALLT
   g_launches += 1;
 }
 
-void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int use_flags, cudaStream_t s) {
-#define CALL(N) k_pairs32<N><<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, s32, use_flags)
-  NH_DISPATCH(mixed_nh(sw), CALL)
+void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,
+                    cudaStream_t s) {
+#define CALL(N, M) k_pairs32<N, M><<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, s32, use_flags)
+  NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL
   g_launches += 1;
 }

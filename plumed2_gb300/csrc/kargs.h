@@ -51,9 +51,18 @@ struct KArgs {
   const double *g;              // [nframes] upstream dV/ds (backward)
 };
 
-// FP32 parameters of a fixedRational<2*NH> switch (mixed path).
+// FP32 parameters of a fixedRational<2*NH> switch (mixed path), plus the
+// constants of the R_0/D_0 gradients (SwitchParams::c_r0).
 struct SwitchF32 {
   float dmax2, invr0_2, stretch, shift, c;  // c = -NH * 2*invr0^2 * stretch
+  float d0, invr0, c_r0, c_d0;
+};
+
+// What a pair kernel accumulates.
+enum EvalMode : int {
+  EVAL_S = 0,      // s only
+  EVAL_DERIV = 1,  // s, ds/dx, virial
+  EVAL_PARAM = 2   // s, ds/dx, virial, ds/dR_0, ds/dD_0
 };
 
 } // namespace coordgpu

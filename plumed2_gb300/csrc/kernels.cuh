@@ -515,10 +515,12 @@ __global__ void k_finalize64(KArgs a, int rank_order) {
   const int s = rank_order ? a.slot_of_rank[fo + r] : r;
   double *acc = a.acc64 + (fo + r) * 3;
   if (a.out_deriv) {
+    // backward: scaled by the upstream dV/ds of the frame
+    const double g = a.g ? a.g[f] : 1.0;
     double *o = a.out_deriv + (fo + s) * 3;
-    o[0] = acc[0];
-    o[1] = acc[1];
-    o[2] = acc[2];
+    o[0] = g * acc[0];
+    o[1] = g * acc[1];
+    o[2] = g * acc[2];
   }
   acc[0] = 0.0;
   acc[1] = 0.0;
@@ -532,10 +534,11 @@ __global__ void k_finalize32(KArgs a, int rank_order) {
   const int s = rank_order ? a.slot_of_rank[fo + r] : r;
   const float4 v = a.acc32[fo + r];
   if (a.out_deriv) {
+    const double g = a.g ? a.g[f] : 1.0;
     double *o = a.out_deriv + (fo + s) * 3;
-    o[0] = (double)v.x;
-    o[1] = (double)v.y;
-    o[2] = (double)v.z;
+    o[0] = g * (double)v.x;
+    o[1] = g * (double)v.y;
+    o[2] = g * (double)v.z;
   }
   a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
 }

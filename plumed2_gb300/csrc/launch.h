@@ -13,16 +13,19 @@ void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int li
 void launch_nl_build(const KArgs &a, cudaStream_t s);
 void launch_pair_flags(const KArgs &a, cudaStream_t s);
 void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s);
-void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, cudaStream_t s);
-void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int tile, int nblocks, cudaStream_t s);
-void launch_pairs64(const KArgs &a, const SwitchParams &sw, int use_flags, cudaStream_t s);
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStream_t s);
+void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int mode, int tile, int nblocks, cudaStream_t s);
+void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_flags, cudaStream_t s);
 void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s);
+void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, double *grad_box, double *grad_param,
+                      cudaStream_t s);
 
 // k_mixed.cu
-void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int block, cudaStream_t s);
-void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int tile, int nblocks,
+void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s);
+void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s);
-void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int use_flags, cudaStream_t s);
+void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,
+                    cudaStream_t s);
 void launch_finalize32(const KArgs &a, int rank_order, cudaStream_t s);
 
 // number of 32-lane switch specialisations compiled for the mixed path

@@ -92,6 +92,30 @@ SW_HD VD<T> rational_rt(bool simplified, T rdist, T secDev, int N, int M, T dfun
   return VD<T>{result, dfunc};
 }
 
+// (1 - x^N)/(1 - x^M) for x >= 0 as a ratio of geometric sums
+// P_N(x)/P_M(x), P_K = 1 + x + ... + x^(K-1): no cancellation near x = 1, so
+// single precision keeps its relative accuracy there (the FP64 path uses the
+// reference's closed form and Taylor window instead).
+template <typename T> SW_HD VD<T> rational_geometric(T x, int N, int M) {
+  T pn = T(0), dpn = T(0), pm = T(0), dpm = T(0), xk = T(1), xkm1 = T(0);
+  const int K = N > M ? N : M;
+  for (int k = 0; k < K; k++) {
+    if (k < N) {
+      pn += xk;
+      dpn += T(k) * xkm1;
+    }
+    if (k < M) {
+      pm += xk;
+      dpm += T(k) * xkm1;
+    }
+    xkm1 = xk;
+    xk *= x;
+  }
+  const T inv = T(1) / pm;
+  const T f = pn * inv;
+  return VD<T>{f, (dpn - f * dpm) * inv};
+}
+
 // switching::function(rdist) of the baseSwitch types
 template <typename T> SW_HD VD<T> sw_function(const SwitchParams &s, T rdist) {
   switch (s.type) {
@@ -99,6 +123,7 @@ template <typename T> SW_HD VD<T> sw_function(const SwitchParams &s, T rdist) {
     return rational_fixed<T>(s.nn, rdist);
   case SW_RATIONAL:
   case SW_RATIONAL_FAST:
+    if (sizeof(T) == 4 && s.nn > 0 && s.mm > 0 && rdist >= T(0)) return rational_geometric<T>(rdist, s.nn, s.mm);
     return rational_rt<T>(false, rdist, T(s.preSecDev), s.nn, s.mm, T(s.preDfunc), T(s.preRes));
   case SW_RATIONAL_SIMPLE:
   case SW_RATIONAL_SIMPLE_FAST:
@@ -194,8 +219,11 @@ template <typename T> SW_HD VD<T> sw_calculate_sqr(const SwitchParams &s, T dist
   case SW_RATIONAL_SIMPLE_FAST:
     if (distance2 <= T(s.dmax_2)) {
       const T rdist = distance2 * T(s.invr0_2);
-      r = rational_rt<T>(s.type == SW_RATIONAL_SIMPLE_FAST, rdist, T(s.preSecDevF), s.nnf, s.mmf, T(s.preDfuncF),
-                         T(s.preRes));
+      if (sizeof(T) == 4 && s.type == SW_RATIONAL_FAST && s.nnf > 0 && s.mmf > 0)
+        r = rational_geometric<T>(rdist, s.nnf, s.mmf);
+      else
+        r = rational_rt<T>(s.type == SW_RATIONAL_SIMPLE_FAST, rdist, T(s.preSecDevF), s.nnf, s.mmf, T(s.preDfuncF),
+                           T(s.preRes));
       r.d *= T(2) * T(s.invr0_2);
       r.f = r.f * T(s.stretch) + T(s.shift);
       r.d *= T(s.stretch);

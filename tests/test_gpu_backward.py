@@ -1,0 +1,162 @@
+"""Backward pass: dV/dx, dV/dh (box), dV/dR_0, dV/dD_0 of a metadynamics-style
+bias V(s) = sum_k h exp(-(s - s_k)^2 / (2 sigma^2)).
+
+Checks, on the FP64 path:
+  * against the oracle's analytic derivatives times V'(s) (the reference's
+    own derivative layout): max|d| / max|ref| <= 1e-10
+  * against FP64 central finite differences, step 1e-6 nm (positions; box
+    with scaled coordinates held fixed) and 1e-6 nm in R_0/D_0:
+    relative error <= 2e-6 of the gradient's scale
+The mixed path's gradients against the FP64 path's: <= 1e-5 (norm-wise).
+"""
+import numpy as np
+import pytest
+
+from plumed2_gb300.frames import jittered_lattice
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def bias(s, s0):
+    rng = np.random.default_rng(3)
+    centres = torch.tensor(rng.uniform(0.8 * s0, 1.2 * s0, 500), dtype=torch.float64, device=s.device)
+    sig = 0.05 * s0
+    return (1.2 * torch.exp(-(s[:, None] - centres[None, :]) ** 2 / (2 * sig * sig))).sum(1)
+
+
+def bias_np(s, s0):
+    rng = np.random.default_rng(3)
+    centres = rng.uniform(0.8 * s0, 1.2 * s0, 500)
+    sig = 0.05 * s0
+    v = 1.2 * np.exp(-(s - centres) ** 2 / (2 * sig * sig))
+    return v.sum(), (v * (-(s - centres) / (sig * sig))).sum()
+
+
+def make(line, prec):
+    from plumed2_gb300.action import Coordination
+    return Coordination(line, precision=prec)
+
+
+CASES = [
+    ("GROUPA=1-216 SWITCH={RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.9}", "SWITCH={RATIONAL R_0=%r NN=6 MM=12 D_MAX=0.9 D_0=%r}"),
+    ("GROUPA=1-216 R_0=0.3", "R_0=%r D_0=%r"),
+    ("GROUPA=1-108 GROUPB=109-216 SWITCH={RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=5",
+     "SWITCH={RATIONAL R_0=%r NN=6 MM=12 D_MAX=0.9 D_0=%r} NLIST NL_CUTOFF=1.0 NL_STRIDE=5"),
+]
+
+
+@pytest.mark.parametrize("line,pline", CASES)
+def test_backward_fp64_against_oracle_and_fd(orc, line, pline):
+    from plumed2_gb300.autograd import coordination
+    dev = torch.device("cuda:0")
+    pos0 = jittered_lattice(216, 0.3, 0.04, 11)
+    L = 1.8
+    box0 = np.diag([L, L, L])
+    act = make(line, "fp64")
+    pos = torch.tensor(pos0[None], dtype=torch.float64, device=dev, requires_grad=True)
+    box = torch.tensor(box0, dtype=torch.float64, requires_grad=True)
+    r0 = torch.tensor(0.3, dtype=torch.float64, device=dev, requires_grad=True)
+    d0 = torch.tensor(0.0, dtype=torch.float64, device=dev, requires_grad=True)
+    s = coordination(act, pos, box, r0, d0)
+    s0 = float(s.item())
+    V = bias(s, s0).sum()
+    V.backward()
+    gpos = pos.grad[0].cpu().numpy()
+    gbox = box.grad.numpy()
+    # oracle analytic derivatives x V'(s)
+    is_nl = "NLIST" in line
+    if "GROUPB" in line:
+        pairs = orc.nl_classic(1, 108, 108, pos0, box0, True, 1.0) if is_nl else orc.all_pairs(1, 108, 108)
+    else:
+        pairs = orc.all_pairs(0, 216)
+    spec = "RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.9" if "SWITCH" in line else "R0SYNTAX 6 0 0.3 0.0"
+    so, do, vo = orc.coordination(spec, pos0, box0, pairs)
+    _, dV = bias_np(so, s0)
+    assert abs(so - s0) <= 1e-12 * abs(so)
+    assert np.abs(gpos - dV * do).max() <= 1e-10 * np.abs(dV * do).max()
+    ref_box = dV * (-np.linalg.inv(box0).T @ vo)
+    assert np.abs(gbox - ref_box).max() <= 1e-10 * np.abs(ref_box).max()
+
+    # central finite differences of V in FP64 (fresh actions, same NL where used)
+    def V_of(p, b, r0v=0.3, d0v=0.0):
+        a = make(line.split(" SWITCH")[0].split(" R_0")[0] + " " + (pline % (r0v, d0v)), "fp64")
+        sv, _, _ = a.calculate(p, b, 0, derivatives=False)
+        a.close()
+        return bias_np(sv, s0)[0]
+
+    h = 1e-6
+    rng = np.random.default_rng(0)
+    for idx in rng.choice(216, 4, replace=False):
+        for k in range(3):
+            pp = pos0.copy()
+            pm = pos0.copy()
+            pp[idx, k] += h
+            pm[idx, k] -= h
+            fd = (V_of(pp, box0) - V_of(pm, box0)) / (2 * h)
+            assert abs(fd - gpos[idx, k]) <= 2e-6 * np.abs(gpos).max() + 1e-9, (idx, k, fd, gpos[idx, k])
+    scaled = pos0 @ np.linalg.inv(box0)
+    for (kk, bb) in ((0, 0), (1, 1), (2, 2), (0, 1)):
+        bp = box0.copy()
+        bm = box0.copy()
+        bp[kk, bb] += h
+        bm[kk, bb] -= h
+        fd = (V_of(scaled @ bp, bp) - V_of(scaled @ bm, bm)) / (2 * h)
+        assert abs(fd - gbox[kk, bb]) <= 2e-6 * np.abs(gbox).max() + 1e-9, (kk, bb, fd, gbox[kk, bb])
+    fd_r0 = (V_of(pos0, box0, 0.3 + h) - V_of(pos0, box0, 0.3 - h)) / (2 * h)
+    assert abs(fd_r0 - r0.grad.item()) <= 2e-6 * abs(fd_r0) + 1e-9, (fd_r0, r0.grad.item())
+    fd_d0 = (V_of(pos0, box0, 0.3, h) - V_of(pos0, box0, 0.3, -h)) / (2 * h)
+    assert abs(fd_d0 - d0.grad.item()) <= 2e-6 * abs(fd_d0) + 1e-9, (fd_d0, d0.grad.item())
+    act.close()
+
+
+def test_backward_mixed_matches_fp64():
+    from plumed2_gb300.autograd import coordination
+    dev = torch.device("cuda:0")
+    n, L = 4096, 16 * 0.31
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6} NLIST NL_CUTOFF=0.8 NL_STRIDE=10" % n
+    frames = np.stack([jittered_lattice(n, 0.31, 0.03, 40 + w) for w in range(2)])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        act = make(line, prec)
+        pos = torch.tensor(frames, dtype=torch.float64, device=dev, requires_grad=True)
+        box = torch.tensor(np.diag([L] * 3), dtype=torch.float64, requires_grad=True)
+        r0 = torch.tensor(0.32, dtype=torch.float64, device=dev, requires_grad=True)
+        d0 = torch.tensor(0.0, dtype=torch.float64, device=dev, requires_grad=True)
+        s = coordination(act, pos, box, r0, d0)
+        s0 = float(s[0].item()) if prec == "fp64" else out["fp64"][0][0]
+        V = bias(s, s0).sum()
+        V.backward()
+        out[prec] = (s.detach().cpu().numpy(), pos.grad.cpu().numpy(), box.grad.numpy(), r0.grad.item(),
+                     d0.grad.item())
+        act.close()
+    a, b = out["fp64"], out["mixed"]
+    assert np.all(np.abs(a[0] - b[0]) <= 1e-6 * np.abs(a[0]))
+    assert np.abs(a[1] - b[1]).max() <= 1e-5 * np.abs(a[1]).max()
+    assert np.abs(a[2] - b[2]).max() <= 1e-5 * np.abs(a[2]).max()
+    assert abs(a[3] - b[3]) <= 1e-5 * abs(a[3])
+    assert abs(a[4] - b[4]) <= 1e-5 * abs(a[4])
+
+
+def test_forward_dr0_flag_matches_backward():
+    """COORD_FLAG_DR0 on the forward returns ds/dR_0, ds/dD_0 (g = 1)."""
+    from plumed2_gb300 import _lib
+    dev = torch.device("cuda:0")
+    act = make("GROUPA=1-512 SWITCH={RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.9}", "fp64")
+    pos = torch.tensor(jittered_lattice(512, 0.3, 0.04, 12)[None], dtype=torch.float64, device=dev)
+    box = np.diag([2.4] * 3)[None]
+    s = torch.zeros(1, dtype=torch.float64, device=dev)
+    der = torch.zeros(1, 512, 3, dtype=torch.float64, device=dev)
+    vir = torch.zeros(1, 9, dtype=torch.float64, device=dev)
+    dp = torch.zeros(1, 2, dtype=torch.float64, device=dev)
+    act.forward_device(pos.data_ptr(), box, 1, s.data_ptr(), der.data_ptr(), vir.data_ptr(), flags=_lib.FLAG_DR0,
+                       dparam_ptr=dp.data_ptr())
+    g = torch.ones(1, dtype=torch.float64, device=dev)
+    gp = torch.zeros_like(der)
+    gb = torch.zeros(1, 9, dtype=torch.float64, device=dev)
+    gq = torch.zeros(1, 2, dtype=torch.float64, device=dev)
+    act.backward_device(pos.data_ptr(), box, 1, g.data_ptr(), gp.data_ptr(), gb.data_ptr(), gq.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.allclose(gp, der, rtol=1e-12, atol=1e-14)
+    assert torch.allclose(gq, dp, rtol=1e-12, atol=1e-14)
