@@ -165,6 +165,25 @@ int coord_multi_forward_device(coord_multi *m, int n_frames, const double *pos, 
 int coord_multi_use_graph(coord_multi *m, int enable);
 const char *coord_multi_last_error(const coord_multi *m);
 
+/* ---- forward without device allocation ------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they call in (an MD engine that reserves its whole device pool
+ * up front and forbids other allocations during a run): the FP64 every-pair
+ * forward (no NLIST, no PAIR) with all working memory in one static device
+ * array of COORD_NOALLOC_MAX_SLOTS slots that each GPU keeps until exit.
+ * ctx comes from coord_create (which touches no CUDA); do not call
+ * coord_set_groups on it.  Groups are host arrays of absolute indices; pos,
+ * s, deriv and virial are device pointers on the current device; box is
+ * host; stream is a cudaStream_t or NULL.  The call allocates nothing and
+ * clears the parts of the shared array that must start at zero; calls that
+ * overlap on the GPU share the array and race.  The first call on a device
+ * looks the array up with cudaGetSymbolAddress: make it before any stream
+ * capture.  More than COORD_NOALLOC_MAX_SLOTS slots: COORD_ERR_ARG. */
+#define COORD_NOALLOC_MAX_SLOTS 32768
+int coord_forward_noalloc(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, const int64_t *group_b, int64_t n_b,
+                          const double *pos, const double box[9], double *s, double *deriv, double *virial,
+                          void *stream);
+
 /* ---- tuning and measurement ------------------------------------------------ */
 /* Run the autotuner for this context's shapes now (it otherwise runs on the
  * first forward).  Returns the chosen configuration as text. */

@@ -94,6 +94,8 @@ def load() -> C.CDLL:
         L.coord_launch_count.restype = C.c_int64
         L.coord_last_kernel_ms.argtypes = [_vp, _dp, C.POINTER(C.c_int)]
         L.coord_set_timing.argtypes = [_vp, C.c_int]
+        L.coord_forward_noalloc.argtypes = [_vp, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_int64), C.c_int64,
+                                            _vp, _dp, _vp, _vp, _vp, _vp]
         _lib = L
         return L
 

@@ -28,6 +28,7 @@ SOURCES = {
     "coord_api.cu": [],
     "multi.cu": [],
     "peaks.cu": [],
+    "noalloc.cu": ["-fmad=false"],
     "host_setup.cpp": [],
 }
 HEADERS = ["coord_internal.h", "switch_eval.cuh", "kargs.h", "kernels.cuh", "eval.cuh", "launch.h"]

@@ -502,6 +502,22 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   return COORD_OK;
 }
 
+} // namespace
+
+namespace coordgpu {
+int ctx_noalloc_view(const coord_ctx *c, const SwitchParams **sw, const coord_params **p) {
+  if (!c) return COORD_ERR_ARG;
+  *sw = &c->sw;
+  *p = &c->p;
+  return COORD_OK;
+}
+void ctx_set_error(coord_ctx *c, const char *msg) {
+  if (c) c->err = msg;
+}
+} // namespace coordgpu
+
+namespace {
+
 int device_init(coord_ctx *c) {
   if (c->stream) {
     cudaSetDevice(c->p.device);
