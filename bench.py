@@ -271,6 +271,18 @@ def run_ours(args):
     ms_step = t / args.steps * 1e3
     value = pairs_per_step * ws * args.steps / t
 
+    # cost of one neighbour-list rebuild step against a plain step (same inputs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step,
+                     flags=_lib.FLAG_REBUILD)
+    torch.cuda.synchronize()
+    t_rebuild_step = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step + 1)
+    torch.cuda.synchronize()
+    t_plain_step = time.perf_counter() - t0
+
     # the plain FP64 GPU path on the same workload (the drop-in, for the 5x target)
     c64 = Coordination(line, precision="fp64", device=local)
     st64 = 0
@@ -345,6 +357,7 @@ def run_ours(args):
                        "atoms": n, "walkers_per_gpu": W, "pairs_per_step_per_gpu": pairs_per_step,
                        "cv_force_us_per_step": ms_step * 1e3, "us_per_walker_step": ms_step * 1e3 / W,
                        "fp64_gpu_ms_per_step": t64 * 1e3,
+                       "rebuild_step_ms": t_rebuild_step * 1e3, "plain_step_ms": t_plain_step * 1e3,
                        "mixed_over_fp64_speedup": (t64 * 1e3) / ms_step,
                        "backward": False, "l2": "working set (0.8 GB) larger than the 129 MB L2",
                        "parallelism": "walkers sharded across GPUs, no collective"},

@@ -27,7 +27,9 @@
  *  - No function allocates or frees caller memory; the context owns its
  *    device buffers.  Host-pointer functions copy in/out through pinned
  *    staging on the context's stream; *_device functions take device pointers
- *    and a cudaStream_t passed as void* (NULL = the context's own stream).
+ *    and a cudaStream_t passed as void*.  NULL orders the call like work on
+ *    the legacy default stream (it runs on the context's own stream, fenced
+ *    with events against the default stream on both sides).
  *  - A context is not thread-safe; use one per action instance (the
  *    reference's contract: one Colvar per action, CoordinationBase.h:33).
  */

@@ -67,6 +67,7 @@ struct coord_ctx {
   SwitchF32 s32{};
   int mode = MODE_SINGLE;
   int64_t nA = 0, nB = 0, ns = 0;
+  std::vector<int64_t> abs_host;  // GROUPA then GROUPB absolute indices
   bool groups_set = false;
   std::string err;
   cudaStream_t stream = nullptr;
@@ -79,7 +80,7 @@ struct coord_ctx {
   // device buffers
   DevBuf<int64_t> abs_of_slot;
   DevBuf<FrameConst> fc;
-  DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, scatter_tmp, row_len, slice_w;
+  DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, scatter_tmp, row_len, slice_w, cell_of_rank;
   DevBuf<double4> x64;
   DevBuf<uint4> q;
   DevBuf<uint32_t> ell, self_pairs;
@@ -96,7 +97,7 @@ struct coord_ctx {
   std::vector<FrameConst> fc_uploaded;
   std::vector<double> boxes_seen;
   // tuning
-  int tile64 = 64, tile32 = 128, ap_blocks = 0;
+  int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0;
   bool tuned = false;
   // timing: one event pair per pair-kernel launch while enabled
   bool timing = false;
@@ -207,6 +208,7 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   }
   ENS(c->fc, F);
   ENS(c->slot_of_rank, F * ns);
+  ENS(c->cell_of_rank, F * ns);
   ENS(c->cell_of_slot, F * ns);
   ENS(c->scatter_tmp, F * ns);
   ENS(c->row_len, F * ns);
@@ -256,6 +258,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.cell_start = c->cell_start.p;
   a.cell_fill = c->cell_fill.p;
   a.slot_of_rank = c->slot_of_rank.p;
+  a.cell_of_rank = c->cell_of_rank.p;
   a.scatter_tmp = c->scatter_tmp.p;
   a.x64 = c->x64.p;
   a.q = c->q.p;
@@ -312,6 +315,7 @@ int estimate_cap(coord_ctx *c, const double *box) {
 
 int set_tuning_defaults(coord_ctx *c) {
   if (c->ap_blocks == 0) c->ap_blocks = std::max(1, c->nsm) * 8;
+  if (c->nl_blocks == 0) c->nl_blocks = std::max(1, c->nsm) * 4;  // 4 resident 256-thread blocks per SM
   return 0;
 }
 
@@ -374,7 +378,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
   } else {
     if (mixed) {
       launch_gather(a, 1, 0, 1, c->stream);
-      launch_eval_nl32(a, c->sw, c->s32, mode, c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, mode, c->nl_blocks, c->stream);
     } else {
       launch_gather(a, 1, 1, 0, c->stream);
       launch_eval_nl64(a, c->sw, mode, c->stream);
@@ -430,6 +434,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   }
   set_tuning_defaults(c);
   c->max_blocks = std::max<int>(c->max_blocks, std::max<int>((int)((c->ns + 255) / 256), c->ap_blocks));
+  c->max_blocks = std::max<int>(c->max_blocks, c->nl_blocks);
   c->max_blocks = std::max<int>(c->max_blocks, (int)((std::max<int64_t>(c->nA, 1) + 255) / 256));
   int rc = ensure_buffers(c, n_frames);
   if (rc) return rc;
@@ -513,6 +518,18 @@ int ctx_noalloc_view(const coord_ctx *c, const SwitchParams **sw, const coord_pa
 }
 void ctx_set_error(coord_ctx *c, const char *msg) {
   if (c) c->err = msg;
+}
+int ctx_multi_view(coord_ctx *c, MultiView *v) {
+  if (!c || !v) return COORD_ERR_ARG;
+  if (!c->groups_set) return COORD_ERR_STATE;
+  v->p = &c->p;
+  v->sw = &c->sw;
+  v->s32 = &c->s32;
+  v->mode = c->mode;
+  v->nA = c->nA;
+  v->ns = c->ns;
+  v->abs = c->abs_host.data();
+  return COORD_OK;
 }
 } // namespace coordgpu
 
@@ -634,6 +651,7 @@ int coord_destroy(coord_ctx *c) {
   c->cell_start.release();
   c->cell_fill.release();
   c->slot_of_rank.release();
+  c->cell_of_rank.release();
   c->scatter_tmp.release();
   c->row_len.release();
   c->slice_w.release();
@@ -687,6 +705,7 @@ int coord_set_groups(coord_ctx *c, const int64_t *a, int64_t na, const int64_t *
   std::vector<int64_t> abs(std::max<int64_t>(c->ns, 1));
   for (int64_t i = 0; i < na; i++) abs[i] = a[i];
   for (int64_t i = 0; i < nb; i++) abs[na + i] = b[i];
+  c->abs_host.assign(abs.begin(), abs.begin() + c->ns);
   if (int rc = device_init(c)) return rc;
   cudaError_t e = c->abs_of_slot.ensure(abs.size());
   if (e != cudaSuccess) return c->cuda_fail(e, "allocation");
@@ -721,11 +740,33 @@ int coord_get_nslots(const coord_ctx *c, int64_t *nslots) {
   return COORD_OK;
 }
 
+// With no stream given, the work runs on the context's stream but is ordered
+// after everything issued so far on the legacy default stream and before
+// anything issued there afterwards (events on both sides), as if it had been
+// issued on that stream.
+struct DefaultStreamFence {
+  coord_ctx *c;
+  bool on;
+  DefaultStreamFence(coord_ctx *cc, void *stream) : c(cc), on(stream == nullptr && cc->stream != nullptr) {
+    if (on) {
+      cudaEventRecord(c->ev0, cudaStreamLegacy);
+      cudaStreamWaitEvent(c->stream, c->ev0, 0);
+    }
+  }
+  ~DefaultStreamFence() {
+    if (on) {
+      cudaEventRecord(c->ev1, c->stream);
+      cudaStreamWaitEvent(cudaStreamLegacy, c->ev1, 0);
+    }
+  }
+};
+
 int coord_forward_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes, int64_t step,
                          unsigned flags, double *s, double *deriv, double *virial, double *dparam, void *stream) {
   if (!c) return COORD_ERR_ARG;
   if (!boxes || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions or boxes");
   cudaSetDevice(c->p.device);
+  DefaultStreamFence fence(c, stream);
   return forward_impl(c, n_frames, pos, boxes, step, flags, s, deriv, virial, dparam, (cudaStream_t)stream);
 }
 
@@ -780,6 +821,7 @@ int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const d
   const bool nl = c->p.nlist != COORD_NL_NONE;
   if (nl && c->built_frames != n_frames)
     return c->fail(COORD_ERR_STATE, "backward needs the neighbour lists of a forward call with the same frames");
+  DefaultStreamFence fence(c, stream);
   cudaStream_t saved = c->stream;
   if (stream) c->stream = (cudaStream_t)stream;
   struct Restore {

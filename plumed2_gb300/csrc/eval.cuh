@@ -143,45 +143,70 @@ struct Acc32 {
   }
 };
 
+// Fire-and-forget vector reduction into a float4 accumulator (16-byte aligned).
+__device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z), "f"(0.f)
+               : "memory");
+}
+
+// Persistent warps: warp w of the frame's grid takes slices w, w + nw, ...;
+// the per-thread accumulators carry across slices and one block reduction
+// closes the kernel.  Inside a slice the loop runs to the slice width (warp
+// uniform); entries and partner positions are loaded kUnroll at a time before
+// any is used, so kUnroll gathers are in flight per lane.
+constexpr int kUnroll = 4;
+
 template <int NH, int MODE>
 __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int nw = gridDim.x * wpb;
   const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const uint4 *__restrict__ q = a.q + fo;
+  float4 *__restrict__ acc4 = a.acc32 + fo;
   Acc32 acc;
-  if (r < a.ns) {
-    const FrameConst &fc = a.fc[f];
-    const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
-    const int len = a.row_len[fo + r];
-    const uint4 qr = a.q[fo + r];
+  for (int slice = blockIdx.x * wpb + (threadIdx.x >> 5); slice < a.nslices; slice += nw) {
+    const int r = slice * 32 + lane;
+    const bool active = r < a.ns;
+    const int len = active ? a.row_len[fo + r] : 0;
+    const int w = a.slice_w[(size_t)f * a.nslices + slice];
+    const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
     float ax = 0.f, ay = 0.f, az = 0.f;
-    const uint32_t *e = a.ell + ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
-    for (int k = 0; k < len; k++) {
-      const uint32_t ent = __ldg(e + (size_t)k * 32);
-      const int p = (int)(ent & kRankMask);
-      const uint4 qp = __ldg(a.q + fo + p);
-      const float dx = fixed_delta(qr.x, qp.x, sx);
-      const float dy = fixed_delta(qr.y, qp.y, sy);
-      const float dz = fixed_delta(qr.z, qp.z, sz);
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (r2 <= s32.dmax2) {
-        float sig, df;
-        sw32<NH>(sw, s32, r2, sig, df);
-        acc.add_s(sig);
-        if (MODE >= EVAL_DERIV) {
-          // d = x_p - x_r: deriv[r] -= df d, deriv[p] += df d (either orientation)
-          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
-          ax -= ddx;
-          ay -= ddy;
-          az -= ddz;
-          atomicAdd(a.acc32 + fo + p, make_float4(ddx, ddy, ddz, 0.f));
-          acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+    const uint32_t *__restrict__ e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    for (int k = 0; k < w; k += kUnroll) {
+      int p[kUnroll];
+      uint4 qp[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldg(e + (size_t)(k + u) * 32) & kRankMask) : -1;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) {
+        const float dx = fixed_delta(qr.x, qp[u].x, sx);
+        const float dy = fixed_delta(qr.y, qp[u].y, sy);
+        const float dz = fixed_delta(qr.z, qp[u].z, sz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (p[u] >= 0 && r2 <= s32.dmax2) {
+          float sig, df;
+          sw32<NH>(sw, s32, r2, sig, df);
+          acc.add_s(sig);
+          if (MODE >= EVAL_DERIV) {
+            // d = x_p - x_r: deriv[r] -= df d, deriv[p] += df d (either orientation)
+            const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+            ax -= ddx;
+            ay -= ddy;
+            az -= ddz;
+            red_add_v4(acc4 + p[u], ddx, ddy, ddz);
+            acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+          }
+          if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
         }
-        if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
       }
     }
-    if (MODE >= EVAL_DERIV && len > 0) atomicAdd(a.acc32 + fo + r, make_float4(ax, ay, az, 0.f));
+    if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az);
   }
   double part[kPartials];
   acc.to_partials(part);

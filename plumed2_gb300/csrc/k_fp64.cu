@@ -24,8 +24,8 @@ void launch_nl_build(const KArgs &a, cudaStream_t s) {
   k_scan_cells<<<a.nframes, 1024, 0, s>>>(a);
   k_scatter<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
   k_cell_sort<<<dim3(std::min(a.ncell_cap, 65535), a.nframes), 64, 0, s>>>(a);
-  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1);
-  k_nl_search<<<grid1(a.ns, 128, a.nframes), 128, 0, s>>>(a);
+  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1, 1);
+  k_nl_search<<<dim3((a.nslices + kSearchWarps - 1) / kSearchWarps, a.nframes), kSearchWarps * 32, 0, s>>>(a);
   g_launches += 6;
 }
 
@@ -35,7 +35,7 @@ void launch_pair_flags(const KArgs &a, cudaStream_t s) {
 }
 
 void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s) {
-  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order, want64, wantq);
+  k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order, want64, wantq, 0);
   g_launches += 1;
 }
 

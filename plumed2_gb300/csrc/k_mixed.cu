@@ -43,8 +43,12 @@ static int nh_compiled(const SwitchParams &sw) {
   return (nh == 2 || nh == 3 || nh == 4 || nh == 6) ? nh : 0;
 }
 
-void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s) {
-#define CALL(N, M) k_eval_nl32<N, M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw, s32)
+void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
+                      cudaStream_t s) {
+  // persistent: nblocks blocks over all frames, at least one per frame
+  const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
+  const dim3 g(per_frame, a.nframes);
+#define CALL(N, M) k_eval_nl32<N, M><<<g, 256, 0, s>>>(a, sw, s32)
   NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL
   g_launches += 1;

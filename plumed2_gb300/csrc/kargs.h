@@ -30,6 +30,7 @@ struct KArgs {
   int *cell_start;              // [nframes][ncell_cap+1]
   int *cell_fill;               // [nframes][ncell_cap]
   int *slot_of_rank;            // [nframes][ns]
+  int *cell_of_rank;            // [nframes][ns] cell of each rank (neighbour-list build)
   int *scatter_tmp;             // [nframes][ns]
   double4 *x64;                 // [nframes][ns] sorted (or slot-order) FP64 positions
   uint4 *q;                     // [nframes][ns] fixed-point positions

@@ -345,11 +345,12 @@ __global__ void k_cell_sort(KArgs a) {
 
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter
 // and the mixed kernels).  rank_order==0: slot order.
-__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq) {
+__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
   const int f = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= a.ns) return;
   const int s = rank_order ? a.slot_of_rank[(size_t)f * a.ns + r] : r;
+  if (wantcell) a.cell_of_rank[(size_t)f * a.ns + r] = a.cell_of_slot[(size_t)f * a.ns + s];
   const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
   const double x0 = x[0], x1 = x[1], x2 = x[2];
   if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, 0.0);
@@ -376,108 +377,199 @@ __device__ __forceinline__ void cell_range(int c, int n, int wrap, int &lo, int 
 }
 __device__ __forceinline__ int wrap_cell(int v, int n) { return (v < 0) ? n - 1 : v % n; }
 
-__global__ void k_nl_search(KArgs a) {
+// Candidate p of row r: ownership, group, cutoff test; stores the entry.
+// Returns 1 for a stored entry (n advanced), 0 otherwise.  nself counts self
+// pairs (kept aside for coord_get_pairs).
+__device__ __forceinline__ void nl_candidate(const KArgs &a, const FrameConst &fc, int f, size_t fo, int r, int sr,
+                                             bool ra, const uint4 &qr, const double4 &xr4, long long absr, int p,
+                                             int sp, const uint4 &qp, size_t slice_base, int &n) {
+  if (p == r) return;
+  // ownership: even rank sum -> lower rank, odd -> higher rank
+  const bool own = ((r + p) & 1) ? (r > p) : (r < p);
+  if (!own) return;
+  bool r_first;
+  if (a.mode == MODE_TWO) {
+    if (ra == (sp < a.nA)) return;
+    r_first = ra;
+  } else {
+    r_first = sr < sp;
+  }
+  bool accept;
+  if (a.nl_kind == 2) {
+    accept = true;  // NLISTCELLS: every pair of neighbouring cells (NeighborList.cpp:194-231)
+  } else {
+    accept = false;
+    bool exact = true;
+    if (fc.fixed_ok) {
+      const float dx = fixed_delta(qr.x, qp.x, fc.scale[0]);
+      const float dy = fixed_delta(qr.y, qp.y, fc.scale[1]);
+      const float dz = fixed_delta(qr.z, qp.z, fc.scale[2]);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 > fc.cut2_hi) {
+        exact = false;
+      } else if (r2 < fc.cut2_lo) {
+        exact = false;
+        accept = true;
+      }
+    }
+    if (exact) {
+      // the reference's own test: modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
+      const double4 xp4 = a.x64[fo + p];
+      const double va[3] = {xr4.x, xr4.y, xr4.z}, vb[3] = {xp4.x, xp4.y, xp4.z};
+      double d[3];
+      const double *v1 = r_first ? va : vb, *v2 = r_first ? vb : va;
+      if (a.do_pbc)
+        pbc_distance(fc.pbc, v1, v2, d);
+      else
+        for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+      accept = mod2(d) <= fc.cut2;
+    }
+  }
+  if (!accept) return;
+  if (a.abs_of_slot[sp] == absr) {
+    // a self pair: counted in the list size, skipped by the CV loop
+    // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
+    unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
+    if (k < (unsigned long long)a.self_cap) {
+      a.self_pairs[((size_t)f * a.self_cap + k) * 2] = r_first ? sr : sp;
+      a.self_pairs[((size_t)f * a.self_cap + k) * 2 + 1] = r_first ? sp : sr;
+    }
+    return;
+  }
+  if (n < a.cap) a.ell[slice_base + (size_t)n * 32] = (uint32_t)p | (r_first ? kOrientBit : 0u);
+  n++;
+}
+
+// x-adjacency of cells cx and cxp in a row of nc cells: the required-cell
+// rule of LinkCells::addRequiredCells for one dimension.
+__device__ __forceinline__ bool x_adjacent(int cx, int cxp, int nc, int wrap) {
+  if (wrap) {
+    if (nc < 3) return true;
+    const int d = (cxp - cx + nc) % nc;
+    return d == 0 || d == 1 || d == nc - 1;
+  }
+  return abs(cxp - cx) <= 1;
+}
+
+// One warp per slice of 32 ranks.  Fast path: when the slice's rows lie in one
+// x-row of cells, the candidates of all 32 rows are the ranks of at most 9
+// contiguous row segments (ranks are cell-major, x fastest); they are staged
+// through shared memory 32 at a time and every lane tests them (broadcast
+// reads, no divergence in the loop).  A slice spanning two x-rows takes the
+// per-lane path over its own required cells.
+constexpr int kSearchWarps = 4;
+
+__global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
   const int f = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const bool active = r < a.ns;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slice = blockIdx.x * kSearchWarps + warp;
+  const int r = slice * 32 + lane;
+  const bool active = r < a.ns && slice < a.nslices;
   const FrameConst &fc = a.fc[f];
   const GridParams &g = fc.grid;
   const size_t fo = (size_t)f * a.ns;
   const int *slot_of_rank = a.slot_of_rank + fo;
   const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
+  __shared__ uint4 sq[kSearchWarps][32];
+  __shared__ int sslot[kSearchWarps][32];
+  __shared__ int scx[kSearchWarps][32];
   int n = 0;
-  unsigned long long nself = 0;
-  if (active && g.ncells > 0) {
-    const int sr = slot_of_rank[r];
+  if (slice < a.nslices && g.ncells > 0) {
+    const int sr = active ? slot_of_rank[r] : 0;
     const bool ra = sr < a.nA;
-    const int cr = a.cell_of_slot[fo + sr];
+    const int cr = active ? a.cell_of_rank[fo + r] : 0;
     const int cx = cr % g.nc[0], cy = (cr / g.nc[0]) % g.nc[1], cz = cr / (g.nc[0] * g.nc[1]);
-    const double4 xr4 = a.x64[fo + r];
-    const uint4 qr = a.q[fo + r];
-    const int64_t absr = a.abs_of_slot[sr];
+    const double4 xr4 = active ? a.x64[fo + r] : make_double4(0, 0, 0, 0);
+    const uint4 qr = active ? a.q[fo + r] : make_uint4(0, 0, 0, 0);
+    const long long absr = active ? a.abs_of_slot[sr] : 0;
     const int cwrap = (a.nl_kind == 2) ? a.do_pbc : g.wrap;
-    int x0, x1, y0, y1, z0, z1;
-    cell_range(cx, g.nc[0], cwrap, x0, x1);
-    cell_range(cy, g.nc[1], cwrap, y0, y1);
-    cell_range(cz, g.nc[2], cwrap, z0, z1);
-    const size_t slice_base = ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
-    for (int nx = x0; nx < x1; ++nx)
+    const size_t slice_base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    // the x-row of the slice's first and last active rows
+    const int last = min(31, a.ns - 1 - slice * 32);
+    const int cfirst = __shfl_sync(0xffffffffu, cr, 0), clast = __shfl_sync(0xffffffffu, cr, last);
+    const int rowfirst = cfirst / g.nc[0], rowlast = clast / g.nc[0];
+    if (rowfirst == rowlast) {
+      const int cxa = cfirst % g.nc[0], cxb = clast % g.nc[0];
+      // x intervals (at most two) covering every lane's x neighbours once
+      int xi0[2], xi1[2], nint;
+      if (cxb - cxa + 3 >= g.nc[0]) {
+        xi0[0] = 0;
+        xi1[0] = g.nc[0] - 1;
+        nint = 1;
+      } else if (cwrap) {
+        const int lo = cxa - 1, hi = cxb + 1;
+        if (lo < 0) {
+          xi0[0] = g.nc[0] - 1;
+          xi1[0] = g.nc[0] - 1;
+          xi0[1] = 0;
+          xi1[1] = hi;
+          nint = 2;
+        } else if (hi >= g.nc[0]) {
+          xi0[0] = lo;
+          xi1[0] = g.nc[0] - 1;
+          xi0[1] = 0;
+          xi1[1] = hi - g.nc[0];
+          nint = 2;
+        } else {
+          xi0[0] = lo;
+          xi1[0] = hi;
+          nint = 1;
+        }
+      } else {
+        xi0[0] = max(cxa - 1, 0);
+        xi1[0] = min(cxb + 1, g.nc[0] - 1);
+        nint = 1;
+      }
+      int y0, y1, z0, z1;
+      cell_range(cy, g.nc[1], cwrap, y0, y1);
+      cell_range(cz, g.nc[2], cwrap, z0, z1);
       for (int ny = y0; ny < y1; ++ny)
         for (int nz = z0; nz < z1; ++nz) {
-          const int c = wrap_cell(nx, g.nc[0]) + wrap_cell(ny, g.nc[1]) * g.nc[0] +
-                        wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
-          const int pe = start[c + 1];
-          for (int p = start[c]; p < pe; p++) {
-            if (p == r) continue;
-            // ownership: even rank sum -> lower rank, odd -> higher rank
-            const bool own = ((r + p) & 1) ? (r > p) : (r < p);
-            if (!own) continue;
-            const int sp = slot_of_rank[p];
-            bool r_first;
-            if (a.mode == MODE_TWO) {
-              if (ra == (sp < a.nA)) continue;
-              r_first = ra;
-            } else {
-              r_first = sr < sp;
-            }
-            bool accept;
-            if (a.nl_kind == 2) {
-              accept = true;  // NLISTCELLS: every pair of neighbouring cells (NeighborList.cpp:194-231)
-            } else {
-              accept = false;
-              bool exact = true;
-              if (fc.fixed_ok) {
-                const uint4 qp = a.q[fo + p];
-                const float dx = fixed_delta(qr.x, qp.x, fc.scale[0]);
-                const float dy = fixed_delta(qr.y, qp.y, fc.scale[1]);
-                const float dz = fixed_delta(qr.z, qp.z, fc.scale[2]);
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > fc.cut2_hi) {
-                  exact = false;
-                } else if (r2 < fc.cut2_lo) {
-                  exact = false;
-                  accept = true;
+          const int rowcell = wrap_cell(ny, g.nc[1]) * g.nc[0] + wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
+          for (int it = 0; it < nint; it++) {
+            const int rb = start[rowcell + xi0[it]], re = start[rowcell + xi1[it] + 1];
+            for (int base = rb; base < re; base += 32) {
+              const int m = min(32, re - base);
+              if (lane < m) {
+                const int p = base + lane;
+                sq[warp][lane] = a.q[fo + p];
+                sslot[warp][lane] = slot_of_rank[p];
+                scx[warp][lane] = a.cell_of_rank[fo + p] % g.nc[0];
+              }
+              __syncwarp();
+              if (active)
+                for (int j = 0; j < m; j++) {
+                  if (!x_adjacent(cx, scx[warp][j], g.nc[0], cwrap)) continue;
+                  nl_candidate(a, fc, f, fo, r, sr, ra, qr, xr4, absr, base + j, sslot[warp][j], sq[warp][j],
+                               slice_base, n);
                 }
-              }
-              if (exact) {
-                // the reference's own test: modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
-                const double4 xp4 = a.x64[fo + p];
-                const double va[3] = {xr4.x, xr4.y, xr4.z}, vb[3] = {xp4.x, xp4.y, xp4.z};
-                double d[3];
-                const double *v1 = r_first ? va : vb, *v2 = r_first ? vb : va;
-                if (a.do_pbc)
-                  pbc_distance(fc.pbc, v1, v2, d);
-                else
-                  for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
-                accept = mod2(d) <= fc.cut2;
-              }
+              __syncwarp();
             }
-            if (!accept) continue;
-            if (a.abs_of_slot[sp] == absr) {
-              // a self pair: counted in the list size, skipped by the CV loop
-              // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
-              unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
-              if (k < (unsigned long long)a.self_cap) {
-                a.self_pairs[((size_t)f * a.self_cap + k) * 2] = r_first ? sr : sp;
-                a.self_pairs[((size_t)f * a.self_cap + k) * 2 + 1] = r_first ? sp : sr;
-              }
-              nself++;
-              continue;
-            }
-            if (n < a.cap) a.ell[slice_base + (size_t)n * 32] = (uint32_t)p | (r_first ? kOrientBit : 0u);
-            n++;
           }
         }
-    a.row_len[fo + r] = min(n, a.cap);
+    } else if (active) {
+      int x0, x1, y0, y1, z0, z1;
+      cell_range(cx, g.nc[0], cwrap, x0, x1);
+      cell_range(cy, g.nc[1], cwrap, y0, y1);
+      cell_range(cz, g.nc[2], cwrap, z0, z1);
+      for (int nx = x0; nx < x1; ++nx)
+        for (int ny = y0; ny < y1; ++ny)
+          for (int nz = z0; nz < z1; ++nz) {
+            const int c = wrap_cell(nx, g.nc[0]) + wrap_cell(ny, g.nc[1]) * g.nc[0] +
+                          wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
+            const int pe = start[c + 1];
+            for (int p = start[c]; p < pe; p++)
+              nl_candidate(a, fc, f, fo, r, sr, ra, qr, xr4, absr, p, slot_of_rank[p], a.q[fo + p], slice_base, n);
+          }
+    }
+    if (active) a.row_len[fo + r] = min(n, a.cap);
   }
   // per-warp bookkeeping: slice width, list size, overflow
   const int wmax = warp_max(active ? n : 0);
   unsigned long long tot = active ? (unsigned long long)n : 0ull;
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  (void)nself;
-  if (lane == 0 && (r >> 5) < a.nslices) {
-    a.slice_w[(size_t)f * a.nslices + (r >> 5)] = min(wmax, a.cap);
+  if (lane == 0 && slice < a.nslices) {
+    a.slice_w[(size_t)f * a.nslices + slice] = min(wmax, a.cap);
     atomicAdd(&a.nl_count[f * 4 + 0], tot);
     if (wmax > a.cap) atomicMax(&a.nl_count[f * 4 + 2], (unsigned long long)wmax);
   }

@@ -1,6 +1,7 @@
 // launch.h -- host launchers of the kernels (defined in k_fp64.cu / k_mixed.cu).
 #pragma once
 #include "kargs.h"
+#include "coordgpu.h"
 #include <atomic>
 
 namespace coordgpu {
@@ -21,7 +22,8 @@ void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, dou
                       cudaStream_t s);
 
 // k_mixed.cu
-void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s);
+void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
+                      cudaStream_t s);
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s);
 void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,
@@ -30,6 +32,17 @@ void launch_finalize32(const KArgs &a, int rank_order, cudaStream_t s);
 
 // number of 32-lane switch specialisations compiled for the mixed path
 int mixed_nh(const SwitchParams &sw);  // N/2 of fixedRational<N>, or 0 for the generic evaluator
+
+// what multi.cu needs to know about a context (coord_api.cu)
+struct MultiView {
+  const coord_params *p;
+  const SwitchParams *sw;
+  const SwitchF32 *s32;
+  int mode;
+  int64_t nA, ns;
+  const int64_t *abs;  // host copy of the groups
+};
+int ctx_multi_view(coord_ctx *c, MultiView *v);
 
 // peaks.cu
 int measure_peaks(int device, double *fp32, double *fp64, double *hbm);
