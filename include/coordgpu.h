@@ -112,6 +112,11 @@ int coord_switch_params(const coord_ctx *ctx, double out[7]);
 #define COORD_FLAG_REBUILD 1u   /* force a neighbour-list rebuild this step   */
 #define COORD_FLAG_NO_DERIV 2u  /* compute s only (no derivatives, no virial) */
 #define COORD_FLAG_DR0 4u       /* also return ds/dR_0 and ds/dD_0            */
+#define COORD_FLAG_SAVE 8u      /* keep ds/dx and the virial of this forward
+                                   (and ds/d(R_0,D_0) with COORD_FLAG_DR0) in
+                                   the context for the next
+                                   coord_backward_device (the positions must be
+                                   unchanged in between, like saved tensors)  */
 
 /* One step of CoordinationBase::prepare()+calculate() for one frame, host
  * buffers.  The neighbour list is rebuilt when the list is new, when
@@ -136,7 +141,10 @@ int coord_forward_device(coord_ctx *ctx, int n_frames, const double *pos, const 
  * g * ds/dh (h = box, scaled coordinates held fixed; the box-derivative
  * convention of ActionAtomistic.cpp:221-265), grad_param [n_frames][2] =
  * g * (ds/dR_0, ds/dD_0).  Reuses the neighbour list of the last forward;
- * any output pointer may be NULL. */
+ * any output pointer may be NULL.  After a forward with COORD_FLAG_SAVE on
+ * the same frames it only scales the saved quantities (an O(N) kernel; with
+ * grad_param set this needs COORD_FLAG_DR0 on that forward too); otherwise
+ * it runs a pair pass over the positions given. */
 int coord_backward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, const double *g,
                           double *grad_pos, double *grad_box, double *grad_param, void *stream);
 
@@ -187,8 +195,10 @@ int coord_forward_noalloc(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, c
                           void *stream);
 
 /* ---- tuning and measurement ------------------------------------------------ */
-/* Run the autotuner for this context's shapes now (it otherwise runs on the
- * first forward).  Returns the chosen configuration as text. */
+/* The configuration the autotuner chose for this context, as text.  The
+ * autotuner runs on the first forward of a mixed-precision neighbour-list
+ * context (blocks per SM x gathers in flight, each timed once); batches
+ * (coord_multi_*) tune tile size x blocks per SM on their first call. */
 int coord_autotune(coord_ctx *ctx, char *desc, size_t desclen);
 /* Microbenchmarks of the device (FP32 FMA, FP64 FMA TFLOP/s, HBM copy GB/s). */
 int coord_measure_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *hbm_gbs);

@@ -26,7 +26,7 @@ COORD_ERR_STATE = 7
 
 NL_NONE, NL_CLASSIC, NL_CELLS = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
-FLAG_REBUILD, FLAG_NO_DERIV, FLAG_DR0 = 1, 2, 4
+FLAG_REBUILD, FLAG_NO_DERIV, FLAG_DR0, FLAG_SAVE = 1, 2, 4, 8
 
 
 class CoordParams(C.Structure):

@@ -20,7 +20,11 @@ template <typename T> struct DevBuf {
   size_t n = 0;
   cudaError_t ensure(size_t want) {
     if (want <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
+    // kernels queued on any stream may still use the old buffer
+    if (p) {
+      cudaDeviceSynchronize();
+      cudaFree(p);
+    }
     p = nullptr;
     n = 0;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
@@ -91,13 +95,18 @@ struct coord_ctx {
   DevBuf<unsigned> tickets;
   // host-API staging
   DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam, d_bvir, d_bpar;
+  // saved forward (COORD_FLAG_SAVE)
+  DevBuf<double> sv_deriv, sv_vir, sv_par;
+  bool saved_valid = false, saved_param = false;
+  int saved_frames = 0;
   HostBuf<double> h_pos, h_out;
   HostBuf<FrameConst> h_fc;
   HostBuf<unsigned long long> h_nl;
   std::vector<FrameConst> fc_uploaded;
   std::vector<double> boxes_seen;
   // tuning
-  int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0;
+  int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0, nl_unroll = 4;
+  int cells_launch = 0;  // cells per frame known on the host (0: use ncell_cap)
   bool tuned = false;
   // timing: one event pair per pair-kernel launch while enabled
   bool timing = false;
@@ -272,6 +281,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.acc32 = c->acc32.p;
   a.partials = c->partials.p;
   a.max_blocks = c->max_blocks;
+  a.cells_launch = c->cells_launch > 0 ? c->cells_launch : c->ncell_cap;
   a.tickets = c->tickets.p;
   a.out_s = s;
   a.out_deriv = deriv;
@@ -378,7 +388,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
   } else {
     if (mixed) {
       launch_gather(a, 1, 0, 1, c->stream);
-      launch_eval_nl32(a, c->sw, c->s32, mode, c->nl_blocks, c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, mode, c->nl_blocks, c->nl_unroll, c->stream);
     } else {
       launch_gather(a, 1, 1, 0, c->stream);
       launch_eval_nl64(a, c->sw, mode, c->stream);
@@ -390,6 +400,50 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
     launch_finalize32(a, rank_order, c->stream);
   else
     launch_finalize64(a, rank_order, c->stream);
+}
+
+// The project's autotuner for the mixed neighbour-list pass: blocks per SM
+// (2, 4, 6, 8 resident 256-thread blocks) x gathers in flight per lane
+// (unroll 2, 4, 8), each candidate timed once with CUDA events on the
+// context's stream; the fastest is kept for the context.  Every candidate run
+// is a complete pass (its finalize kernel rewrites the outputs), so the
+// results of the call are unaffected.
+void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  const int bps[4] = {2, 4, 6, 8}, unr[3] = {2, 4, 8};
+  float best = 1e30f;
+  int bb = c->nl_blocks, bu = c->nl_unroll;
+  const bool timing = c->timing;
+  c->timing = false;
+  for (int b : bps)
+    for (int u : unr) {
+      c->nl_blocks = b * std::max(c->nsm, 1);
+      c->nl_unroll = u;
+      c->max_blocks = std::max(c->max_blocks, c->nl_blocks);
+      if (ensure_buffers(c, a.nframes)) continue;
+      KArgs aa = a;
+      aa.partials = c->partials.p;
+      aa.max_blocks = c->max_blocks;
+      cudaEventRecord(t0, c->stream);
+      launch_evaluation(c, aa, mode);
+      cudaEventRecord(t1, c->stream);
+      cudaEventSynchronize(t1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (ms < best) {
+        best = ms;
+        bb = c->nl_blocks;
+        bu = u;
+      }
+    }
+  c->nl_blocks = bb;
+  c->nl_unroll = bu;
+  c->timing = timing;
+  c->tuned = true;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
 }
 
 int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
@@ -423,14 +477,18 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   // sizes
   if (c->cap == 0 && nl) c->cap = estimate_cap(c, boxes);
   {
-    int need_cells = (int)std::max<int64_t>(c->ns, 64);
+    int need_cells = (int)std::max<int64_t>(c->ns, 64), host_cells = 0;
+    bool device_cells = false;
     for (int f = 0; f < n_frames; f++) {
       FrameConst tmp;
       bool nb;
       frame_setup(c, boxes + 9 * (size_t)f, &tmp, &nb);
       need_cells = std::max(need_cells, tmp.grid.ncells);
+      host_cells = std::max(host_cells, tmp.grid.ncells);
+      device_cells = device_cells || nb;
     }
     if (need_cells > c->ncell_cap) c->ncell_cap = need_cells;
+    c->cells_launch = device_cells ? 0 : host_cells;
   }
   set_tuning_defaults(c);
   c->max_blocks = std::max<int>(c->max_blocks, std::max<int>((int)((c->ns + 255) / 256), c->ap_blocks));
@@ -442,8 +500,18 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   rc = upload_frames(c, n_frames, boxes, &need_bounds);
   if (rc) return rc;
 
-  KArgs a = make_args(c, n_frames, d_pos, flags, s, (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv,
-                      (flags & COORD_FLAG_NO_DERIV) ? nullptr : virial, dparam);
+  const bool save = (flags & COORD_FLAG_SAVE) && !(flags & COORD_FLAG_NO_DERIV);
+  c->saved_valid = false;
+  if (save) {
+    cudaError_t es;
+    if ((es = c->sv_deriv.ensure((size_t)n_frames * c->ns * 3)) || (es = c->sv_vir.ensure((size_t)n_frames * 9)) ||
+        (es = c->sv_par.ensure((size_t)n_frames * 2)))
+      return c->cuda_fail(es, "allocation of the saved forward");
+  }
+  double *const k_deriv = (flags & COORD_FLAG_NO_DERIV) ? nullptr : (save ? c->sv_deriv.p : deriv);
+  double *const k_virial = (flags & COORD_FLAG_NO_DERIV) ? nullptr : (save ? c->sv_vir.p : virial);
+  double *const k_dparam = save ? c->sv_par.p : dparam;
+  KArgs a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
   cudaError_t e;
   if (rebuild) cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
   if (need_bounds && (mixed || rebuild)) {
@@ -490,8 +558,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
         }
         if (!again) break;
         if ((rc = ensure_buffers(c, n_frames))) return rc;
-        a = make_args(c, n_frames, d_pos, flags, s, (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv,
-                      (flags & COORD_FLAG_NO_DERIV) ? nullptr : virial, dparam);
+        a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
         if (attempt == 7) return c->fail(COORD_ERR_NOMEM, "neighbour list did not fit after 8 attempts");
       }
     }
@@ -502,7 +569,24 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   const int mode = (flags & COORD_FLAG_NO_DERIV) ? EVAL_S : ((flags & COORD_FLAG_DR0) ? EVAL_PARAM : EVAL_DERIV);
   if (mode == EVAL_PARAM && !c->sw.grad_ok)
     return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
+  if (!c->tuned && mixed && nl && c->mode != MODE_PAIR) {
+    autotune_nl(c, a, mode);
+    a.partials = c->partials.p;
+    a.max_blocks = c->max_blocks;
+  }
   launch_evaluation(c, a, mode);
+  if (save) {
+    // hand the caller its copies of what was kept
+    const size_t nd = (size_t)n_frames * c->ns * 3;
+    if (deriv && nd) cudaMemcpyAsync(deriv, c->sv_deriv.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    if (virial) cudaMemcpyAsync(virial, c->sv_vir.p, (size_t)n_frames * 9 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c->stream);
+    c->saved_param = (flags & COORD_FLAG_DR0) != 0;
+    if (dparam && c->saved_param)
+      cudaMemcpyAsync(dparam, c->sv_par.p, (size_t)n_frames * 2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    c->saved_valid = true;
+    c->saved_frames = n_frames;
+  }
   if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "kernel launch");
   return COORD_OK;
 }
@@ -673,6 +757,9 @@ int coord_destroy(coord_ctx *c) {
   c->d_dparam.release();
   c->d_bvir.release();
   c->d_bpar.release();
+  c->sv_deriv.release();
+  c->sv_vir.release();
+  c->sv_par.release();
   c->h_pos.release();
   c->h_out.release();
   c->h_fc.release();
@@ -832,6 +919,15 @@ int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const d
   cudaError_t e;
   if ((e = c->d_bvir.ensure((size_t)9 * n_frames)) || (e = c->d_bpar.ensure((size_t)2 * n_frames)))
     return c->cuda_fail(e, "allocation");
+  if (c->saved_valid && c->saved_frames == n_frames && (!grad_param || c->saved_param)) {
+    // the forward kept ds/dx, the virial and ds/d(R_0, D_0): scale them
+    KArgs a = make_args(c, n_frames, pos, 0, nullptr, nullptr, nullptr, nullptr);
+    a.g = g;
+    if (grad_pos && c->ns) launch_scale_saved(a, c->sv_deriv.p, grad_pos, c->stream);
+    if (grad_box || grad_param) launch_grad_post(a, c->sv_vir.p, c->sv_par.p, grad_box, grad_param, c->stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "backward launch");
+    return COORD_OK;
+  }
   bool need_bounds = false;
   int rc = upload_frames(c, n_frames, boxes, &need_bounds);
   if (rc) return rc;
@@ -920,7 +1016,9 @@ int coord_get_pairs(coord_ctx *c, int frame, uint32_t *pairs, int64_t cap, int64
 
 int coord_autotune(coord_ctx *c, char *desc, size_t desclen) {
   if (!c) return COORD_ERR_ARG;
-  if (desc && desclen) std::snprintf(desc, desclen, "tile64=%d tile32=%d blocks=%d", c->tile64, c->tile32, c->ap_blocks);
+  if (desc && desclen)
+    std::snprintf(desc, desclen, "tuned=%d nl_blocks=%d nl_unroll=%d allpairs_tile64=%d allpairs_tile32=%d blocks=%d",
+                  (int)c->tuned, c->nl_blocks, c->nl_unroll, c->tile64, c->tile32, c->ap_blocks);
   return COORD_OK;
 }
 

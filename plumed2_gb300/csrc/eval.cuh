@@ -154,9 +154,9 @@ __device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z)
 // closes the kernel.  Inside a slice the loop runs to the slice width (warp
 // uniform); entries and partner positions are loaded kUnroll at a time before
 // any is used, so kUnroll gathers are in flight per lane.
-constexpr int kUnroll = 4;
-
-template <int NH, int MODE>
+// Entries are streamed once per step (ld.global.cs: evict first) so that the
+// fixed-point positions, gathered many times, stay resident in L2.
+template <int NH, int MODE, int kUnroll>
 __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y;
   const int lane = threadIdx.x & 31;
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
       int p[kUnroll];
       uint4 qp[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldg(e + (size_t)(k + u) * 32) & kRankMask) : -1;
+      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldcs(e + (size_t)(k + u) * 32) & kRankMask) : -1;
 #pragma unroll
       for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
 #pragma unroll

@@ -23,7 +23,7 @@ void launch_nl_build(const KArgs &a, cudaStream_t s) {
   k_bin<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
   k_scan_cells<<<a.nframes, 1024, 0, s>>>(a);
   k_scatter<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
-  k_cell_sort<<<dim3(std::min(a.ncell_cap, 65535), a.nframes), 64, 0, s>>>(a);
+  k_cell_sort<<<dim3(std::max(1, std::min(a.cells_launch, 65535)), a.nframes), 64, 0, s>>>(a);
   k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1, 1);
   k_nl_search<<<dim3((a.nslices + kSearchWarps - 1) / kSearchWarps, a.nframes), kSearchWarps * 32, 0, s>>>(a);
   g_launches += 6;
@@ -80,6 +80,12 @@ void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_fl
 #define CALL(M) k_pairs64<M><<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, use_flags)
   MODE_DISPATCH(mode, CALL)
 #undef CALL
+  g_launches += 1;
+}
+
+void launch_scale_saved(const KArgs &a, const double *saved, double *grad, cudaStream_t s) {
+  const size_t n = (size_t)a.ns * 3;
+  k_scale_saved<<<dim3((unsigned)((n + 255) / 256), a.nframes), 256, 0, s>>>(a, saved, grad);
   g_launches += 1;
 }
 

@@ -44,6 +44,7 @@ struct KArgs {
   float4 *acc32;                // [nframes][ns]    derivative accumulators (mixed path)
   double *partials;             // [nframes][max_blocks][kPartials]
   int max_blocks;
+  int cells_launch;             // blocks of the per-cell sort (cells per frame, when known)
   unsigned *tickets;            // [nframes]
   double *out_s;                // [nframes]
   double *out_deriv;            // [nframes][ns][3] slot order

@@ -377,16 +377,30 @@ __device__ __forceinline__ void cell_range(int c, int n, int wrap, int &lo, int 
 }
 __device__ __forceinline__ int wrap_cell(int v, int n) { return (v < 0) ? n - 1 : v % n; }
 
-// Candidate p of row r: ownership, group, cutoff test; stores the entry.
-// Returns 1 for a stored entry (n advanced), 0 otherwise.  nself counts self
-// pairs (kept aside for coord_get_pairs).
+// Candidate p of row r: ownership, cutoff test, group; stores the entry.
+// Ordered so the common case (a candidate beyond the cutoff) costs an
+// ownership test and an FP32 fixed-point distance; the slot, orientation,
+// absolute indices and FP64 positions are read only for candidates that
+// survive (about one in ten).
 __device__ __forceinline__ void nl_candidate(const KArgs &a, const FrameConst &fc, int f, size_t fo, int r, int sr,
-                                             bool ra, const uint4 &qr, const double4 &xr4, long long absr, int p,
-                                             int sp, const uint4 &qp, size_t slice_base, int &n) {
+                                             bool ra, const uint4 &qr, int p, int sp, const uint4 &qp,
+                                             size_t slice_base, int &n) {
   if (p == r) return;
   // ownership: even rank sum -> lower rank, odd -> higher rank
-  const bool own = ((r + p) & 1) ? (r > p) : (r < p);
-  if (!own) return;
+  if (((r + p) & 1) ? (r < p) : (r > p)) return;
+  bool need_exact = true, accept = true;
+  if (a.nl_kind != 2) {
+    if (fc.fixed_ok) {
+      const float dx = fixed_delta(qr.x, qp.x, fc.scale[0]);
+      const float dy = fixed_delta(qr.y, qp.y, fc.scale[1]);
+      const float dz = fixed_delta(qr.z, qp.z, fc.scale[2]);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 > fc.cut2_hi) return;
+      need_exact = !(r2 < fc.cut2_lo);
+    }
+  } else {
+    need_exact = false;  // NLISTCELLS: every pair of neighbouring cells (NeighborList.cpp:194-231)
+  }
   bool r_first;
   if (a.mode == MODE_TWO) {
     if (ra == (sp < a.nA)) return;
@@ -394,39 +408,20 @@ __device__ __forceinline__ void nl_candidate(const KArgs &a, const FrameConst &f
   } else {
     r_first = sr < sp;
   }
-  bool accept;
-  if (a.nl_kind == 2) {
-    accept = true;  // NLISTCELLS: every pair of neighbouring cells (NeighborList.cpp:194-231)
-  } else {
-    accept = false;
-    bool exact = true;
-    if (fc.fixed_ok) {
-      const float dx = fixed_delta(qr.x, qp.x, fc.scale[0]);
-      const float dy = fixed_delta(qr.y, qp.y, fc.scale[1]);
-      const float dz = fixed_delta(qr.z, qp.z, fc.scale[2]);
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 > fc.cut2_hi) {
-        exact = false;
-      } else if (r2 < fc.cut2_lo) {
-        exact = false;
-        accept = true;
-      }
-    }
-    if (exact) {
-      // the reference's own test: modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
-      const double4 xp4 = a.x64[fo + p];
-      const double va[3] = {xr4.x, xr4.y, xr4.z}, vb[3] = {xp4.x, xp4.y, xp4.z};
-      double d[3];
-      const double *v1 = r_first ? va : vb, *v2 = r_first ? vb : va;
-      if (a.do_pbc)
-        pbc_distance(fc.pbc, v1, v2, d);
-      else
-        for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
-      accept = mod2(d) <= fc.cut2;
-    }
+  if (need_exact) {
+    // the reference's own test: modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
+    const double4 xr4 = a.x64[fo + r], xp4 = a.x64[fo + p];
+    const double va[3] = {xr4.x, xr4.y, xr4.z}, vb[3] = {xp4.x, xp4.y, xp4.z};
+    double d[3];
+    const double *v1 = r_first ? va : vb, *v2 = r_first ? vb : va;
+    if (a.do_pbc)
+      pbc_distance(fc.pbc, v1, v2, d);
+    else
+      for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+    accept = mod2(d) <= fc.cut2;
   }
   if (!accept) return;
-  if (a.abs_of_slot[sp] == absr) {
+  if (a.abs_of_slot[sp] == a.abs_of_slot[sr]) {
     // a self pair: counted in the list size, skipped by the CV loop
     // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
     unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
@@ -443,12 +438,9 @@ __device__ __forceinline__ void nl_candidate(const KArgs &a, const FrameConst &f
 // x-adjacency of cells cx and cxp in a row of nc cells: the required-cell
 // rule of LinkCells::addRequiredCells for one dimension.
 __device__ __forceinline__ bool x_adjacent(int cx, int cxp, int nc, int wrap) {
-  if (wrap) {
-    if (nc < 3) return true;
-    const int d = (cxp - cx + nc) % nc;
-    return d == 0 || d == 1 || d == nc - 1;
-  }
-  return abs(cxp - cx) <= 1;
+  const int d = abs(cxp - cx);
+  if (wrap) return nc < 3 || d <= 1 || d == nc - 1;
+  return d <= 1;
 }
 
 // One warp per slice of 32 ranks.  Fast path: when the slice's rows lie in one
@@ -479,17 +471,20 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
     const bool ra = sr < a.nA;
     const int cr = active ? a.cell_of_rank[fo + r] : 0;
     const int cx = cr % g.nc[0], cy = (cr / g.nc[0]) % g.nc[1], cz = cr / (g.nc[0] * g.nc[1]);
-    const double4 xr4 = active ? a.x64[fo + r] : make_double4(0, 0, 0, 0);
     const uint4 qr = active ? a.q[fo + r] : make_uint4(0, 0, 0, 0);
-    const long long absr = active ? a.abs_of_slot[sr] : 0;
     const int cwrap = (a.nl_kind == 2) ? a.do_pbc : g.wrap;
+    const bool cells_kind = a.nl_kind == 2;
     const size_t slice_base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
     // the x-row of the slice's first and last active rows
     const int last = min(31, a.ns - 1 - slice * 32);
     const int cfirst = __shfl_sync(0xffffffffu, cr, 0), clast = __shfl_sync(0xffffffffu, cr, last);
     const int rowfirst = cfirst / g.nc[0], rowlast = clast / g.nc[0];
     if (rowfirst == rowlast) {
+      // every loop bound below is warp-uniform (taken from the slice's row,
+      // not the lane's cell), so lanes past the end of a partial last slice
+      // stage the same segments and meet every __syncwarp
       const int cxa = cfirst % g.nc[0], cxb = clast % g.nc[0];
+      const int ry = rowfirst % g.nc[1], rz = rowfirst / g.nc[1];
       // x intervals (at most two) covering every lane's x neighbours once
       int xi0[2], xi1[2], nint;
       if (cxb - cxa + 3 >= g.nc[0]) {
@@ -521,8 +516,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
         nint = 1;
       }
       int y0, y1, z0, z1;
-      cell_range(cy, g.nc[1], cwrap, y0, y1);
-      cell_range(cz, g.nc[2], cwrap, z0, z1);
+      cell_range(ry, g.nc[1], cwrap, y0, y1);
+      cell_range(rz, g.nc[2], cwrap, z0, z1);
       for (int ny = y0; ny < y1; ++ny)
         for (int nz = z0; nz < z1; ++nz) {
           const int rowcell = wrap_cell(ny, g.nc[1]) * g.nc[0] + wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
@@ -534,14 +529,16 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
                 const int p = base + lane;
                 sq[warp][lane] = a.q[fo + p];
                 sslot[warp][lane] = slot_of_rank[p];
-                scx[warp][lane] = a.cell_of_rank[fo + p] % g.nc[0];
+                if (cells_kind) scx[warp][lane] = a.cell_of_rank[fo + p] % g.nc[0];
               }
               __syncwarp();
               if (active)
                 for (int j = 0; j < m; j++) {
-                  if (!x_adjacent(cx, scx[warp][j], g.nc[0], cwrap)) continue;
-                  nl_candidate(a, fc, f, fo, r, sr, ra, qr, xr4, absr, base + j, sslot[warp][j], sq[warp][j],
-                               slice_base, n);
+                  // classic lists need no adjacency test: cells are at least
+                  // NL_CUTOFF*(1+1e-9) wide, so a pair two cells apart fails the
+                  // distance test anyway
+                  if (cells_kind && !x_adjacent(cx, scx[warp][j], g.nc[0], cwrap)) continue;
+                  nl_candidate(a, fc, f, fo, r, sr, ra, qr, base + j, sslot[warp][j], sq[warp][j], slice_base, n);
                 }
               __syncwarp();
             }
@@ -559,7 +556,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
                           wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
             const int pe = start[c + 1];
             for (int p = start[c]; p < pe; p++)
-              nl_candidate(a, fc, f, fo, r, sr, ra, qr, xr4, absr, p, slot_of_rank[p], a.q[fo + p], slice_base, n);
+              nl_candidate(a, fc, f, fo, r, sr, ra, qr, p, slot_of_rank[p], a.q[fo + p], slice_base, n);
           }
     }
     if (active) a.row_len[fo + r] = min(n, a.cap);
@@ -633,6 +630,15 @@ __global__ void k_finalize32(KArgs a, int rank_order) {
     o[2] = g * (double)v.z;
   }
   a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// backward from a saved forward: grad = g * saved ds/dx (slot order)
+__global__ void k_scale_saved(KArgs a, const double *saved, double *grad) {
+  const int f = blockIdx.y;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = (size_t)a.ns * 3;
+  if (i >= n) return;
+  grad[(size_t)f * n + i] = a.g[f] * saved[(size_t)f * n + i];
 }
 
 // ---------------------------------------------------------------------------

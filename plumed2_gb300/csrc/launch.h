@@ -18,12 +18,13 @@ void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStre
 void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int mode, int tile, int nblocks, cudaStream_t s);
 void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_flags, cudaStream_t s);
 void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s);
+void launch_scale_saved(const KArgs &a, const double *saved, double *grad, cudaStream_t s);
 void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, double *grad_box, double *grad_param,
                       cudaStream_t s);
 
 // k_mixed.cu
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
-                      cudaStream_t s);
+                      int unroll, cudaStream_t s);
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s);
 void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,

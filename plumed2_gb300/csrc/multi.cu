@@ -234,7 +234,11 @@ template <typename T> struct Buf {
   size_t n = 0;
   cudaError_t ensure(size_t want) {
     if (want <= n && p) return cudaSuccess;
-    if (p) cudaFree(p);
+    // kernels queued on any stream may still use the old buffer
+    if (p) {
+      cudaDeviceSynchronize();
+      cudaFree(p);
+    }
     p = nullptr;
     n = 0;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
@@ -342,9 +346,13 @@ int build_group_tables(coord_multi *m, Group &g, int tile, int n_frames) {
       (e = g.out_of_slot.ensure(outs.size())) || (e = g.acc.ensure((size_t)n_frames * atoms.size())) ||
       (e = g.partials.ensure((size_t)n_frames * std::max(items, 1) * kPartials)))
     return m->fail(COORD_ERR_CUDA, std::string("batch allocation: ") + cudaGetErrorString(e));
+  // pageable copies on the legacy stream: wait for them before any kernel of
+  // the batch's non-blocking stream reads the tables
   cudaMemcpy(g.desc.p, d.data(), sizeof(ActionDesc) * d.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(g.atom_of_slot.p, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(g.out_of_slot.p, outs.data(), sizeof(long long) * outs.size(), cudaMemcpyHostToDevice);
+  if ((e = cudaDeviceSynchronize()))
+    return m->fail(COORD_ERR_CUDA, std::string("batch tables: ") + cudaGetErrorString(e));
   g.tile_built = tile;
   return COORD_OK;
 }
@@ -622,14 +630,19 @@ int coord_multi_forward_device(coord_multi *m, int n_frames, const double *pos, 
       issue_fused(m, n_frames, pos, s, deriv, virial, st);
     }
   }
-  // the other actions through their own contexts
+  // the other actions through their own contexts; staging sized once for the
+  // largest of them, before anything is queued
+  if (!m->others.empty()) {
+    size_t ns_max = 1;
+    for (int k : m->others) ns_max = std::max(ns_max, (size_t)m->views[k].ns);
+    if ((e = m->tmp_pos.ensure((size_t)n_frames * ns_max * 3)) || (e = m->tmp_s.ensure(n_frames)) ||
+        (e = m->tmp_d.ensure((size_t)n_frames * ns_max * 3)) || (e = m->tmp_v.ensure((size_t)n_frames * 9)) ||
+        (e = m->tmp_atoms.ensure(ns_max)))
+      return m->fail(COORD_ERR_CUDA, std::string("batch allocation: ") + cudaGetErrorString(e));
+  }
   for (int k : m->others) {
     const MultiView &v = m->views[k];
     const size_t ns = (size_t)v.ns;
-    if ((e = m->tmp_pos.ensure((size_t)n_frames * ns * 3)) || (e = m->tmp_s.ensure(n_frames)) ||
-        (e = m->tmp_d.ensure((size_t)n_frames * ns * 3)) || (e = m->tmp_v.ensure((size_t)n_frames * 9)) ||
-        (e = m->tmp_atoms.ensure(std::max<size_t>(ns, 1))))
-      return m->fail(COORD_ERR_CUDA, "batch allocation");
     if (ns) {
       cudaMemcpyAsync(m->tmp_atoms.p, v.abs, sizeof(int64_t) * ns, cudaMemcpyHostToDevice, st);
       k_multi_gather<<<dim3((unsigned)((ns + 255) / 256), n_frames), 256, 0, st>>>(pos, (int)m->n_atoms, n_frames,

@@ -160,3 +160,54 @@ def test_forward_dr0_flag_matches_backward():
     torch.cuda.synchronize()
     assert torch.allclose(gp, der, rtol=1e-12, atol=1e-14)
     assert torch.allclose(gq, dp, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_saved_forward_matches_recompute(prec):
+    """COORD_FLAG_SAVE keeps ds/dx and the virial of the forward (and
+    ds/d(R_0, D_0) with COORD_FLAG_DR0); the next backward scales them instead
+    of re-running the pairs.  Every route gives the same gradients (1e-12
+    relative on FP64, 1e-6 mixed: only the order of the atomic additions
+    differs) and a SAVE forward still hands back its own derivatives."""
+    from plumed2_gb300 import _lib
+    dev = torch.device("cuda:0")
+    n, L, F = 1000, 10 * 0.31, 2
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=10" % n
+    frames = np.stack([jittered_lattice(n, 0.31, 0.03, 60 + f) for f in range(F)])
+    boxes = np.stack([np.diag([L] * 3)] * F)
+    pos = torch.tensor(frames, dtype=torch.float64, device=dev)
+    g = torch.tensor([0.7, -1.3], dtype=torch.float64, device=dev)
+    routes = {"recompute": (0, True), "save": (_lib.FLAG_SAVE, False), "save+dr0": (_lib.FLAG_SAVE | _lib.FLAG_DR0, True),
+              "save, params recomputed": (_lib.FLAG_SAVE, True)}
+    res = {}
+    for name, (flags, want_param) in routes.items():
+        act = make(line, prec)
+        s = torch.zeros(F, dtype=torch.float64, device=dev)
+        der = torch.zeros(F, n, 3, dtype=torch.float64, device=dev)
+        vir = torch.zeros(F, 9, dtype=torch.float64, device=dev)
+        dp = torch.zeros(F, 2, dtype=torch.float64, device=dev)
+        act.forward_device(pos.data_ptr(), boxes, F, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=0,
+                           flags=flags, dparam_ptr=dp.data_ptr() if flags & _lib.FLAG_DR0 else 0)
+        gp = torch.zeros(F, n, 3, dtype=torch.float64, device=dev)
+        gb = torch.zeros(F, 9, dtype=torch.float64, device=dev)
+        gq = torch.zeros(F, 2, dtype=torch.float64, device=dev)
+        act.backward_device(pos.data_ptr(), boxes, F, g.data_ptr(), gp.data_ptr(), gb.data_ptr(),
+                            gq.data_ptr() if want_param else 0)
+        torch.cuda.synchronize()
+        res[name] = [t.cpu().numpy() for t in (s, der, vir, gp, gb, gq)]
+        if flags & _lib.FLAG_DR0:
+            assert np.abs(dp.cpu().numpy() * g.cpu().numpy()[:, None] - res[name][5]).max() <= \
+                1e-14 * np.abs(res[name][5]).max()
+        act.close()
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    ref = res["recompute"]
+    for name, got in res.items():
+        for k, (a, b) in enumerate(zip(ref, got)):
+            if k == 5 and not routes[name][1]:
+                assert np.all(b == 0.0)  # no grad_param requested
+                continue
+            assert np.abs(a - b).max() <= tol * max(np.abs(a).max(), 1e-300), (name, k)
+        # the saved gradient is g times the forward's own derivatives
+        if name in ("save", "save+dr0"):
+            s_, der, vir, gp = got[:4]
+            assert np.abs(gp - g.cpu().numpy()[:, None, None] * der).max() <= 1e-14 * np.abs(gp).max()

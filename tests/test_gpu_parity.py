@@ -213,6 +213,32 @@ def test_rt20_switch_goldens(golden):
                 assert np.all(np.abs(got - rows[:, 1 + col]) <= 5.01e-5), (name, lab, fi)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["NLIST", "NLISTCELLS"])
+@pytest.mark.parametrize("groups", ["GROUPA=8853-8937", "GROUPA=8001-8333 GROUPB=8500-8700", "GROUPA=1-1000"])
+def test_nlist_ragged_slices(orc, prec, kind, groups):
+    """Group sizes that are not a multiple of 32 (a partial last slice of the
+    neighbour list), taken as clustered sub-ranges of a larger lattice."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.436 NN=6 MM=12 D_MAX=1.0"
+    n, L = 12167, 23 * 0.31
+    box = np.diag([L] * 3)
+    full = jittered_lattice(n, 0.31, 0.03, 200)
+    c = Coordination("%s SWITCH={%s} %s NL_CUTOFF=1.2 NL_STRIDE=5" % (groups, spec, kind), precision=prec)
+    pos = full[c.requested_atoms]
+    nA = c.nslots if "GROUPB" not in groups else 333
+    m, n0, n1 = (0, c.nslots, 0) if "GROUPB" not in groups else (1, nA, c.nslots - nA)
+    got = c.calculate(pos, box, 0)
+    if kind == "NLIST":
+        ref_pairs = orc.nl_classic_cells(m, n0, n1, pos, box, True, 1.2)
+    else:
+        ref_pairs = orc.nl_linkcells(m, n0, n1, pos, box, True, 1.2)
+    assert np.array_equal(_sorted(c.pairs()), _sorted(ref_pairs))
+    ref = orc.coordination(spec, pos, box, ref_pairs)
+    _check(prec, got, ref, groups)
+    c.close()
+
+
 def test_empty_and_tiny_groups(orc):
     from plumed2_gb300.action import Coordination
     box = np.diag([3.0] * 3)
