@@ -121,6 +121,23 @@ class Clocks:
         return out
 
 
+def rank_walkers(rank, walkers_per_rank):
+    """Walker seeds a rank owns: disjoint blocks, so N ranks run N x the walkers with no exchange
+    (weak scaling)."""
+    return list(range(rank * walkers_per_rank, (rank + 1) * walkers_per_rank))
+
+
+def reduce_over_ranks(x, op="max", device=None):
+    """x reduced over the ranks of the default process group (identity without one)."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return t.item()
+
+
 def make_walkers(n_walkers, n_atoms, first):
     from plumed2_gb300.frames import sc_sites
     sites = sc_sites(n_atoms)
@@ -225,7 +242,7 @@ def run_ours(args):
 
     W = args.walkers
     n = args.atoms if not args.quick else 32768
-    frames, box = make_walkers(W, n, rank * W)
+    frames, box = make_walkers(W, n, rank_walkers(rank, W)[0])
     boxes = np.stack([box] * W)
     line = LINE % (n, SPEC)
     c = Coordination(line, precision="mixed", device=local)
@@ -275,46 +292,53 @@ def run_ours(args):
     torch.cuda.synchronize()
     l0 = _lib.launch_count()
     clocks.start()
-    t0 = time.perf_counter()
+    # device time: CUDA events on the default stream, which the library's calls
+    # with a NULL stream are fenced against on both sides
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
     for _ in range(args.steps):
         one_step(c)
+    ev1.record()
     torch.cuda.synchronize()
-    t = time.perf_counter() - t0
+    t = ev0.elapsed_time(ev1) * 1e-3
     clk = clocks.stop()
     launches = _lib.launch_count() - l0
+    ktimes = c.kernel_times()
     kern_ms, kern_n = c.kernel_ms()
     c.set_timing(False)
-    if ws > 1:
-        tt = torch.tensor([t], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = tt.item()
+    t = reduce_over_ranks(t, "max", dev)
+    pairs_job = reduce_over_ranks(pairs_per_step, "sum", dev)
     ms_step = t / args.steps * 1e3
-    value = pairs_per_step * ws * args.steps / t
+    value = pairs_job * args.steps / t
 
     # cost of one neighbour-list rebuild against a plain CV+force pass (same inputs), and the
     # CV+force pass alone (s, ds/dx, virial: CoordinationBase::calculate) averaged over 5 calls
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    ev0.record()
     c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step,
                      flags=_lib.FLAG_REBUILD)
+    ev1.record()
     torch.cuda.synchronize()
-    t_rebuild_step = time.perf_counter() - t0
-    t0 = time.perf_counter()
+    t_rebuild_step = ev0.elapsed_time(ev1) * 1e-3
+    base = (step // 10 + 1) * 10 + 1  # five steps between rebuilds (NL_STRIDE=10)
+    ev0.record()
     for k in range(5):
-        c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step + 1 + k)
+        c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=base + k)
+    ev1.record()
     torch.cuda.synchronize()
-    t_plain_step = (time.perf_counter() - t0) / 5
+    t_plain_step = ev0.elapsed_time(ev1) * 1e-3 / 5
 
     # the plain FP64 GPU path on the same workload (the drop-in, for the 5x target)
     c64 = Coordination(line, precision="fp64", device=local)
     st64 = 0
     c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=0)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    ev0.record()
     for k in range(1, 1 + args.fp64_steps):
         c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=k)
+    ev1.record()
     torch.cuda.synchronize()
-    t64 = (time.perf_counter() - t0) / max(args.fp64_steps, 1)
+    t64 = ev0.elapsed_time(ev1) * 1e-3 / max(args.fp64_steps, 1)
     c64.close()
     del st64
 
@@ -342,23 +366,31 @@ def run_ours(args):
             roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                     "frac": frac_fp32, "traffic": None,
                     "peak_source": "coord_measure_peaks FP32 FMA microbenchmark (measured live)"}
+        kt = sorted(ktimes) or [0.0]
         roof.update({"kernel": "k_eval_nl32 (mixed NL pair kernel)", "kernel_ms": kern_ms, "launches": kern_n,
+                     "kernel_ms_min_median_max": [kt[0], kt[len(kt) // 2], kt[-1]],
                      "fp64_peak_tflops": peaks["fp64_tflops"], "hbm_microbench_gbs": peaks["hbm_gbs"],
                      "alg_flops_per_launch": flops, "alg_bytes_per_launch": bytes_alg,
                      "other_roof_frac": frac_hbm if roof["bound"] == "fp32" else frac_fp32})
 
         # e2e through the plugin-facing host call, one context per walker
         e2e_v, h2d, d2h = None, 0, 0
+        pageable, tables = _lib.host_memory_access(local)
+        host_path = ("direct: kernels read the positions from and write s, virial and forces into the caller's "
+                     "pageable host arrays through the host page tables" if pageable and tables and
+                     os.environ.get("COORD_HOST_STAGED") != "1" else "staged through pinned host buffers")
         if args.e2e_steps > 0:
             ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
             host_pos = [np.ascontiguousarray(frames[w]) for w in range(W)]
+            # per walker force and virial arrays reused from step to step, as an MD engine does
+            outs = [(np.zeros((n, 3)), np.zeros(9)) for _ in range(W)]
             for w in range(W):
-                ctxs[w].calculate(host_pos[w], box, 0)
+                ctxs[w].calculate(host_pos[w], box, 0, out=outs[w])
             t0 = time.perf_counter()
             npairs = 0
             for k in range(1, 1 + args.e2e_steps):
                 for w in range(W):
-                    sv, dv, vv = ctxs[w].calculate(host_pos[w], box, k)
+                    sv, dv, vv = ctxs[w].calculate(host_pos[w], box, k, out=outs[w])
             te = time.perf_counter() - t0
             npairs = sum(ctxs[w].nl_size() for w in range(W)) * args.e2e_steps
             e2e_v = npairs / te
@@ -387,7 +419,9 @@ def run_ours(args):
                        "backward": True, "l2": "working set (0.8 GB) larger than the 129 MB L2",
                        "parallelism": "walkers sharded across GPUs, no collective"},
             "roofline": roof, "cpu_baseline": cpu,
-            "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "call": "coord_forward (host arrays) per walker and step, %d steps" % args.e2e_steps,
+                    "host_path": host_path},
             "gpu_launches": launches, "clocks": clk,
         }
         print(json.dumps(line_out), flush=True)

@@ -202,6 +202,16 @@ int coord_forward_noalloc(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, c
 int coord_autotune(coord_ctx *ctx, char *desc, size_t desclen);
 /* Microbenchmarks of the device (FP32 FMA, FP64 FMA TFLOP/s, HBM copy GB/s). */
 int coord_measure_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *hbm_gbs);
+/* Whether the device reads and writes pageable host memory coherently
+ * (cudaDevAttrPageableMemoryAccess) and does so through the host's page
+ * tables without migrating pages (cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+ * e.g. a Grace CPU with NVLink-C2C).  When both hold, coord_forward moves
+ * positions and results with kernels that access the caller's arrays
+ * directly instead of staging them through pinned buffers (unless the
+ * environment sets COORD_HOST_STAGED=1 when the context first runs).  No
+ * reference counterpart. */
+int coord_host_memory_access(int device, int *pageable, int *host_page_tables);
+
 /* Kernel launches issued by this library since load (for launch accounting). */
 int64_t coord_launch_count(void);
 /* Average device time (ms) of the pair-evaluation kernel over the launches
@@ -211,6 +221,11 @@ int64_t coord_launch_count(void);
 int coord_last_kernel_ms(coord_ctx *ctx, double *ms, int *count);
 /* Turn per-launch event timing of the pair kernel on/off (default off). */
 int coord_set_timing(coord_ctx *ctx, int enable);
+/* The individual device times (ms) behind coord_last_kernel_ms, in launch
+ * order: writes min(count, cap) values and returns count in *count.  Waits for
+ * the events; does not reset the record (coord_last_kernel_ms does).
+ * Diagnostic; no reference counterpart. */
+int coord_kernel_times(coord_ctx *ctx, float *ms, int cap, int *count);
 
 #ifdef __cplusplus
 }

@@ -94,6 +94,8 @@ def load() -> C.CDLL:
         L.coord_launch_count.restype = C.c_int64
         L.coord_last_kernel_ms.argtypes = [_vp, _dp, C.POINTER(C.c_int)]
         L.coord_set_timing.argtypes = [_vp, C.c_int]
+        L.coord_kernel_times.argtypes = [_vp, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
+        L.coord_host_memory_access.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.coord_forward_noalloc.argtypes = [_vp, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_int64), C.c_int64,
                                             _vp, _dp, _vp, _vp, _vp, _vp]
         _lib = L
@@ -121,3 +123,10 @@ def measure_peaks(device: int = 0):
 
 def launch_count() -> int:
     return int(load().coord_launch_count())
+
+
+def host_memory_access(device: int = 0):
+    """(pageable, via host page tables): whether kernels can access the caller's host arrays directly."""
+    a, b = C.c_int(), C.c_int()
+    load().coord_host_memory_access(device, C.byref(a), C.byref(b))
+    return bool(a.value), bool(b.value)

@@ -166,16 +166,24 @@ class Coordination:
         return list(self.group_a) + list(self.group_b)
 
     # -- per step ----------------------------------------------------------
-    def calculate(self, positions, box, step: int = 0, rebuild: bool = False,
-                  derivatives: bool = True) -> Tuple[float, Optional[np.ndarray], Optional[np.ndarray]]:
+    def calculate(self, positions, box, step: int = 0, rebuild: bool = False, derivatives: bool = True,
+                  out=None) -> Tuple[float, Optional[np.ndarray], Optional[np.ndarray]]:
+        """One step through the host-buffer call (coord_forward).  out=(deriv (nslots, 3), virial (9,)) reuses
+        the caller's float64 C-contiguous arrays, as an MD engine reuses its force arrays from step to step."""
         self._ensure_groups()
         pos = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).reshape(-1, 3))
         if len(pos) != self.nslots:
             raise ValueError("expected %d positions, got %d" % (self.nslots, len(pos)))
         bx = np.ascontiguousarray(np.asarray(box, dtype=np.float64).reshape(9))
         s = C.c_double()
-        deriv = np.zeros((self.nslots, 3)) if derivatives else None
-        vir = np.zeros(9) if derivatives else None
+        if out is not None and derivatives:
+            deriv, vir = out
+            if (deriv.dtype != np.float64 or not deriv.flags.c_contiguous or deriv.size != 3 * self.nslots or
+                    vir.dtype != np.float64 or not vir.flags.c_contiguous or vir.size != 9):
+                raise ValueError("out needs float64 C-contiguous arrays of %d and 9 values" % (3 * self.nslots))
+        else:
+            deriv = np.zeros((self.nslots, 3)) if derivatives else None
+            vir = np.zeros(9) if derivatives else None
         flags = (_lib.FLAG_REBUILD if rebuild else 0) | (0 if derivatives else _lib.FLAG_NO_DERIV)
         rc = self._L.coord_forward(self._ctx, dptr(pos), dptr(bx), int(step), flags, C.byref(s),
                                    dptr(deriv) if derivatives else None, dptr(vir) if derivatives else None)
@@ -241,6 +249,14 @@ class Coordination:
     # -- tuning / timing -----------------------------------------------------
     def set_timing(self, enable: bool = True):
         check(self._L, self._ctx, self._L.coord_set_timing(self._ctx, int(enable)))
+
+    def kernel_times(self):
+        """Per-launch device times (ms) of the pair kernel since timing was enabled/last read."""
+        n = C.c_int()
+        check(self._L, self._ctx, self._L.coord_kernel_times(self._ctx, None, 0, C.byref(n)))
+        out = (C.c_float * max(n.value, 1))()
+        check(self._L, self._ctx, self._L.coord_kernel_times(self._ctx, out, n.value, C.byref(n)))
+        return list(out)[:n.value]
 
     def kernel_ms(self):
         """(average ms, launches) of the pair kernel since timing was enabled/last read."""

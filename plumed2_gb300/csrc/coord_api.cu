@@ -7,6 +7,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -72,6 +73,8 @@ struct coord_ctx {
   int mode = MODE_SINGLE;
   int64_t nA = 0, nB = 0, ns = 0;
   std::vector<int64_t> abs_host;  // GROUPA then GROUPB absolute indices
+  bool has_dup = false;           // an absolute index in two slots
+  int host_direct = -1;           // kernels access pageable host arrays in place (-1: not probed)
   bool groups_set = false;
   std::string err;
   cudaStream_t stream = nullptr;
@@ -106,6 +109,9 @@ struct coord_ctx {
   std::vector<double> boxes_seen;
   // tuning
   int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0, nl_unroll = 4;
+  // mixed NL pass, tuned per evaluation mode (EVAL_S / EVAL_DERIV / EVAL_PARAM)
+  int nlm_blocks[3] = {0, 0, 0}, nlm_unroll[3] = {4, 4, 4};
+  bool nlm_tuned[3] = {false, false, false};
   int cells_launch = 0;  // cells per frame known on the host (0: use ncell_cap)
   bool tuned = false;
   // timing: one event pair per pair-kernel launch while enabled
@@ -259,6 +265,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.self_cap = c->self_cap;
   a.nslices = (int)((c->ns + 31) / 32);
   a.flags = (int)flags;
+  a.has_dup = c->has_dup ? 1 : 0;
   a.fc = c->fc.p;
   a.abs_of_slot = c->abs_of_slot.p;
   a.pos = d_pos;
@@ -359,6 +366,13 @@ int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bo
 void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
   const bool nl = c->p.nlist != COORD_NL_NONE;
   const bool mixed = c->p.precision == COORD_PREC_MIXED;
+  // positions for the pair kernel: fixed-point (mixed) or FP64 in rank order
+  if (c->mode == MODE_PAIR || !nl) {
+    if (mixed) launch_gather(a, 0, 0, 1, c->stream);
+  } else {
+    launch_gather(a, 1, mixed ? 0 : 1, mixed ? 1 : 0, c->stream);
+  }
+  // the pair kernel alone, between the timing events
   cudaEvent_t tev1 = nullptr;
   if (c->timing) {
     if (c->ev_used == c->ev_pool.size()) {
@@ -372,25 +386,21 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
     c->ev_used++;
   }
   if (c->mode == MODE_PAIR) {
-    if (mixed) {
-      launch_gather(a, 0, 0, 1, c->stream);
+    if (mixed)
       launch_pairs32(a, c->sw, c->s32, mode, nl ? 1 : 0, c->stream);
-    } else {
+    else
       launch_pairs64(a, c->sw, mode, nl ? 1 : 0, c->stream);
-    }
   } else if (!nl) {
-    if (mixed) {
-      launch_gather(a, 0, 0, 1, c->stream);
+    if (mixed)
       launch_allpairs32(a, c->sw, c->s32, mode, c->tile32, c->ap_blocks, c->stream);
-    } else {
+    else
       launch_allpairs64(a, c->sw, mode, c->tile64, c->ap_blocks, c->stream);
-    }
   } else {
     if (mixed) {
-      launch_gather(a, 1, 0, 1, c->stream);
-      launch_eval_nl32(a, c->sw, c->s32, mode, c->nl_blocks, c->nl_unroll, c->stream);
+      const int m = std::min(std::max(mode, 0), 2);
+      const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
+      launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
     } else {
-      launch_gather(a, 1, 1, 0, c->stream);
       launch_eval_nl64(a, c->sw, mode, c->stream);
     }
   }
@@ -413,15 +423,16 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   const int bps[4] = {2, 4, 6, 8}, unr[3] = {2, 4, 8};
+  const int m = std::min(std::max(mode, 0), 2);
   float best = 1e30f;
   int bb = c->nl_blocks, bu = c->nl_unroll;
   const bool timing = c->timing;
   c->timing = false;
   for (int b : bps)
     for (int u : unr) {
-      c->nl_blocks = b * std::max(c->nsm, 1);
-      c->nl_unroll = u;
-      c->max_blocks = std::max(c->max_blocks, c->nl_blocks);
+      c->nlm_blocks[m] = b * std::max(c->nsm, 1);
+      c->nlm_unroll[m] = u;
+      c->max_blocks = std::max(c->max_blocks, c->nlm_blocks[m]);
       if (ensure_buffers(c, a.nframes)) continue;
       KArgs aa = a;
       aa.partials = c->partials.p;
@@ -434,10 +445,13 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
       cudaEventElapsedTime(&ms, t0, t1);
       if (ms < best) {
         best = ms;
-        bb = c->nl_blocks;
+        bb = c->nlm_blocks[m];
         bu = u;
       }
     }
+  c->nlm_blocks[m] = bb;
+  c->nlm_unroll[m] = bu;
+  c->nlm_tuned[m] = true;
   c->nl_blocks = bb;
   c->nl_unroll = bu;
   c->timing = timing;
@@ -531,10 +545,12 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
       cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
       launch_pair_flags(a, c->stream);
     } else {
+      bool classic = c->p.nlist == COORD_NL_CLASSIC;
+      for (const FrameConst &fq : c->fc_uploaded) classic = classic && fq.fixed_ok;
       for (int attempt = 0; attempt < 8; attempt++) {
         if (attempt > 0)
           cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
-        launch_nl_build(a, c->stream);
+        launch_nl_build(a, classic, c->stream);
         if ((e = cudaMemcpyAsync(c->h_nl.p, c->nl_count.p, sizeof(unsigned long long) * 4 * n_frames,
                                  cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
           return c->cuda_fail(e, "neighbour-list count");
@@ -569,7 +585,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   const int mode = (flags & COORD_FLAG_NO_DERIV) ? EVAL_S : ((flags & COORD_FLAG_DR0) ? EVAL_PARAM : EVAL_DERIV);
   if (mode == EVAL_PARAM && !c->sw.grad_ok)
     return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
-  if (!c->tuned && mixed && nl && c->mode != MODE_PAIR) {
+  if (!c->nlm_tuned[std::min(std::max(mode, 0), 2)] && mixed && nl && c->mode != MODE_PAIR) {
     autotune_nl(c, a, mode);
     a.partials = c->partials.p;
     a.max_blocks = c->max_blocks;
@@ -578,12 +594,12 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   if (save) {
     // hand the caller its copies of what was kept
     const size_t nd = (size_t)n_frames * c->ns * 3;
-    if (deriv && nd) cudaMemcpyAsync(deriv, c->sv_deriv.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-    if (virial) cudaMemcpyAsync(virial, c->sv_vir.p, (size_t)n_frames * 9 * sizeof(double), cudaMemcpyDeviceToDevice,
+    if (deriv && nd) cudaMemcpyAsync(deriv, c->sv_deriv.p, nd * sizeof(double), cudaMemcpyDefault, c->stream);
+    if (virial) cudaMemcpyAsync(virial, c->sv_vir.p, (size_t)n_frames * 9 * sizeof(double), cudaMemcpyDefault,
                                 c->stream);
     c->saved_param = (flags & COORD_FLAG_DR0) != 0;
     if (dparam && c->saved_param)
-      cudaMemcpyAsync(dparam, c->sv_par.p, (size_t)n_frames * 2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+      cudaMemcpyAsync(dparam, c->sv_par.p, (size_t)n_frames * 2 * sizeof(double), cudaMemcpyDefault, c->stream);
     c->saved_valid = true;
     c->saved_frames = n_frames;
   }
@@ -793,6 +809,11 @@ int coord_set_groups(coord_ctx *c, const int64_t *a, int64_t na, const int64_t *
   for (int64_t i = 0; i < na; i++) abs[i] = a[i];
   for (int64_t i = 0; i < nb; i++) abs[na + i] = b[i];
   c->abs_host.assign(abs.begin(), abs.begin() + c->ns);
+  {
+    std::vector<int64_t> sorted(c->abs_host);
+    std::sort(sorted.begin(), sorted.end());
+    c->has_dup = std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end();
+  }
   if (int rc = device_init(c)) return rc;
   cudaError_t e = c->abs_of_slot.ensure(abs.size());
   if (e != cudaSuccess) return c->cuda_fail(e, "allocation");
@@ -864,7 +885,32 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   if (!(flags & COORD_FLAG_NO_DERIV) && !deriv && c->ns > 0) return c->fail(COORD_ERR_ARG, "null deriv");
   cudaSetDevice(c->p.device);
   const size_t n3 = (size_t)c->ns * 3;
+  const bool want_d = !(flags & COORD_FLAG_NO_DERIV);
   cudaError_t e;
+  if (c->ns == 0) {
+    *s = 0.0;
+    if (want_d && virial) std::memset(virial, 0, 9 * sizeof(double));
+    return COORD_OK;
+  }
+  if (c->host_direct < 0) {
+    int pageable = 0, tables = 0;
+    coord_host_memory_access(c->p.device, &pageable, &tables);
+    const char *staged = std::getenv("COORD_HOST_STAGED");  // "1": always stage through pinned buffers
+    c->host_direct = (pageable && tables && !(staged && staged[0] == '1')) ? 1 : 0;
+  }
+  if (c->host_direct && !(flags & COORD_FLAG_SAVE)) {
+    // The device reads and writes the caller's pageable arrays through the
+    // host page tables (cache-coherent CPU-GPU link): one kernel pulls the
+    // positions in, the pair pass writes s, the virial and the derivatives
+    // straight into the caller's arrays.
+    if ((e = c->d_pos.ensure(n3))) return c->cuda_fail(e, "staging allocation");
+    launch_copy_in(pos, c->d_pos.p, n3, c->stream);
+    int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, s, want_d ? deriv : nullptr,
+                          want_d ? virial : nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    if ((e = cudaStreamSynchronize(c->stream))) return c->cuda_fail(e, "forward");
+    return COORD_OK;
+  }
   if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3)) || (e = c->d_s.ensure(1)) ||
       (e = c->d_virial.ensure(9)) || (e = c->h_pos.ensure(n3)) || (e = c->h_out.ensure(n3 + 10)))
     return c->cuda_fail(e, "staging allocation");
@@ -876,7 +922,6 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, c->d_s.p, c->d_deriv.p, c->d_virial.p, nullptr, nullptr);
   if (rc) return rc;
   cudaMemcpyAsync(c->h_out.p, c->d_s.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-  const bool want_d = !(flags & COORD_FLAG_NO_DERIV);
   if (want_d) {
     cudaMemcpyAsync(c->h_out.p + 1, c->d_virial.p, 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (n3) cudaMemcpyAsync(c->h_out.p + 10, c->d_deriv.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
@@ -1017,8 +1062,11 @@ int coord_get_pairs(coord_ctx *c, int frame, uint32_t *pairs, int64_t cap, int64
 int coord_autotune(coord_ctx *c, char *desc, size_t desclen) {
   if (!c) return COORD_ERR_ARG;
   if (desc && desclen)
-    std::snprintf(desc, desclen, "tuned=%d nl_blocks=%d nl_unroll=%d allpairs_tile64=%d allpairs_tile32=%d blocks=%d",
-                  (int)c->tuned, c->nl_blocks, c->nl_unroll, c->tile64, c->tile32, c->ap_blocks);
+    std::snprintf(desc, desclen,
+                  "tuned=%d nl_pass(s/deriv/param)=%d/%d/%d blocks, unroll %d/%d/%d allpairs_tile64=%d "
+                  "allpairs_tile32=%d blocks=%d",
+                  (int)c->tuned, c->nlm_blocks[0], c->nlm_blocks[1], c->nlm_blocks[2], c->nlm_unroll[0],
+                  c->nlm_unroll[1], c->nlm_unroll[2], c->tile64, c->tile32, c->ap_blocks);
   return COORD_OK;
 }
 
@@ -1041,6 +1089,27 @@ int coord_last_kernel_ms(coord_ctx *c, double *ms, int *count) {
   if (c->ev_used) *ms = tot / (double)c->ev_used;
   if (count) *count = (int)c->ev_used;
   c->ev_used = 0;
+  return COORD_OK;
+}
+
+int coord_host_memory_access(int device, int *pageable, int *host_page_tables) {
+  int a = 0, b = 0;
+  if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) a = 0;
+  if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) b = 0;
+  if (pageable) *pageable = a;
+  if (host_page_tables) *host_page_tables = b;
+  return COORD_OK;
+}
+
+int coord_kernel_times(coord_ctx *c, float *ms, int cap, int *count) {
+  if (!c || !count) return COORD_ERR_ARG;
+  *count = (int)c->ev_used;
+  for (size_t i = 0; i < c->ev_used && (int)i < cap; i++) {
+    float t = 0.f;
+    cudaEventSynchronize(c->ev_pool[i].second);
+    cudaEventElapsedTime(&t, c->ev_pool[i].first, c->ev_pool[i].second);
+    if (ms) ms[i] = t;
+  }
   return COORD_OK;
 }
 

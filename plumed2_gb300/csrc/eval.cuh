@@ -153,9 +153,11 @@ __device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z)
 // the per-thread accumulators carry across slices and one block reduction
 // closes the kernel.  Inside a slice the loop runs to the slice width (warp
 // uniform); entries and partner positions are loaded kUnroll at a time before
-// any is used, so kUnroll gathers are in flight per lane.
-// Entries are streamed once per step (ld.global.cs: evict first) so that the
-// fixed-point positions, gathered many times, stay resident in L2.
+// any is used, so kUnroll gathers are in flight per lane.  Entries are
+// streamed once per step (ld.global.cs: evict first) so that the fixed-point
+// positions, gathered many times, stay resident in L2.  (A grid that visits
+// the frames in order, for L2 locality, measured 2x slower: the per-frame
+// block barrier costs more than the locality gains.)
 template <int NH, int MODE, int kUnroll>
 __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y;

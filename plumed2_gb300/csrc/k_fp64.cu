@@ -18,15 +18,33 @@ void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int li
   g_launches += 2;
 }
 
-void launch_nl_build(const KArgs &a, cudaStream_t s) {
+void launch_nl_build(const KArgs &a, bool classic, cudaStream_t s) {
   cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)a.ncell_cap * a.nframes, s);
   k_bin<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
   k_scan_cells<<<a.nframes, 1024, 0, s>>>(a);
   k_scatter<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
   k_cell_sort<<<dim3(std::max(1, std::min(a.cells_launch, 65535)), a.nframes), 64, 0, s>>>(a);
   k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1, 1);
-  k_nl_search<<<dim3((a.nslices + kSearchWarps - 1) / kSearchWarps, a.nframes), kSearchWarps * 32, 0, s>>>(a);
+  const dim3 sgrid((a.nslices + kSearchWarps - 1) / kSearchWarps, a.nframes);
+  if (classic)
+    k_nl_search<<<sgrid, kSearchWarps * 32, 0, s>>>(a);
+  else
+    k_nl_search_cells<<<sgrid, kSearchWarps * 32, 0, s>>>(a);
   g_launches += 6;
+}
+
+namespace {
+__global__ void k_copy_in(const double *__restrict__ src, double *__restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+}  // namespace
+
+void launch_copy_in(const double *src, double *dst, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  const size_t blocks = std::min<size_t>((n + 255) / 256, 2048);
+  k_copy_in<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n);
+  g_launches += 1;
 }
 
 void launch_pair_flags(const KArgs &a, cudaStream_t s) {

@@ -45,7 +45,8 @@ static int nh_compiled(const SwitchParams &sw) {
 
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
                       int unroll, cudaStream_t s) {
-  // persistent: nblocks blocks over all frames, at least one per frame
+  // persistent: nblocks blocks over all frames, at least one per frame, at
+  // most one per 8 slices of a frame (8 warps per block)
   const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
   const dim3 g(per_frame, a.nframes);
   if (unroll >= 8) {

@@ -75,23 +75,37 @@ __device__ void block_partials_finish(const KArgs &a, int frame, double v[kParti
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  if (threadIdx.x < kPartials) {
-    const double *base = a.partials + (size_t)frame * a.max_blocks * kPartials;
-    double s = 0.0, c = 0.0;  // Kahan-Babuska (Neumaier) compensated sum
-    for (int b = 0; b < nblocks_frame; b++) {
-      const double x = __ldcg(base + (size_t)b * kPartials + threadIdx.x);
+  // Quantity k is summed by warp k % nwarps: each lane a Neumaier-compensated
+  // sum over records lane, lane+32, ...; the lanes' (sum, compensation) pairs
+  // then meet in a fixed shuffle tree with exact two-sums, so the result does
+  // not depend on timing and the loads of a quantity are spread over 32 lanes.
+  const double *base = a.partials + (size_t)frame * a.max_blocks * kPartials;
+  for (int k = warp; k < kPartials; k += nwarps) {
+    double s = 0.0, c = 0.0;
+    for (int b = lane; b < nblocks_frame; b += 32) {
+      const double x = __ldcg(base + (size_t)b * kPartials + k);
       const double t = s + x;
       c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
       s = t;
     }
-    s += c;
-    const int k = threadIdx.x;
-    if (k == 0) {
-      if (a.out_s) a.out_s[frame] = s;
-    } else if (k <= 9) {
-      if (a.out_virial) a.out_virial[(size_t)frame * 9 + (k - 1)] = s;
-    } else {
-      if (a.out_dparam) a.out_dparam[(size_t)frame * 2 + (k - 10)] = s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+      // the lower lane of each exchange orders the operands, so both lanes agree bit for bit
+      const double x = (lane & o) ? s2 : s, y = (lane & o) ? s : s2;
+      const double t = x + y, bv = t - x;
+      c = ((lane & o) ? c2 + c : c + c2) + ((x - (t - bv)) + (y - bv));
+      s = t;
+    }
+    if (lane == 0) {
+      const double v = s + c;
+      if (k == 0) {
+        if (a.out_s) a.out_s[frame] = v;
+      } else if (k <= 9) {
+        if (a.out_virial) a.out_virial[(size_t)frame * 9 + (k - 1)] = v;
+      } else {
+        if (a.out_dparam) a.out_dparam[(size_t)frame * 2 + (k - 10)] = v;
+      }
     }
   }
   if (threadIdx.x == 0) a.tickets[frame] = 0u;
@@ -421,7 +435,7 @@ __device__ __forceinline__ void nl_candidate(const KArgs &a, const FrameConst &f
     accept = mod2(d) <= fc.cut2;
   }
   if (!accept) return;
-  if (a.abs_of_slot[sp] == a.abs_of_slot[sr]) {
+  if (a.has_dup && a.abs_of_slot[sp] == a.abs_of_slot[sr]) {
     // a self pair: counted in the list size, skipped by the CV loop
     // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
     unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
@@ -443,15 +457,241 @@ __device__ __forceinline__ bool x_adjacent(int cx, int cxp, int nc, int wrap) {
   return d <= 1;
 }
 
-// One warp per slice of 32 ranks.  Fast path: when the slice's rows lie in one
-// x-row of cells, the candidates of all 32 rows are the ranks of at most 9
-// contiguous row segments (ranks are cell-major, x fastest); they are staged
-// through shared memory 32 at a time and every lane tests them (broadcast
-// reads, no divergence in the loop).  A slice spanning two x-rows takes the
-// per-lane path over its own required cells.
 constexpr int kSearchWarps = 4;
 
+// The reference's own cutoff test for ranks (first, second) in its orientation:
+// modulo2(pbc.distance(x[first], x[second])) <= cutoff^2
+// (NeighborList.cpp:190-200).  Out of line: taken only inside the band.
+__device__ __noinline__ bool nl_exact(const double4 *x64, const FrameConst *fc, int do_pbc, int first, int second) {
+  const double4 x1 = x64[first], x2 = x64[second];
+  const double v1[3] = {x1.x, x1.y, x1.z}, v2[3] = {x2.x, x2.y, x2.z};
+  double d[3];
+  if (do_pbc)
+    pbc_distance(fc->pbc, v1, v2, d);
+  else
+    for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+  return mod2(d) <= fc->cut2;
+}
+
+// A candidate that passed the FP32 prefilter (r2 <= cut2_hi) of a classic
+// list: group and orientation, the reference's own FP64 test when r2 lies in
+// the band around cutoff^2, self pairs, store.
+__device__ __forceinline__ void nl_accept(const KArgs &a, const FrameConst &fc, int f, size_t fo, int r, int sr,
+                                          bool ra, int p, int sp, float r2, size_t slice_base, int &n) {
+  bool r_first;
+  if (a.mode == MODE_TWO) {
+    if (ra == (sp < a.nA)) return;
+    r_first = ra;
+  } else {
+    r_first = sr < sp;
+  }
+  if (!(r2 < fc.cut2_lo) && !nl_exact(a.x64 + fo, &fc, a.do_pbc, r_first ? r : p, r_first ? p : r)) return;
+  if (a.has_dup && a.abs_of_slot[sp] == a.abs_of_slot[sr]) {
+    // a self pair: counted in the list size, skipped by the CV loop
+    // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
+    unsigned long long k = atomicAdd(&a.nl_count[f * 4 + 1], 1ull);
+    if (k < (unsigned long long)a.self_cap) {
+      a.self_pairs[((size_t)f * a.self_cap + k) * 2] = r_first ? sr : sp;
+      a.self_pairs[((size_t)f * a.self_cap + k) * 2 + 1] = r_first ? sp : sr;
+    }
+    return;
+  }
+  if (n < a.cap) a.ell[slice_base + (size_t)n * 32] = (uint32_t)p | (r_first ? kOrientBit : 0u);
+  n++;
+}
+
+// Classic lists with a fixed-point frame (orthorhombic box or no PBC).  The
+// slice's rows are processed one x-row of cells at a time; the candidates of a
+// row pass are the ranks of at most 9 row segments (ranks are cell-major, x
+// fastest), staged 32 at a time in shared memory and tested by every lane of
+// the row.  kRel: candidates are staged as FP32 coordinates relative to the
+// pass's first row (an exact integer difference of fixed-point positions, one
+// rounding), so a test is three subtractions and a squared norm; otherwise
+// each test takes the wrapped fixed-point difference itself.  Ownership (even
+// rank sum -> lower rank, odd -> higher) selects every other candidate of a
+// batch that lies wholly above or below the lane's rank.
+template <bool kRel>
+__device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc, int f, size_t fo, int r, int sr, bool ra,
+                                        uint4 qr, bool mine, int ry, int rz, int nint, int xa0, int xb0, int xa1,
+                                        int xb1, uint4 qref, size_t slice_base, int lane, int n) {
+  __shared__ uint4 stage_w[kSearchWarps][32];
+  uint4 *stage = stage_w[threadIdx.x >> 5];
+  const GridParams &g = fc.grid;
+  const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
+  const int *slot_of_rank = a.slot_of_rank + fo;
+  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const float hi2 = fc.cut2_hi;
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  if (kRel) {
+    mx = fixed_delta(qref.x, qr.x, sx);
+    my = fixed_delta(qref.y, qr.y, sy);
+    mz = fixed_delta(qref.z, qr.z, sz);
+  }
+  const int cwrap = g.wrap;
+  int y0, y1, z0, z1;
+  cell_range(ry, g.nc[1], cwrap, y0, y1);
+  cell_range(rz, g.nc[2], cwrap, z0, z1);
+  for (int ny = y0; ny < y1; ++ny)
+    for (int nz = z0; nz < z1; ++nz) {
+      const int rowcell = wrap_cell(ny, g.nc[1]) * g.nc[0] + wrap_cell(nz, g.nc[2]) * g.nc[0] * g.nc[1];
+      for (int it = 0; it < nint; it++) {
+        const int rb = start[rowcell + (it ? xa1 : xa0)], re = start[rowcell + (it ? xb1 : xb0) + 1];
+        for (int base = rb; base < re; base += 32) {
+          const int m = min(32, re - base);
+          if (lane < m) {
+            const int p = base + lane;
+            const uint4 qp = a.q[fo + p];
+            const int sp = slot_of_rank[p];
+            if (kRel)
+              stage[lane] = make_uint4(__float_as_uint(fixed_delta(qref.x, qp.x, sx)),
+                                       __float_as_uint(fixed_delta(qref.y, qp.y, sy)),
+                                       __float_as_uint(fixed_delta(qref.z, qp.z, sz)), (uint32_t)sp);
+            else
+              stage[lane] = make_uint4(qp.x, qp.y, qp.z, (uint32_t)sp);
+          }
+          __syncwarp();
+          if (mine) {
+            int j0 = 0, js = 1;
+            if (r < base) {
+              j0 = (r - base) & 1;  // p > r: owned when r + p is even
+              js = 2;
+            } else if (r >= base + m) {
+              j0 = (r - base + 1) & 1;  // p < r: owned when r + p is odd
+              js = 2;
+            }
+            for (int j = j0; j < m; j += js) {
+              const int p = base + j;
+              if (js == 1 && (p == r || ((((r + p) & 1) != 0) ? (r < p) : (r > p)))) continue;
+              const uint4 c = stage[j];
+              float dx, dy, dz;
+              if (kRel) {
+                dx = __uint_as_float(c.x) - mx;
+                dy = __uint_as_float(c.y) - my;
+                dz = __uint_as_float(c.z) - mz;
+              } else {
+                dx = fixed_delta(qr.x, c.x, sx);
+                dy = fixed_delta(qr.y, c.y, sy);
+                dz = fixed_delta(qr.z, c.z, sz);
+              }
+              const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (r2 <= hi2) nl_accept(a, fc, f, fo, r, sr, ra, p, (int)c.w, r2, slice_base, n);
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+  return n;
+}
+
+// x intervals (at most two) of the cells within one cell of [cxa, cxb] in a
+// row of nc cells, each cell once.
+__device__ __forceinline__ int x_intervals(int cxa, int cxb, int nc, int cwrap, int *xi0, int *xi1) {
+  if (cxb - cxa + 3 >= nc) {
+    xi0[0] = 0;
+    xi1[0] = nc - 1;
+    return 1;
+  }
+  if (cwrap) {
+    const int lo = cxa - 1, hi = cxb + 1;
+    if (lo < 0) {
+      xi0[0] = nc - 1;
+      xi1[0] = nc - 1;
+      xi0[1] = 0;
+      xi1[1] = hi;
+      return 2;
+    }
+    if (hi >= nc) {
+      xi0[0] = lo;
+      xi1[0] = nc - 1;
+      xi0[1] = 0;
+      xi1[1] = hi - nc;
+      return 2;
+    }
+    xi0[0] = lo;
+    xi1[0] = hi;
+    return 1;
+  }
+  xi0[0] = max(cxa - 1, 0);
+  xi1[0] = min(cxb + 1, nc - 1);
+  return 1;
+}
+
+// Per-warp bookkeeping of a search: slice width, list size, overflow.
+__device__ __forceinline__ void nl_slice_done(const KArgs &a, int f, int slice, int lane, bool active, int n) {
+  const int wmax = warp_max(active ? n : 0);
+  unsigned long long tot = active ? (unsigned long long)n : 0ull;
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (lane == 0 && slice < a.nslices) {
+    a.slice_w[(size_t)f * a.nslices + slice] = min(wmax, a.cap);
+    atomicAdd(&a.nl_count[f * 4 + 0], tot);
+    if (wmax > a.cap) atomicMax(&a.nl_count[f * 4 + 2], (unsigned long long)wmax);
+  }
+}
+
+// Classic lists (NLIST) over frames with a fixed-point frame (orthorhombic
+// box or no PBC): one warp per slice of 32 ranks, one nl_row_pass per x-row of
+// cells that the slice's rows occupy (usually one).
 __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
+  const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slice = blockIdx.x * kSearchWarps + warp;
+  const int r = slice * 32 + lane;
+  const bool active = r < a.ns && slice < a.nslices;
+  const FrameConst &fc = a.fc[f];
+  const GridParams &g = fc.grid;
+  const size_t fo = (size_t)f * a.ns;
+  int n = 0;
+  if (slice < a.nslices && g.ncells > 0) {
+    const int sr = active ? a.slot_of_rank[fo + r] : 0;
+    const bool ra = sr < a.nA;
+    const int cr = active ? a.cell_of_rank[fo + r] : 0;
+    const uint4 qr = active ? a.q[fo + r] : make_uint4(0, 0, 0, 0);
+    const size_t slice_base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    const int last = min(31, a.ns - 1 - slice * 32);  // last active lane
+    const int myrow = cr / g.nc[0];
+    const double cut = sqrt(fc.cut2);
+    int lo = 0;
+    while (lo <= last) {  // warp-uniform passes over the x-rows of the slice
+      const int row = __shfl_sync(0xffffffffu, myrow, lo);
+      const unsigned inrow = __ballot_sync(0xffffffffu, active && myrow == row);
+      const int hi = 31 - __clz(inrow);
+      const int cxa = __shfl_sync(0xffffffffu, cr, lo) % g.nc[0];
+      const int cxb = __shfl_sync(0xffffffffu, cr, hi) % g.nc[0];
+      const uint4 qref = make_uint4(__shfl_sync(0xffffffffu, qr.x, lo), __shfl_sync(0xffffffffu, qr.y, lo),
+                                    __shfl_sync(0xffffffffu, qr.z, lo), 0u);
+      int xi0[2] = {0, 0}, xi1[2] = {0, 0};
+      const int nint = x_intervals(cxa, cxb, g.nc[0], g.wrap, xi0, xi1);
+      const int ry = row % g.nc[1], rz = row / g.nc[1];
+      // relative FP32 coordinates are exact enough (error << the prefilter
+      // band) while every offset from the reference row stays within 8
+      // cutoffs, and give the minimum image while offsets stay below half the
+      // box
+      const double cw0 = g.wrap ? fc.pbc.box[0] / g.nc[0] : 1.0 / (g.inv_width[0] * g.nc[0]);
+      const double cw1 = g.wrap ? fc.pbc.box[4] / g.nc[1] : 1.0 / (g.inv_width[1] * g.nc[1]);
+      const double cw2 = g.wrap ? fc.pbc.box[8] / g.nc[2] : 1.0 / (g.inv_width[2] * g.nc[2]);
+      const int spanx = cxb - cxa + 2;
+      bool rel = fmax(spanx * cw0, 2.0 * fmax(cw1, cw2)) <= 8.0 * cut;
+      if (g.wrap) rel = rel && 2 * spanx <= g.nc[0] && g.nc[1] >= 4 && g.nc[2] >= 4 && (cxb - cxa + 3 < g.nc[0]);
+      const bool mine = active && lane >= lo && lane <= hi;
+      if (rel)
+        n = nl_row_pass<true>(a, fc, f, fo, r, sr, ra, qr, mine, ry, rz, nint, xi0[0], xi1[0], xi0[1], xi1[1], qref,
+                              slice_base, lane, n);
+      else
+        n = nl_row_pass<false>(a, fc, f, fo, r, sr, ra, qr, mine, ry, rz, nint, xi0[0], xi1[0], xi0[1], xi1[1], qref,
+                               slice_base, lane, n);
+      lo = hi + 1;
+    }
+    if (active) a.row_len[fo + r] = min(n, a.cap);
+  }
+  nl_slice_done(a, f, slice, lane, active, n);
+}
+
+// NLISTCELLS (every pair of neighbouring link cells), or a classic list in a
+// generic (triclinic) box: one warp per slice.  When the slice lies in one
+// x-row the candidates are staged as in k_nl_search, with the x-adjacency test
+// of the link cells; otherwise each lane walks its own 27 cells.
+__global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search_cells(KArgs a) {
   const int f = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int slice = blockIdx.x * kSearchWarps + warp;
@@ -470,13 +710,12 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
     const int sr = active ? slot_of_rank[r] : 0;
     const bool ra = sr < a.nA;
     const int cr = active ? a.cell_of_rank[fo + r] : 0;
-    const int cx = cr % g.nc[0], cy = (cr / g.nc[0]) % g.nc[1], cz = cr / (g.nc[0] * g.nc[1]);
     const uint4 qr = active ? a.q[fo + r] : make_uint4(0, 0, 0, 0);
+    const size_t slice_base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    const int last = min(31, a.ns - 1 - slice * 32);  // last active lane
+    const int cx = cr % g.nc[0], cy = (cr / g.nc[0]) % g.nc[1], cz = cr / (g.nc[0] * g.nc[1]);
     const int cwrap = (a.nl_kind == 2) ? a.do_pbc : g.wrap;
     const bool cells_kind = a.nl_kind == 2;
-    const size_t slice_base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
-    // the x-row of the slice's first and last active rows
-    const int last = min(31, a.ns - 1 - slice * 32);
     const int cfirst = __shfl_sync(0xffffffffu, cr, 0), clast = __shfl_sync(0xffffffffu, cr, last);
     const int rowfirst = cfirst / g.nc[0], rowlast = clast / g.nc[0];
     if (rowfirst == rowlast) {
@@ -485,36 +724,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
       // stage the same segments and meet every __syncwarp
       const int cxa = cfirst % g.nc[0], cxb = clast % g.nc[0];
       const int ry = rowfirst % g.nc[1], rz = rowfirst / g.nc[1];
-      // x intervals (at most two) covering every lane's x neighbours once
-      int xi0[2], xi1[2], nint;
-      if (cxb - cxa + 3 >= g.nc[0]) {
-        xi0[0] = 0;
-        xi1[0] = g.nc[0] - 1;
-        nint = 1;
-      } else if (cwrap) {
-        const int lo = cxa - 1, hi = cxb + 1;
-        if (lo < 0) {
-          xi0[0] = g.nc[0] - 1;
-          xi1[0] = g.nc[0] - 1;
-          xi0[1] = 0;
-          xi1[1] = hi;
-          nint = 2;
-        } else if (hi >= g.nc[0]) {
-          xi0[0] = lo;
-          xi1[0] = g.nc[0] - 1;
-          xi0[1] = 0;
-          xi1[1] = hi - g.nc[0];
-          nint = 2;
-        } else {
-          xi0[0] = lo;
-          xi1[0] = hi;
-          nint = 1;
-        }
-      } else {
-        xi0[0] = max(cxa - 1, 0);
-        xi1[0] = min(cxb + 1, g.nc[0] - 1);
-        nint = 1;
-      }
+      int xi0[2] = {0, 0}, xi1[2] = {0, 0};
+      const int nint = x_intervals(cxa, cxb, g.nc[0], cwrap, xi0, xi1);
       int y0, y1, z0, z1;
       cell_range(ry, g.nc[1], cwrap, y0, y1);
       cell_range(rz, g.nc[2], cwrap, z0, z1);
@@ -534,9 +745,6 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
               __syncwarp();
               if (active)
                 for (int j = 0; j < m; j++) {
-                  // classic lists need no adjacency test: cells are at least
-                  // NL_CUTOFF*(1+1e-9) wide, so a pair two cells apart fails the
-                  // distance test anyway
                   if (cells_kind && !x_adjacent(cx, scx[warp][j], g.nc[0], cwrap)) continue;
                   nl_candidate(a, fc, f, fo, r, sr, ra, qr, base + j, sslot[warp][j], sq[warp][j], slice_base, n);
                 }
@@ -561,15 +769,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
     }
     if (active) a.row_len[fo + r] = min(n, a.cap);
   }
-  // per-warp bookkeeping: slice width, list size, overflow
-  const int wmax = warp_max(active ? n : 0);
-  unsigned long long tot = active ? (unsigned long long)n : 0ull;
-  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  if (lane == 0 && slice < a.nslices) {
-    a.slice_w[(size_t)f * a.nslices + slice] = min(wmax, a.cap);
-    atomicAdd(&a.nl_count[f * 4 + 0], tot);
-    if (wmax > a.cap) atomicMax(&a.nl_count[f * 4 + 2], (unsigned long long)wmax);
-  }
+  nl_slice_done(a, f, slice, lane, active, n);
 }
 
 // PAIR mode list: pair i kept when |d(i, i+nA)| <= cutoff (NeighborList.cpp:150-152,252-266)

@@ -1,0 +1,62 @@
+"""The host-buffer call (coord_forward) moves data two ways: kernels that
+access the caller's pageable arrays in place (devices that use the host page
+tables, e.g. behind NVLink-C2C), or copies staged through pinned buffers
+(COORD_HOST_STAGED=1, and every other device).  Both give the same results as
+the device-pointer call on the same inputs (FP64 path: 1e-12 relative; only
+the order of the atomic additions differs)."""
+import os
+
+import numpy as np
+import pytest
+
+from plumed2_gb300.frames import jittered_lattice
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_direct_and_staged_host_paths_agree(prec):
+    from plumed2_gb300.action import Coordination
+    n, L = 2000, 13 * 0.31
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=10" % n
+    pos = jittered_lattice(n, 0.31, 0.03, 70)
+    box = np.diag([L] * 3)
+    res = {}
+    for staged in (False, True):
+        if staged:
+            os.environ["COORD_HOST_STAGED"] = "1"
+        try:
+            c = Coordination(line, precision=prec)
+            out = (np.zeros((n, 3)), np.zeros(9))
+            r0 = c.calculate(pos, box, 0)
+            r1 = c.calculate(pos, box, 1, out=out)
+            assert r1[1] is out[0]
+            res[staged] = (r0, r1)
+            c.close()
+        finally:
+            os.environ.pop("COORD_HOST_STAGED", None)
+    # the device-pointer call on the same inputs
+    c = Coordination(line, precision=prec)
+    dev = torch.device("cuda:0")
+    tp = torch.tensor(pos[None], dtype=torch.float64, device=dev)
+    s = torch.zeros(1, dtype=torch.float64, device=dev)
+    d = torch.zeros(1, n, 3, dtype=torch.float64, device=dev)
+    v = torch.zeros(1, 9, dtype=torch.float64, device=dev)
+    c.forward_device(tp.data_ptr(), box[None], 1, s.data_ptr(), d.data_ptr(), v.data_ptr(), step=0)
+    torch.cuda.synchronize()
+    ref = (s.item(), d[0].cpu().numpy(), v[0].cpu().numpy().reshape(3, 3))
+    c.close()
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    for staged in (False, True):
+        for got in res[staged]:
+            assert abs(got[0] - ref[0]) <= tol * abs(ref[0])
+            assert np.abs(got[1] - ref[1]).max() <= tol * np.abs(ref[1]).max()
+            assert np.abs(got[2] - ref[2]).max() <= tol * np.abs(ref[2]).max()
+
+
+def test_self_pair_only_host_call():
+    from plumed2_gb300.action import Coordination
+    c = Coordination("GROUPA=1 GROUPB=1 R_0=0.3")
+    s, d, v = c.calculate(np.zeros((2, 3)), np.diag([3.0] * 3))
+    assert s == 0.0 and np.all(d == 0) and np.all(v == 0)
