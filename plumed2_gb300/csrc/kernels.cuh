@@ -475,9 +475,9 @@ __device__ __noinline__ bool nl_exact(const double4 *x64, const FrameConst *fc, 
 
 // A candidate that passed the FP32 prefilter (r2 <= cut2_hi) of a classic
 // list: group and orientation, the reference's own FP64 test when r2 lies in
-// the band around cutoff^2, self pairs, store.
+// the band around cutoff^2 (in_band: r2 >= cut2_lo), self pairs, store.
 __device__ __forceinline__ void nl_accept(const KArgs &a, const FrameConst &fc, int f, size_t fo, int r, int sr,
-                                          bool ra, int p, int sp, float r2, size_t slice_base, int &n) {
+                                          bool ra, int p, int sp, bool in_band, size_t slice_base, int &n) {
   bool r_first;
   if (a.mode == MODE_TWO) {
     if (ra == (sp < a.nA)) return;
@@ -485,7 +485,7 @@ __device__ __forceinline__ void nl_accept(const KArgs &a, const FrameConst &fc, 
   } else {
     r_first = sr < sp;
   }
-  if (!(r2 < fc.cut2_lo) && !nl_exact(a.x64 + fo, &fc, a.do_pbc, r_first ? r : p, r_first ? p : r)) return;
+  if (in_band && !nl_exact(a.x64 + fo, &fc, a.do_pbc, r_first ? r : p, r_first ? p : r)) return;
   if (a.has_dup && a.abs_of_slot[sp] == a.abs_of_slot[sr]) {
     // a self pair: counted in the list size, skipped by the CV loop
     // (CoordinationBase.cpp:183); kept aside for coord_get_pairs
@@ -520,7 +520,7 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
   const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
   const int *slot_of_rank = a.slot_of_rank + fo;
   const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
-  const float hi2 = fc.cut2_hi;
+  const float hi2 = fc.cut2_hi, lo2 = fc.cut2_lo;
   float mx = 0.f, my = 0.f, mz = 0.f;
   if (kRel) {
     mx = fixed_delta(qref.x, qr.x, sx);
@@ -551,17 +551,12 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
           }
           __syncwarp();
           if (mine) {
-            int j0 = 0, js = 1;
-            if (r < base) {
-              j0 = (r - base) & 1;  // p > r: owned when r + p is even
-              js = 2;
-            } else if (r >= base + m) {
-              j0 = (r - base + 1) & 1;  // p < r: owned when r + p is odd
-              js = 2;
-            }
-            for (int j = j0; j < m; j += js) {
-              const int p = base + j;
-              if (js == 1 && (p == r || ((((r + p) & 1) != 0) ? (r < p) : (r > p)))) continue;
+            // branch-free tests record the candidates within cut2_hi (hit)
+            // and those inside the band (band) as bits of j; the accepted
+            // ones are handled afterwards, so the divergent accept path runs
+            // once per hit of the busiest lane rather than at every j
+            uint32_t hit = 0u, band = 0u;
+            auto test = [&](int j) {
               const uint4 c = stage[j];
               float dx, dy, dz;
               if (kRel) {
@@ -574,7 +569,30 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
                 dz = fixed_delta(qr.z, c.z, sz);
               }
               const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-              if (r2 <= hi2) nl_accept(a, fc, f, fo, r, sr, ra, p, (int)c.w, r2, slice_base, n);
+              hit |= (r2 <= hi2 ? 1u : 0u) << j;
+              band |= (r2 < lo2 ? 0u : 1u) << j;
+            };
+            if (r < base || r >= base + m) {
+              // the whole batch lies above r (owned when r + p is even) or
+              // below it (owned when r + p is odd): every other candidate
+              const int j0 = (r < base) ? ((r - base) & 1) : ((r - base + 1) & 1);
+              int j = j0;
+              for (; j + 2 < m; j += 4) {
+                test(j);
+                test(j + 2);
+              }
+              if (j < m) test(j);
+            } else {
+              for (int j = 0; j < m; j++) {
+                const int p = base + j;
+                if (p == r || ((((r + p) & 1) != 0) ? (r < p) : (r > p))) continue;
+                test(j);
+              }
+            }
+            while (hit) {
+              const int j = __ffs(hit) - 1;
+              hit &= hit - 1u;
+              nl_accept(a, fc, f, fo, r, sr, ra, base + j, (int)stage[j].w, (band >> j) & 1u, slice_base, n);
             }
           }
           __syncwarp();
