@@ -99,8 +99,10 @@ struct coord_ctx {
   // host-API staging
   DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam, d_bvir, d_bpar;
   // saved forward (COORD_FLAG_SAVE)
-  DevBuf<double> sv_deriv, sv_vir, sv_par;
-  bool saved_valid = false, saved_param = false;
+  // saved forward: the derivative accumulators stay in place (acc_kept), the
+  // virial and parameter derivatives are copied aside
+  DevBuf<double> sv_vir, sv_par;
+  bool saved_valid = false, saved_param = false, acc_kept = false;
   int saved_frames = 0;
   HostBuf<double> h_pos, h_out;
   HostBuf<FrameConst> h_fc;
@@ -190,6 +192,10 @@ int frame_setup(coord_ctx *c, const double *box, FrameConst *fc, bool *need_boun
   }
   g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
   fc->cut2 = cut * cut;
+  struct FinishFixed {  // the one-FMA constants once inv_l and grid.lo are final
+    FrameConst *fc;
+    ~FinishFixed() { fixed_frame_finish(*fc); }
+  } finish_fixed{fc};
   // fixed-point frame
   if (usepbc && fc->pbc.type == PBC_ORTHO) {
     fc->fixed_ok = 1;
@@ -361,6 +367,19 @@ int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bo
   return COORD_OK;
 }
 
+// A saved forward left ds/dx in the accumulators; any other pass needs them
+// zero first.
+int clear_kept_acc(coord_ctx *c) {
+  if (!c->acc_kept) return COORD_OK;
+  cudaError_t e = cudaSuccess;
+  if (c->acc32.p) e = cudaMemsetAsync(c->acc32.p, 0, c->acc32.n * sizeof(float4), c->stream);
+  if (!e && c->acc64.p) e = cudaMemsetAsync(c->acc64.p, 0, c->acc64.n * sizeof(double), c->stream);
+  if (e) return c->cuda_fail(e, "clearing saved derivatives");
+  c->acc_kept = false;
+  c->saved_valid = false;
+  return COORD_OK;
+}
+
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
 void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
@@ -406,6 +425,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
   }
   if (tev1) cudaEventRecord(tev1, c->stream);
   const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  if (a.keep_acc && !a.out_deriv) return;  // saved forward, no copy of ds/dx wanted
   if (mixed)
     launch_finalize32(a, rank_order, c->stream);
   else
@@ -437,6 +457,7 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
       KArgs aa = a;
       aa.partials = c->partials.p;
       aa.max_blocks = c->max_blocks;
+      aa.keep_acc = 0;  // every candidate clears its accumulators
       cudaEventRecord(t0, c->stream);
       launch_evaluation(c, aa, mode);
       cudaEventRecord(t1, c->stream);
@@ -516,16 +537,17 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
 
   const bool save = (flags & COORD_FLAG_SAVE) && !(flags & COORD_FLAG_NO_DERIV);
   c->saved_valid = false;
+  if ((rc = clear_kept_acc(c))) return rc;
   if (save) {
     cudaError_t es;
-    if ((es = c->sv_deriv.ensure((size_t)n_frames * c->ns * 3)) || (es = c->sv_vir.ensure((size_t)n_frames * 9)) ||
-        (es = c->sv_par.ensure((size_t)n_frames * 2)))
+    if ((es = c->sv_vir.ensure((size_t)n_frames * 9)) || (es = c->sv_par.ensure((size_t)n_frames * 2)))
       return c->cuda_fail(es, "allocation of the saved forward");
   }
-  double *const k_deriv = (flags & COORD_FLAG_NO_DERIV) ? nullptr : (save ? c->sv_deriv.p : deriv);
+  double *const k_deriv = (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv;
   double *const k_virial = (flags & COORD_FLAG_NO_DERIV) ? nullptr : (save ? c->sv_vir.p : virial);
   double *const k_dparam = save ? c->sv_par.p : dparam;
   KArgs a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
+  a.keep_acc = save ? 1 : 0;
   cudaError_t e;
   if (rebuild) cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
   if (need_bounds && (mixed || rebuild)) {
@@ -575,6 +597,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
         if (!again) break;
         if ((rc = ensure_buffers(c, n_frames))) return rc;
         a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
+        a.keep_acc = save ? 1 : 0;
         if (attempt == 7) return c->fail(COORD_ERR_NOMEM, "neighbour list did not fit after 8 attempts");
       }
     }
@@ -592,9 +615,9 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   }
   launch_evaluation(c, a, mode);
   if (save) {
-    // hand the caller its copies of what was kept
-    const size_t nd = (size_t)n_frames * c->ns * 3;
-    if (deriv && nd) cudaMemcpyAsync(deriv, c->sv_deriv.p, nd * sizeof(double), cudaMemcpyDefault, c->stream);
+    // ds/dx stays in the accumulators until the backward; the caller gets
+    // its copies of the virial and parameter derivatives
+    c->acc_kept = true;
     if (virial) cudaMemcpyAsync(virial, c->sv_vir.p, (size_t)n_frames * 9 * sizeof(double), cudaMemcpyDefault,
                                 c->stream);
     c->saved_param = (flags & COORD_FLAG_DR0) != 0;
@@ -773,7 +796,6 @@ int coord_destroy(coord_ctx *c) {
   c->d_dparam.release();
   c->d_bvir.release();
   c->d_bpar.release();
-  c->sv_deriv.release();
   c->sv_vir.release();
   c->sv_par.release();
   c->h_pos.release();
@@ -966,15 +988,24 @@ int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const d
     return c->cuda_fail(e, "allocation");
   if (c->saved_valid && c->saved_frames == n_frames && (!grad_param || c->saved_param)) {
     // the forward kept ds/dx, the virial and ds/d(R_0, D_0): scale them
-    KArgs a = make_args(c, n_frames, pos, 0, nullptr, nullptr, nullptr, nullptr);
+    KArgs a = make_args(c, n_frames, pos, 0, nullptr, grad_pos, nullptr, nullptr);
     a.g = g;
-    if (grad_pos && c->ns) launch_scale_saved(a, c->sv_deriv.p, grad_pos, c->stream);
+    // g * ds/dx from the kept accumulators, which are cleared on the way
+    const bool nl_order = c->p.nlist != COORD_NL_NONE && c->mode != MODE_PAIR;
+    if (c->p.precision == COORD_PREC_MIXED)
+      launch_finalize32(a, nl_order ? 1 : 0, c->stream);
+    else
+      launch_finalize64(a, nl_order ? 1 : 0, c->stream);
+    c->acc_kept = false;
+    c->saved_valid = false;
     if (grad_box || grad_param) launch_grad_post(a, c->sv_vir.p, c->sv_par.p, grad_box, grad_param, c->stream);
     if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "backward launch");
     return COORD_OK;
   }
+  int rc = clear_kept_acc(c);
+  if (rc) return rc;
   bool need_bounds = false;
-  int rc = upload_frames(c, n_frames, boxes, &need_bounds);
+  rc = upload_frames(c, n_frames, boxes, &need_bounds);
   if (rc) return rc;
   KArgs a = make_args(c, n_frames, pos, COORD_FLAG_DR0, nullptr, grad_pos, c->d_bvir.p, c->d_bpar.p);
   a.g = g;

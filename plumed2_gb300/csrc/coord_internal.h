@@ -86,11 +86,27 @@ struct FrameConst {
   GridParams grid;
   double cut2;        // NL_CUTOFF^2 (classic test, NeighborList.cpp:238)
   float  cut2_lo, cut2_hi; // FP32 prefilter band around cut2
-  // fixed-point frame of the mixed path: q = frac(x * inv_l) * 2^32
+  // fixed-point frame of the mixed path: q = frac((x - grid.lo) * inv_l) * 2^32
   double inv_l[3];
   float  scale[3];    // L / 2^32 per axis (FP32)
   int    fixed_ok;    // box is orthorhombic (or none) so fixed point applies
+  // the same q in one FMA: q = rn(x * fx_s + fx_c) mod 2^32 with
+  // fx_s = inv_l * 2^32 and fx_c = -grid.lo * fx_s (fixed_frame_finish)
+  double fx_s[3], fx_c[3];
 };
+
+#ifdef __CUDACC__
+#define COORD_HD __host__ __device__
+#else
+#define COORD_HD
+#endif
+// Fills the one-FMA constants of the fixed-point frame from inv_l and grid.lo.
+COORD_HD inline void fixed_frame_finish(FrameConst &fc) {
+  for (int k = 0; k < 3; k++) {
+    fc.fx_s[k] = fc.inv_l[k] * 4294967296.0;
+    fc.fx_c[k] = -(fc.grid.lo[k] * fc.fx_s[k]);
+  }
+}
 
 // Pair modes (NeighborList::NNStyle, NeighborList.h:39).
 enum PairMode : int { MODE_SINGLE = 0, MODE_TWO = 1, MODE_PAIR = 2 };

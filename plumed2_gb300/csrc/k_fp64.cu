@@ -101,12 +101,6 @@ void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_fl
   g_launches += 1;
 }
 
-void launch_scale_saved(const KArgs &a, const double *saved, double *grad, cudaStream_t s) {
-  const size_t n = (size_t)a.ns * 3;
-  k_scale_saved<<<dim3((unsigned)((n + 255) / 256), a.nframes), 256, 0, s>>>(a, saved, grad);
-  g_launches += 1;
-}
-
 void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, double *grad_box, double *grad_param,
                       cudaStream_t s) {
   k_grad_post<<<(a.nframes + 63) / 64, 64, 0, s>>>(a, vir, dpar, grad_box, grad_param);

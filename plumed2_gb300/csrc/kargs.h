@@ -23,6 +23,7 @@ struct KArgs {
   int nslices;    // ceil(ns/32)
   int flags;      // COORD_FLAG_* of the call
   int has_dup;    // some absolute index appears in two slots (self pairs possible)
+  int keep_acc;   // finalize leaves the derivative accumulators in place (saved forward)
   FrameConst *fc;               // [nframes]
   const int64_t *abs_of_slot;   // [ns]
   const double *pos;            // [nframes][ns][3]   input, slot order

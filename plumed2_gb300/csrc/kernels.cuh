@@ -114,15 +114,16 @@ __device__ void block_partials_finish(const KArgs &a, int frame, double v[kParti
 // ---------------------------------------------------------------------------
 // fixed-point positions (mixed path and the FP32 neighbour-list prefilter)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t to_fixed(double x, double lo, double inv_l) {
-  double f = (x - lo) * inv_l;
-  f = f - floor(f);
-  const long long v = __double2ll_rn(f * 4294967296.0);
-  return (uint32_t)(v & 0xffffffffll);
+// Two FP64 operations per coordinate (the FP64 pipe is the bound of the O(N)
+// kernels that convert positions): rn((x - lo) / L * 2^32) as one FMA and one
+// conversion; the low 32 bits of the 64-bit integer are the fraction of the
+// frame, wrapped exactly as frac() would (to within the final rounding).
+__device__ __forceinline__ uint32_t to_fixed_fma(double x, double s, double c) {
+  return (uint32_t)(unsigned long long)__double2ll_rn(fma(x, s, c));
 }
 __device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x) {
-  return make_uint4(to_fixed(x[0], fc.grid.lo[0], fc.inv_l[0]), to_fixed(x[1], fc.grid.lo[1], fc.inv_l[1]),
-                    to_fixed(x[2], fc.grid.lo[2], fc.inv_l[2]), 0u);
+  return make_uint4(to_fixed_fma(x[0], fc.fx_s[0], fc.fx_c[0]), to_fixed_fma(x[1], fc.fx_s[1], fc.fx_c[1]),
+                    to_fixed_fma(x[2], fc.fx_s[2], fc.fx_c[2]), 0u);
 }
 __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float scale) {
   return (float)(int)(b - a) * scale;  // wraps modulo 2^32: minimum image
@@ -268,6 +269,7 @@ __global__ void k_bounds_finish(KArgs a, const unsigned long long *mm, double cu
     fc.scale[k] = (float)(span / 4294967296.0);
     spanmax = fmax(spanmax, span);
   }
+  fixed_frame_finish(fc);
   // FP32 prefilter band around cutoff^2 (covers quantisation and rounding)
   const double band = 1e-4 * fc.cut2 + 8.0 * cutoff * spanmax / 4294967296.0 + 1e-12;
   fc.cut2_lo = (float)(fc.cut2 - band);
@@ -829,9 +831,11 @@ __global__ void k_finalize64(KArgs a, int rank_order) {
     o[1] = g * acc[1];
     o[2] = g * acc[2];
   }
-  acc[0] = 0.0;
-  acc[1] = 0.0;
-  acc[2] = 0.0;
+  if (!a.keep_acc) {
+    acc[0] = 0.0;
+    acc[1] = 0.0;
+    acc[2] = 0.0;
+  }
 }
 __global__ void k_finalize32(KArgs a, int rank_order) {
   const int f = blockIdx.y;
@@ -847,17 +851,9 @@ __global__ void k_finalize32(KArgs a, int rank_order) {
     o[1] = g * (double)v.y;
     o[2] = g * (double)v.z;
   }
-  a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// backward from a saved forward: grad = g * saved ds/dx (slot order)
-__global__ void k_scale_saved(KArgs a, const double *saved, double *grad) {
-  const int f = blockIdx.y;
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n = (size_t)a.ns * 3;
-  if (i >= n) return;
-  grad[(size_t)f * n + i] = a.g[f] * saved[(size_t)f * n + i];
-}
 
 // ---------------------------------------------------------------------------
 // FP64 pair math of one (first, second) pair: the reference's operations.

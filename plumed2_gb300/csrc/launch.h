@@ -23,7 +23,6 @@ void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStre
 void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int mode, int tile, int nblocks, cudaStream_t s);
 void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_flags, cudaStream_t s);
 void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s);
-void launch_scale_saved(const KArgs &a, const double *saved, double *grad, cudaStream_t s);
 void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, double *grad_box, double *grad_param,
                       cudaStream_t s);
 

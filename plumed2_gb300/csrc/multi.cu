@@ -571,6 +571,7 @@ int coord_multi_forward_device(coord_multi *m, int n_frames, const double *pos, 
       fc.inv_l[k] = fc.pbc.invbox[4 * k];
       fc.scale[k] = (float)(fc.pbc.box[4 * k] / 4294967296.0);
     }
+    fixed_frame_finish(fc);
   }
   if (!m->groups.empty()) {
     if ((e = m->fc.ensure(n_frames)) || (e = m->qsys.ensure((size_t)n_frames * m->n_atoms)))
