@@ -432,17 +432,22 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
     launch_finalize64(a, rank_order, c->stream);
 }
 
-// The project's autotuner for the mixed neighbour-list pass: blocks per SM
-// (2, 4, 6, 8 resident 256-thread blocks) x gathers in flight per lane
-// (unroll 2, 4, 8), each candidate timed once with CUDA events on the
-// context's stream; the fastest is kept for the context.  Every candidate run
+// The project's autotuner for the mixed neighbour-list pass: persistent grids
+// of 2 to 32 256-thread blocks per SM, or one slice per warp -- grids larger
+// than what is resident run in waves that the hardware dispatches in frame
+// order, so only a few frames' positions and accumulators compete for L2 --
+// x gathers in flight per lane (unroll 2, 4, 8); each candidate is timed
+// once with CUDA events on the context's stream and the fastest kept, per
+// mode.  Every candidate run
 // is a complete pass (its finalize kernel rewrites the outputs), so the
 // results of the call are unaffected.
 void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  const int bps[4] = {2, 4, 6, 8}, unr[3] = {2, 4, 8};
+  // blocks per SM: up to 8 all resident at once; 16 and 32 run in waves, so
+  // a few frames at a time hold L2; 0: one slice per warp
+  const int bps[7] = {2, 4, 6, 8, 16, 32, 0}, unr[3] = {2, 4, 8};
   const int m = std::min(std::max(mode, 0), 2);
   float best = 1e30f;
   int bb = c->nl_blocks, bu = c->nl_unroll;
@@ -450,9 +455,10 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   c->timing = false;
   for (int b : bps)
     for (int u : unr) {
-      c->nlm_blocks[m] = b * std::max(c->nsm, 1);
+      const int slices_blocks = (int)(((c->ns + 31) / 32 + 7) / 8);  // blocks of one frame at one slice per warp
+      c->nlm_blocks[m] = b > 0 ? b * std::max(c->nsm, 1) : a.nframes * slices_blocks;
       c->nlm_unroll[m] = u;
-      c->max_blocks = std::max(c->max_blocks, c->nlm_blocks[m]);
+      c->max_blocks = std::max(c->max_blocks, std::min(slices_blocks, (c->nlm_blocks[m] + a.nframes - 1) / a.nframes));
       if (ensure_buffers(c, a.nframes)) continue;
       KArgs aa = a;
       aa.partials = c->partials.p;
