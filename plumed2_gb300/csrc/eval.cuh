@@ -143,6 +143,12 @@ struct Acc32 {
   }
 };
 
+// Asks the TMA engine to bring [p, p + bytes) into L2 (no registers, no
+// completion to wait for); p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Fire-and-forget vector reduction into a float4 accumulator (16-byte aligned).
 __device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z), "f"(0.f)
@@ -170,11 +176,27 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
   const uint4 *__restrict__ q = a.q + fo;
   float4 *__restrict__ acc4 = a.acc32 + fo;
   Acc32 acc;
+  const size_t slice_words = (size_t)a.cap * 32;
+  const uint32_t *ell_f = a.ell + (size_t)f * a.nslices * slice_words;
+  const int *sw_f = a.slice_w + (size_t)f * a.nslices;
+  {
+    // this warp's first slice: its entries (w rows of 32 words) into L2
+    const int s0 = blockIdx.x * wpb + (threadIdx.x >> 5);
+    if (lane == 0 && s0 < a.nslices) {
+      const int w0 = sw_f[s0];
+      if (w0 > 0) prefetch_l2_bulk(ell_f + (size_t)s0 * slice_words, (uint32_t)w0 * 128u);
+    }
+  }
   for (int slice = blockIdx.x * wpb + (threadIdx.x >> 5); slice < a.nslices; slice += nw) {
     const int r = slice * 32 + lane;
     const bool active = r < a.ns;
     const int len = active ? a.row_len[fo + r] : 0;
-    const int w = a.slice_w[(size_t)f * a.nslices + slice];
+    const int w = sw_f[slice];
+    if (lane == 0 && slice + nw < a.nslices) {
+      // the next slice's entries stream into L2 while this one is evaluated
+      const int wn = sw_f[slice + nw];
+      if (wn > 0) prefetch_l2_bulk(ell_f + (size_t)(slice + nw) * slice_words, (uint32_t)wn * 128u);
+    }
     const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
     float ax = 0.f, ay = 0.f, az = 0.f;
     const uint32_t *__restrict__ e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
