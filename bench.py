@@ -121,6 +121,23 @@ class Clocks:
         return out
 
 
+PROFILE_EVAL = os.path.join(ROOT, "profiles", "k_eval_nl32_262144atoms_16walkers.md")
+PROFILE_EVAL_PAIRS = 158607420  # pair-evaluations of the launch that capture measured
+
+
+def eval_traffic(pairs_launch):
+    """DRAM bytes (read + write) per pair-kernel launch from the committed ncu summary, scaled to this launch's
+    pair count when the workload differs from the captured one; None without the summary."""
+    try:
+        for line in open(PROFILE_EVAL):
+            if line.startswith("traffic_bytes_per_launch:"):
+                t = float(line.split(":", 1)[1])
+                return t * pairs_launch / PROFILE_EVAL_PAIRS
+    except OSError:
+        pass
+    return None
+
+
 def rank_walkers(rank, walkers_per_rank):
     """Walker seeds a rank owns: disjoint blocks, so N ranks run N x the walkers with no exchange
     (weak scaling)."""
@@ -366,6 +383,12 @@ def run_ours(args):
             roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
                     "frac": frac_fp32, "traffic": None,
                     "peak_source": "coord_measure_peaks FP32 FMA microbenchmark (measured live)"}
+        traffic = eval_traffic(pairs_launch)
+        for k in ("traffic",):
+            roof[k] = traffic
+        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                  "profiles/k_eval_nl32_262144atoms_16walkers.md" +
+                                  ("" if pairs_launch == PROFILE_EVAL_PAIRS else ", scaled by pair count"))
         kt = sorted(ktimes) or [0.0]
         roof.update({"kernel": "k_eval_nl32 (mixed NL pair kernel)", "kernel_ms": kern_ms, "launches": kern_n,
                      "kernel_ms_min_median_max": [kt[0], kt[len(kt) // 2], kt[-1]],
