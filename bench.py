@@ -403,18 +403,24 @@ def run_ours(args):
                      "pageable host arrays through the host page tables" if pageable and tables and
                      os.environ.get("COORD_HOST_STAGED") != "1" else "staged through pinned host buffers")
         if args.e2e_steps > 0:
+            from plumed2_gb300._lib import addr
             ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
             host_pos = [np.ascontiguousarray(frames[w]) for w in range(W)]
-            # per walker force and virial arrays reused from step to step, as an MD engine does
-            outs = [(np.zeros((n, 3)), np.zeros(9)) for _ in range(W)]
+            # per walker force and virial arrays reused from step to step, as an MD engine does; the call is the
+            # C ABI's coord_forward with the arrays' addresses, as the PLUMED plugin makes it
+            outs = [(np.zeros((n, 3)), np.zeros(9), np.zeros(1)) for _ in range(W)]
+            hbox = np.ascontiguousarray(box.reshape(9))
+            ptrs = [(addr(host_pos[w]), addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
             for w in range(W):
-                ctxs[w].calculate(host_pos[w], box, 0, out=outs[w])
+                ctxs[w].forward_host(ptrs[w][0], addr(hbox), 0, 0, ptrs[w][1], ptrs[w][2], ptrs[w][3])
             t0 = time.perf_counter()
             npairs = 0
             for k in range(1, 1 + args.e2e_steps):
                 for w in range(W):
-                    sv, dv, vv = ctxs[w].calculate(host_pos[w], box, k, out=outs[w])
+                    ctxs[w].forward_host(ptrs[w][0], addr(hbox), k, 0, ptrs[w][1], ptrs[w][2], ptrs[w][3])
             te = time.perf_counter() - t0
+            # the results landed in the caller's arrays
+            assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
             npairs = sum(ctxs[w].nl_size() for w in range(W)) * args.e2e_steps
             e2e_v = npairs / te
             h2d = W * n * 3 * 8
@@ -443,7 +449,8 @@ def run_ours(args):
                        "parallelism": "walkers sharded across GPUs, no collective"},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "call": "coord_forward (host arrays) per walker and step, %d steps" % args.e2e_steps,
+                    "call": "coord_forward (C ABI, host arrays by address) per walker and step, %d steps" %
+                            args.e2e_steps,
                     "host_path": host_path},
             "gpu_launches": launches, "clocks": clk,
         }

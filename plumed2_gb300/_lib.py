@@ -78,6 +78,10 @@ def load() -> C.CDLL:
         L.coord_switch_eval.argtypes = [_vp, C.c_int, _dp, C.c_int, _dp, _dp]
         L.coord_switch_params.argtypes = [_vp, _dp]
         L.coord_forward.argtypes = [_vp, _dp, _dp, C.c_int64, C.c_uint, _dp, _dp, _dp]
+        # the same entry with plain addresses (integers), as a compiled caller passes them
+        L.coord_forward_addr = L["coord_forward"]
+        L.coord_forward_addr.argtypes = [_vp, _vp, _vp, C.c_int64, C.c_uint, _vp, _vp, _vp]
+        L.coord_forward_addr.restype = C.c_int
         L.coord_forward_device.argtypes = [_vp, C.c_int, _vp, _dp, C.c_int64, C.c_uint, _vp, _vp, _vp, _vp, _vp]
         L.coord_backward_device.argtypes = [_vp, C.c_int, _vp, _dp, _vp, _vp, _vp, _vp, _vp]
         L.coord_nl_size.argtypes = [_vp, C.c_int, C.POINTER(C.c_int64)]
@@ -103,7 +107,12 @@ def load() -> C.CDLL:
 
 
 def dptr(a: np.ndarray):
-    return a.ctypes.data_as(_dp)
+    return C.cast(a.__array_interface__["data"][0], _dp)
+
+
+def addr(a: np.ndarray) -> int:
+    """Address of a numpy array's first element."""
+    return a.__array_interface__["data"][0]
 
 
 def check(L, ctx, rc: int):

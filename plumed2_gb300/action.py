@@ -190,6 +190,17 @@ class Coordination:
         check(self._L, self._ctx, rc)
         return s.value, deriv, (vir.reshape(3, 3) if derivatives else None)
 
+    def forward_host(self, pos_addr: int, box_addr: int, step: int, flags: int, s_addr: int, deriv_addr: int,
+                     virial_addr: int):
+        """coord_forward with plain addresses of host arrays (positions nslots x 3, box 9, s 1, derivatives
+        nslots x 3, virial 9): the call a compiled caller such as the PLUMED plugin makes, with no array
+        checks on the Python side."""
+        self._ensure_groups()
+        rc = self._L.coord_forward_addr(self._ctx, pos_addr, box_addr, int(step), int(flags), s_addr,
+                                        deriv_addr or None, virial_addr or None)
+        if rc:
+            check(self._L, self._ctx, rc)
+
     def calculate_system(self, system_positions, box, step: int = 0, **kw):
         """Gather the requested atoms from a full system array and calculate."""
         sp = np.asarray(system_positions, dtype=np.float64).reshape(-1, 3)

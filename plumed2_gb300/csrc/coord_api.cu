@@ -87,7 +87,8 @@ struct coord_ctx {
   // device buffers
   DevBuf<int64_t> abs_of_slot;
   DevBuf<FrameConst> fc;
-  DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, scatter_tmp, row_len, slice_w, cell_of_rank;
+  DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, rank_of_slot, scatter_tmp, row_len, slice_w,
+      cell_of_rank;
   DevBuf<double4> x64;
   DevBuf<uint4> q;
   DevBuf<uint32_t> ell, self_pairs;
@@ -229,6 +230,7 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   }
   ENS(c->fc, F);
   ENS(c->slot_of_rank, F * ns);
+  ENS(c->rank_of_slot, F * ns);
   ENS(c->cell_of_rank, F * ns);
   ENS(c->cell_of_slot, F * ns);
   ENS(c->scatter_tmp, F * ns);
@@ -280,6 +282,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.cell_start = c->cell_start.p;
   a.cell_fill = c->cell_fill.p;
   a.slot_of_rank = c->slot_of_rank.p;
+  a.rank_of_slot = c->rank_of_slot.p;
   a.cell_of_rank = c->cell_of_rank.p;
   a.scatter_tmp = c->scatter_tmp.p;
   a.x64 = c->x64.p;
@@ -380,13 +383,26 @@ int clear_kept_acc(coord_ctx *c) {
   return COORD_OK;
 }
 
+// Host arrays of a coord_forward call on a device that accesses them in
+// place: the positions are turned into the pair kernel's fixed-point,
+// rank-ordered copy in one pass over the caller's array, and the derivatives
+// go from the accumulators to the caller's array in one pass.
+struct HostIO {
+  const double *pos;  // caller's positions (slot order)
+  double *deriv;      // caller's derivatives (slot order) or nullptr
+  bool fused;         // prep/finalize straight from/to the caller's arrays
+};
+
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
-void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
+void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io = nullptr) {
   const bool nl = c->p.nlist != COORD_NL_NONE;
   const bool mixed = c->p.precision == COORD_PREC_MIXED;
+  const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
   // positions for the pair kernel: fixed-point (mixed) or FP64 in rank order
-  if (c->mode == MODE_PAIR || !nl) {
+  if (io && io->fused) {
+    launch_prep_host(a, io->pos, rank_order, c->stream);
+  } else if (c->mode == MODE_PAIR || !nl) {
     if (mixed) launch_gather(a, 0, 0, 1, c->stream);
   } else {
     launch_gather(a, 1, mixed ? 0 : 1, mixed ? 1 : 0, c->stream);
@@ -424,7 +440,10 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode) {
     }
   }
   if (tev1) cudaEventRecord(tev1, c->stream);
-  const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  if (io && io->fused && io->deriv) {
+    launch_finalize_host32(a, io->deriv, rank_order, c->stream);
+    return;
+  }
   if (a.keep_acc && !a.out_deriv) return;  // saved forward, no copy of ds/dx wanted
   if (mixed)
     launch_finalize32(a, rank_order, c->stream);
@@ -488,7 +507,8 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
 }
 
 int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
-                 double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream) {
+                 double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream,
+                 HostIO *hio = nullptr) {
   if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
   if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
   if (c->ns == 0) {
@@ -548,6 +568,12 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     cudaError_t es;
     if ((es = c->sv_vir.ensure((size_t)n_frames * 9)) || (es = c->sv_par.ensure((size_t)n_frames * 2)))
       return c->cuda_fail(es, "allocation of the saved forward");
+  }
+  if (hio) {
+    // fused host transfers on steps that need no device copy of the positions
+    // (no rebuild, no bounding frame): mixed pair kernels only
+    hio->fused = mixed && !rebuild && !need_bounds && c->mode != MODE_PAIR && !save;
+    if (!hio->fused) launch_copy(hio->pos, const_cast<double *>(d_pos), (size_t)n_frames * c->ns * 3, c->stream);
   }
   double *const k_deriv = (flags & COORD_FLAG_NO_DERIV) ? nullptr : deriv;
   double *const k_virial = (flags & COORD_FLAG_NO_DERIV) ? nullptr : (save ? c->sv_vir.p : virial);
@@ -619,7 +645,9 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     a.partials = c->partials.p;
     a.max_blocks = c->max_blocks;
   }
-  launch_evaluation(c, a, mode);
+  launch_evaluation(c, a, mode, hio);
+  if (hio && !hio->fused && hio->deriv && k_deriv)
+    launch_copy(k_deriv, hio->deriv, (size_t)n_frames * c->ns * 3, c->stream);
   if (save) {
     // ds/dx stays in the accumulators until the backward; the caller gets
     // its copies of the virial and parameter derivatives
@@ -928,13 +956,15 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   }
   if (c->host_direct && !(flags & COORD_FLAG_SAVE)) {
     // The device reads and writes the caller's pageable arrays through the
-    // host page tables (cache-coherent CPU-GPU link): one kernel pulls the
-    // positions in, the pair pass writes s, the virial and the derivatives
-    // straight into the caller's arrays.
-    if ((e = c->d_pos.ensure(n3))) return c->cuda_fail(e, "staging allocation");
-    launch_copy_in(pos, c->d_pos.p, n3, c->stream);
-    int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, s, want_d ? deriv : nullptr,
-                          want_d ? virial : nullptr, nullptr, nullptr);
+    // host page tables (cache-coherent CPU-GPU link).  Streaming copies move
+    // the arrays (coalesced, whole lines across the link); the derivatives
+    // are scattered to slot order in HBM first, never across the link.  s and
+    // the virial are written by the pair pass straight into the caller's
+    // variables.
+    if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3))) return c->cuda_fail(e, "staging allocation");
+    HostIO hio{pos, want_d ? deriv : nullptr, false};
+    int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, s, want_d ? c->d_deriv.p : nullptr,
+                          want_d ? virial : nullptr, nullptr, nullptr, &hio);
     if (rc) return rc;
     if ((e = cudaStreamSynchronize(c->stream))) return c->cuda_fail(e, "forward");
     return COORD_OK;

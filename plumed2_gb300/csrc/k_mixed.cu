@@ -93,6 +93,16 @@ void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32
   g_launches += 1;
 }
 
+void launch_prep_host(const KArgs &a, const double *hpos, int rank_order, cudaStream_t s) {
+  k_prep_host<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, hpos, rank_order);
+  g_launches += 1;
+}
+
+void launch_finalize_host32(const KArgs &a, double *hderiv, int rank_order, cudaStream_t s) {
+  k_finalize_host32<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, hderiv, rank_order);
+  g_launches += 1;
+}
+
 void launch_finalize32(const KArgs &a, int rank_order, cudaStream_t s) {
   k_finalize32<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order);
   g_launches += 1;

@@ -32,6 +32,7 @@ struct KArgs {
   int *cell_start;              // [nframes][ncell_cap+1]
   int *cell_fill;               // [nframes][ncell_cap]
   int *slot_of_rank;            // [nframes][ns]
+  int *rank_of_slot;            // [nframes][ns] inverse of slot_of_rank (neighbour-list build)
   int *cell_of_rank;            // [nframes][ns] cell of each rank (neighbour-list build)
   int *scatter_tmp;             // [nframes][ns]
   double4 *x64;                 // [nframes][ns] sorted (or slot-order) FP64 positions

@@ -348,6 +348,7 @@ __global__ void k_cell_sort(KArgs a) {
   const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
   const int *tmp = a.scatter_tmp + (size_t)f * a.ns;
   int *out = a.slot_of_rank + (size_t)f * a.ns;
+  int *inv = a.rank_of_slot + (size_t)f * a.ns;
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int b = start[c], m = start[c + 1] - b;
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -355,8 +356,39 @@ __global__ void k_cell_sort(KArgs a) {
       int r = 0;
       for (int j = 0; j < m; j++) r += (tmp[b + j] < v);
       out[b + r] = v;
+      inv[v] = b + r;
     }
   }
+}
+
+// Host-array calls on devices that access pageable host memory in place:
+// positions read from the caller's array in slot order (coalesced across the
+// link) and written as fixed-point values straight to rank order, replacing
+// a copy and k_gather; derivatives read through rank_of_slot and written to
+// the caller's array in slot order, replacing k_finalize32 and a copy.
+__global__ void k_prep_host(KArgs a, const double *__restrict__ hpos, int rank_order) {
+  const int f = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  const size_t fo = (size_t)f * a.ns;
+  const double *x = hpos + (fo + s) * 3;
+  const double xx[3] = {x[0], x[1], x[2]};
+  const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+  a.q[fo + r] = fixed_of(a.fc[f], xx);
+}
+__global__ void k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
+  const int f = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  const size_t fo = (size_t)f * a.ns;
+  const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+  const float4 v = a.acc32[fo + r];
+  const double g = a.g ? a.g[f] : 1.0;
+  double *o = hderiv + (fo + s) * 3;
+  o[0] = g * (double)v.x;
+  o[1] = g * (double)v.y;
+  o[2] = g * (double)v.z;
+  if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter

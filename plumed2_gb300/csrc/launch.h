@@ -13,9 +13,15 @@ extern std::atomic<long long> g_launches;
 void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int linkcells, cudaStream_t s);
 // classic: NLIST with a fixed-point frame in every frame (k_nl_search);
 // otherwise NLISTCELLS or a generic box (k_nl_search_cells)
-// dst[i] = src[i] for i < n; src may be any address the device can read
-// (a pageable host array when the device uses the host page tables)
-void launch_copy_in(const double *src, double *dst, size_t n, cudaStream_t s);
+// dst[i] = src[i] for i < n, coalesced; either side may be any address the
+// device can access (a pageable host array when the device uses the host
+// page tables)
+void launch_copy(const double *src, double *dst, size_t n, cudaStream_t s);
+// host-array calls: fixed-point positions from the caller's array straight
+// to rank order; derivatives from the accumulators straight to the caller's
+// array (mixed path)
+void launch_prep_host(const KArgs &a, const double *hpos, int rank_order, cudaStream_t s);
+void launch_finalize_host32(const KArgs &a, double *hderiv, int rank_order, cudaStream_t s);
 void launch_nl_build(const KArgs &a, bool classic, cudaStream_t s);
 void launch_pair_flags(const KArgs &a, cudaStream_t s);
 void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s);

@@ -16,10 +16,15 @@ torch = pytest.importorskip("torch")
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_direct_and_staged_host_paths_agree(prec):
+@pytest.mark.parametrize("nlist", [True, False])
+def test_direct_and_staged_host_paths_agree(prec, nlist):
+    """Step 0 rebuilds the list (positions copied to the device); step 1 does
+    not (mixed path: positions and derivatives move in one pass each)."""
     from plumed2_gb300.action import Coordination
     n, L = 2000, 13 * 0.31
-    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=10" % n
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9}" % n
+    if nlist:
+        line += " NLIST NL_CUTOFF=1.0 NL_STRIDE=10"
     pos = jittered_lattice(n, 0.31, 0.03, 70)
     box = np.diag([L] * 3)
     res = {}
