@@ -270,29 +270,28 @@ def run_ours(args):
     torch.cuda.synchronize()
 
     step = 0
-    # a metadynamics-style bias V(s) = sum_k h exp(-(s - s_k)^2 / (2 sigma^2)) per walker: 500 hills,
+    # a metadynamics bias per walker: 500 METAD hills (truncated, stretched Gaussians, coord_bias_hills),
     # h = 1.2, sigma = 0.05 s0, centres uniform in [0.8 s0, 1.2 s0], s0 = the walker's first CV
     c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), 0, 0, step=0, flags=_lib.FLAG_NO_DERIV)
     torch.cuda.synchronize()
     s0 = s.clone()
     gen = torch.Generator(device="cpu").manual_seed(7)
     centres = (s0.cpu()[:, None] * (0.8 + 0.4 * torch.rand(W, 500, generator=gen, dtype=torch.float64))).to(dev)
-    sig2 = (0.05 * s0[:, None]) ** 2
+    sigmas = (0.05 * s0[:, None]).expand(W, 500).contiguous()
+    heights = torch.full((W, 500), 1.2, dtype=torch.float64, device=dev)
     g = torch.zeros(W, dtype=torch.float64, device=dev)
     gpos = torch.zeros(W, n, 3, dtype=torch.float64, device=dev)
     gbox = torch.zeros(W, 9, dtype=torch.float64, device=dev)
     energy = torch.zeros(W, dtype=torch.float64, device=dev)
 
     def one_step(ctx):
-        """CV (derivatives and virial kept for backward) -> bias energy and dV/ds -> backward kernel: forces and
-        the box gradient (what a metadynamics step needs)."""
+        """CV (derivatives and virial kept for backward) -> METAD hills bias energy and dV/ds on the device ->
+        backward kernel: forces and the box gradient (what a metadynamics step needs)."""
         nonlocal step
         ctx.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), 0, vir.data_ptr(), step=step,
                            flags=_lib.FLAG_SAVE)
-        diff = s[:, None] - centres
-        e = 1.2 * torch.exp(-diff * diff / (2 * sig2))
-        energy.copy_(e.sum(1))
-        g.copy_((e * (-diff / sig2)).sum(1))
+        _lib.bias_hills(W, s.data_ptr(), 500, centres.data_ptr(), sigmas.data_ptr(), heights.data_ptr(),
+                        energy.data_ptr(), g.data_ptr())
         ctx.backward_device(tpos.data_ptr(), boxes, W, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(), 0)
         step += 1
 
@@ -442,8 +441,8 @@ def run_ours(args):
                        "fp64_gpu_ms_per_step": t64 * 1e3,
                        "rebuild_step_ms": t_rebuild_step * 1e3,
                        "mixed_over_fp64_speedup_cv_force": t64 / t_plain_step,
-                       "step": "CV with saved derivatives and virial + 500-hill bias + backward kernel (forces "
-                               "and box gradient) for all walkers; NL rebuilt every 10th step",
+                       "step": "CV with saved derivatives and virial + 500-hill METAD bias (device kernel) + "
+                               "backward kernel (forces and box gradient) for all walkers; NL rebuilt every 10th step",
                        "cv_force_pass_ms": t_plain_step * 1e3, "autotune": c.autotune(),
                        "backward": True, "l2": "working set (0.8 GB) larger than the 129 MB L2",
                        "parallelism": "walkers sharded across GPUs, no collective"},

@@ -202,6 +202,22 @@ int coord_forward_noalloc(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, c
 int coord_autotune(coord_ctx *ctx, char *desc, size_t desclen);
 /* Microbenchmarks of the device (FP32 FMA, FP64 FMA TFLOP/s, HBM copy GB/s). */
 int coord_measure_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *hbm_gbs);
+/* ---- biases on the CV, on the device ------------------------------------- */
+/* Sum of truncated Gaussian hills of a one-dimensional CV for every frame:
+ * the non-multivariate hills of METAD (MetaD::evaluateGaussianAndDerivatives,
+ * src/bias/MetaD.cpp:2148-2181,2256-2273; cutoff dp2 < 6.25 and the stretch
+ * of src/tools/Tools.h:71-74, on when stretch != 0).  Device arrays: s
+ * [n_frames]; centers, sigmas, heights [n_frames][n_hills]; V, dVds
+ * [n_frames] (either may be NULL), overwritten or, with accumulate != 0,
+ * added to.  Runs on `stream` (NULL: the legacy default stream). */
+int coord_bias_hills(int n_frames, const double *s, int n_hills, const double *centers, const double *sigmas,
+                     const double *heights, int stretch, int accumulate, double *V, double *dVds, void *stream);
+/* RESTRAINT on one argument (Restraint::calculate, src/bias/Restraint.cpp:
+ * 125-141): V = kappa/2 (s-at)^2 + slope (s-at), dV/ds = kappa (s-at) + slope
+ * for every frame; same array conventions as coord_bias_hills. */
+int coord_bias_restraint(int n_frames, const double *s, double at, double kappa, double slope, int accumulate,
+                         double *V, double *dVds, void *stream);
+
 /* Whether the device reads and writes pageable host memory coherently
  * (cudaDevAttrPageableMemoryAccess) and does so through the host's page
  * tables without migrating pages (cudaDevAttrPageableMemoryAccessUsesHostPageTables,

@@ -100,6 +100,8 @@ def load() -> C.CDLL:
         L.coord_set_timing.argtypes = [_vp, C.c_int]
         L.coord_kernel_times.argtypes = [_vp, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
         L.coord_host_memory_access.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.coord_bias_hills.argtypes = [C.c_int, _vp, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp]
+        L.coord_bias_restraint.argtypes = [C.c_int, _vp, C.c_double, C.c_double, C.c_double, C.c_int, _vp, _vp, _vp]
         L.coord_forward_noalloc.argtypes = [_vp, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_int64), C.c_int64,
                                             _vp, _dp, _vp, _vp, _vp, _vp]
         _lib = L
@@ -139,3 +141,24 @@ def host_memory_access(device: int = 0):
     a, b = C.c_int(), C.c_int()
     load().coord_host_memory_access(device, C.byref(a), C.byref(b))
     return bool(a.value), bool(b.value)
+
+
+def bias_hills(n_frames: int, s_ptr: int, n_hills: int, centers_ptr: int, sigmas_ptr: int, heights_ptr: int,
+               V_ptr: int = 0, dVds_ptr: int = 0, stretch: bool = True, accumulate: bool = False, stream: int = 0):
+    """Truncated Gaussian hills on the device (coord_bias_hills); pointers are device addresses."""
+    rc = load().coord_bias_hills(int(n_frames), C.c_void_p(s_ptr), int(n_hills), C.c_void_p(centers_ptr),
+                                 C.c_void_p(sigmas_ptr), C.c_void_p(heights_ptr), int(bool(stretch)),
+                                 int(bool(accumulate)), C.c_void_p(V_ptr or None), C.c_void_p(dVds_ptr or None),
+                                 C.c_void_p(stream or None))
+    if rc:
+        raise CoordError(rc, "coord_bias_hills")
+
+
+def bias_restraint(n_frames: int, s_ptr: int, at: float, kappa: float, slope: float = 0.0, V_ptr: int = 0,
+                   dVds_ptr: int = 0, accumulate: bool = False, stream: int = 0):
+    """RESTRAINT on the device (coord_bias_restraint); pointers are device addresses."""
+    rc = load().coord_bias_restraint(int(n_frames), C.c_void_p(s_ptr), float(at), float(kappa), float(slope),
+                                     int(bool(accumulate)), C.c_void_p(V_ptr or None), C.c_void_p(dVds_ptr or None),
+                                     C.c_void_p(stream or None))
+    if rc:
+        raise CoordError(rc, "coord_bias_restraint")

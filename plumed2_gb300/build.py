@@ -29,6 +29,7 @@ SOURCES = {
     "multi.cu": [],
     "peaks.cu": [],
     "noalloc.cu": ["-fmad=false"],
+    "bias.cu": ["-fmad=false"],
     "host_setup.cpp": [],
 }
 HEADERS = ["coord_internal.h", "switch_eval.cuh", "kargs.h", "kernels.cuh", "eval.cuh", "launch.h"]
