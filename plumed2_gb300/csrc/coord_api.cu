@@ -96,7 +96,9 @@ struct coord_ctx {
   DevBuf<unsigned char> pair_flag;
   DevBuf<double> acc64, partials;
   DevBuf<float4> acc32;
-  DevBuf<unsigned> tickets;
+  DevBuf<unsigned> tickets, band_tickets;
+  DevBuf<unsigned char> band_flag;
+  DevBuf<double> band_rec;
   // host-API staging
   DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam, d_bvir, d_bpar;
   // saved forward (COORD_FLAG_SAVE)
@@ -243,6 +245,9 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->nl_count, F * 4);
   ENS(c->mm, F * 6);
   ENS(c->tickets, F);
+  ENS(c->band_tickets, F);
+  ENS(c->band_flag, F * (size_t)((nslices + 31) & ~31) + 32);
+  ENS(c->band_rec, F * std::max(nslices, 1) * kPartials);
   ENS(c->cell_count, F * (size_t)c->ncell_cap);
   ENS(c->cell_fill, F * (size_t)c->ncell_cap);
   ENS(c->cell_start, F * ((size_t)c->ncell_cap + 1));
@@ -299,6 +304,9 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.max_blocks = c->max_blocks;
   a.cells_launch = c->cells_launch > 0 ? c->cells_launch : c->ncell_cap;
   a.tickets = c->tickets.p;
+  a.band_flag = c->band_flag.p;
+  a.band_rec = c->band_rec.p;
+  a.band_tickets = c->band_tickets.p;
   a.out_s = s;
   a.out_deriv = deriv;
   a.out_virial = virial;
@@ -435,6 +443,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
       const int m = std::min(std::max(mode, 0), 2);
       const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
       launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
+      launch_band_fix(a, c->sw, c->s32, mode, c->stream);
     } else {
       launch_eval_nl64(a, c->sw, mode, c->stream);
     }
@@ -580,6 +589,9 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   double *const k_dparam = save ? c->sv_par.p : dparam;
   KArgs a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
   a.keep_acc = save ? 1 : 0;
+  // fused host steps leave the device copy stale: the pair kernels' rare
+  // exact d_max tests read the caller's array itself
+  if (hio && hio->fused) a.pos = hio->pos;
   cudaError_t e;
   if (rebuild) cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
   if (need_bounds && (mixed || rebuild)) {
@@ -779,6 +791,12 @@ int coord_create(const coord_params *p, coord_ctx **out) {
   {
     const SwitchParams &s = c->sw;
     c->s32.dmax2 = (s.dmax_2 >= 3.0e38) ? INFINITY : (float)s.dmax_2;
+    // FP32 r^2 from fixed-point deltas is within ~4e-7 relative of the FP64
+    // value (conversion, scale and three roundings) plus quantisation; 2e-6
+    // leaves a margin of five
+    c->s32.dmax2_lo = (s.dmax_2 >= 3.0e38) ? INFINITY : (float)(s.dmax_2 * (1.0 - 2e-6));
+    c->s32.dmax2_hi = (s.dmax_2 >= 3.0e38) ? INFINITY : (float)(s.dmax_2 * (1.0 + 2e-6));
+    c->s32.dmax_2 = s.dmax_2;
     c->s32.invr0_2 = (float)s.invr0_2;
     c->s32.stretch = (float)s.stretch;
     c->s32.shift = (float)s.shift;
@@ -823,6 +841,9 @@ int coord_destroy(coord_ctx *c) {
   c->partials.release();
   c->acc32.release();
   c->tickets.release();
+  c->band_tickets.release();
+  c->band_flag.release();
+  c->band_rec.release();
   c->d_pos.release();
   c->d_s.release();
   c->d_deriv.release();

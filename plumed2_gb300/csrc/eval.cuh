@@ -143,6 +143,30 @@ struct Acc32 {
   }
 };
 
+// The reference's inclusive d_max test, r^2 = modulo2(pbc.distance(x1, x2))
+// <= d_max^2 in FP64 (CoordinationBase.cpp:187-190, SwitchingFunction.cpp:
+// 206), for the rare pair whose FP32 r^2 falls in the band around d_max^2
+// (a stretched switch is zero at d_max but its derivative is not, so the
+// decision must match).  x1 is the reference's first atom; every operation is
+// an explicitly rounded intrinsic, so no contraction changes the result.
+// Orthorhombic box or none (the mixed path's frames).
+__device__ __forceinline__ bool dmax_exact(const double *x1, const double *x2, const PbcParams *pbc, int do_pbc,
+                                        double dmax_2) {
+  double d[3];
+  for (int k = 0; k < 3; k++) d[k] = __dsub_rn(x2[k], x1[k]);
+  if (do_pbc && pbc->type == PBC_ORTHO) {
+    for (int k = 0; k < 3; k++) {
+      // Tools::pbc (Tools.h:557-563) of d * invBox(k,k), times box(k,k)
+      double x = __dadd_rn(__dmul_rn(d[k], pbc->invbox[4 * k]), 100.0);
+      const double t = (x >= 0) ? (double)__double2int_rz(__dadd_rn(x, 0.5))
+                                : (double)__double2int_rz(__dsub_rn(x, 0.5));
+      d[k] = __dmul_rn(__dsub_rn(x, t), pbc->box[4 * k]);
+    }
+  }
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+  return r2 <= dmax_2;
+}
+
 // Asks the TMA engine to bring [p, p + bytes) into L2 (no registers, no
 // completion to wait for); p 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) {
@@ -154,6 +178,9 @@ __device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z)
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z), "f"(0.f)
                : "memory");
 }
+
+// Bytes per frame of band_flag: slices rounded up to 32 (16-byte vector loads).
+__device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)a.nslices + 31) & ~(size_t)31; }
 
 // Persistent warps: warp w of the frame's grid takes slices w, w + nw, ...;
 // the per-thread accumulators carry across slices and one block reduction
@@ -200,6 +227,31 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
     const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
     float ax = 0.f, ay = 0.f, az = 0.f;
     const uint32_t *__restrict__ e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    // one pair inside d_max: s, the two derivatives (d = x_p - x_r:
+    // deriv[r] -= df d, deriv[p] += df d, either orientation), the virial
+    auto pair = [&](int p, float dx, float dy, float dz, float r2) {
+      float sig, df;
+      sw32<NH>(sw, s32, r2, sig, df);
+      acc.add_s(sig);
+      if (MODE >= EVAL_DERIV) {
+        const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+        ax -= ddx;
+        ay -= ddy;
+        az -= ddz;
+        red_add_v4(acc4 + p, ddx, ddy, ddz);
+        acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+      }
+      if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
+    };
+    // pairs whose FP32 r^2 lies in (dmax2_lo, dmax2_hi] cannot decide the
+    // reference's inclusive test r^2 <= d_max^2: they are left to the FP64
+    // fix-up pass (k_band_fix).  bits(r^2) - bits(lo) - 1 is below the band
+    // width exactly for them (r^2 >= 0 orders like its bits; pairs below lo
+    // and dead entries, r^2 = 0, wrap to large values), so one unsigned min
+    // per pair finds them.
+    const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
+    const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
+    uint32_t band_min = 0xffffffffu;
     for (int k = 0; k < w; k += kUnroll) {
       int p[kUnroll];
       uint4 qp[kUnroll];
@@ -213,28 +265,152 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
         const float dy = fixed_delta(qr.y, qp[u].y, sy);
         const float dz = fixed_delta(qr.z, qp[u].z, sz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (p[u] >= 0 && r2 <= s32.dmax2) {
-          float sig, df;
-          sw32<NH>(sw, s32, r2, sig, df);
-          acc.add_s(sig);
-          if (MODE >= EVAL_DERIV) {
-            // d = x_p - x_r: deriv[r] -= df d, deriv[p] += df d (either orientation)
-            const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
-            ax -= ddx;
-            ay -= ddy;
-            az -= ddz;
-            red_add_v4(acc4 + p[u], ddx, ddy, ddz);
-            acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
-          }
-          if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
-        }
+        if (p[u] >= 0 && r2 <= s32.dmax2_lo)
+          pair(p[u], dx, dy, dz, r2);
+        else
+          band_min = min(band_min, __float_as_uint(r2) - band_lo);
       }
     }
+    if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az);
   }
   double part[kPartials];
   acc.to_partials(part);
   block_partials_finish(a, f, part, gridDim.x);
+}
+
+// FP64 fix-up of the mixed NL pass: the slices flagged by k_eval_nl32 scan
+// their rows again; every pair whose FP32 r^2 lies in the band around
+// d_max^2 takes the reference's own FP64 test (dmax_exact, in the pair's
+// orientation) and, if kept, is evaluated at d_max^2 (both sides of the FP32
+// rounding agree there): partner and row derivatives by vector reductions
+// (before the finalize kernel), s / virial / parameter sums into the slice's
+// record.  The frame's last block adds the records of the flagged slices in
+// slice order to the frame's results and clears the flags, so the outcome
+// does not depend on timing.  With no flagged slice this is a scan of one
+// byte per slice.
+template <int NH, int MODE>
+__global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
+  const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const uint4 *__restrict__ q = a.q + fo;
+  float4 *__restrict__ acc4 = a.acc32 + fo;
+  unsigned char *flag = a.band_flag + (size_t)f * band_stride(a);
+  const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
+  const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
+  // each warp takes 32 consecutive slices: one coalesced load of their flags
+  for (int chunk = blockIdx.x * nwarps + warp; chunk * 32 < a.nslices; chunk += gridDim.x * nwarps) {
+    const int s_l = chunk * 32 + lane;
+    unsigned todo = __ballot_sync(0xffffffffu, s_l < a.nslices && flag[s_l] != 0);
+    while (todo) {
+    const int slice = chunk * 32 + __ffs(todo) - 1;
+    todo &= todo - 1u;
+    const int r = slice * 32 + lane;
+    const bool active = r < a.ns;
+    const int len = active ? a.row_len[fo + r] : 0;
+    const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t *e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    Acc32 acc;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    constexpr int kU = 8;  // entries and partner positions in flight per lane
+    for (int k0 = 0; k0 < len; k0 += kU) {
+      uint32_t en[kU];
+      uint4 qq[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) en[u] = (k0 + u < len) ? e[(size_t)(k0 + u) * 32] : 0xffffffffu;
+#pragma unroll
+      for (int u = 0; u < kU; u++) qq[u] = (en[u] != 0xffffffffu) ? q[en[u] & kRankMask] : qr;
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const float dx = fixed_delta(qr.x, qq[u].x, sx), dy = fixed_delta(qr.y, qq[u].y, sy),
+                    dz = fixed_delta(qr.z, qq[u].z, sz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if ((__float_as_uint(r2) - band_lo) >= band_w) continue;  // dead entries: r2 = 0, never in the band
+        const int p = (int)(en[u] & kRankMask);
+        const double *xr = a.pos + (fo + a.slot_of_rank[fo + r]) * 3;
+        const double *xp = a.pos + (fo + a.slot_of_rank[fo + p]) * 3;
+        const bool in = (en[u] & kOrientBit) ? dmax_exact(xr, xp, &fc.pbc, a.do_pbc, s32.dmax_2)
+                                             : dmax_exact(xp, xr, &fc.pbc, a.do_pbc, s32.dmax_2);
+        if (!in) continue;
+        float sig, df;
+        sw32<NH>(sw, s32, s32.dmax2, sig, df);
+        acc.add_s(sig);
+        if (MODE >= EVAL_DERIV) {
+          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+          ax -= ddx;
+          ay -= ddy;
+          az -= ddz;
+          red_add_v4(acc4 + p, ddx, ddy, ddz);
+          acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+        }
+        if (MODE == EVAL_PARAM) acc.add_param(s32, s32.dmax2, sig, df);
+      }
+    }
+    if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f)) red_add_v4(acc4 + r, ax, ay, az);
+    double part[kPartials];
+    acc.to_partials(part);
+    double *rec = a.band_rec + ((size_t)f * a.nslices + slice) * kPartials;
+#pragma unroll
+    for (int k = 0; k < kPartials; k++) {
+      const double v = warp_sum(part[k]);  // fixed shuffle tree
+      if (lane == 0) rec[k] = v;
+    }
+    }
+  }
+  // the frame's last block: records of the flagged slices, in slice order
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(&a.band_tickets[f], 1u) == gridDim.x - 1u;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  // thread t: slices [32 t', 32 t' + 32) for t' = t, t + 256, ... in order,
+  // their flags as two 16-byte loads
+  double v[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) v[k] = 0.0;
+  bool any = false;
+  for (int c0 = threadIdx.x * 32; c0 < a.nslices; c0 += blockDim.x * 32) {
+    uint4 *fv = reinterpret_cast<uint4 *>(flag + c0);
+    const uint4 f0 = __ldcg(fv), f1 = __ldcg(fv + 1);
+    if ((f0.x | f0.y | f0.z | f0.w | f1.x | f1.y | f1.z | f1.w) == 0u) continue;
+    any = true;
+    for (int sl = c0; sl < min(c0 + 32, a.nslices); sl++) {
+      if (!flag[sl]) continue;
+      const double *rec = a.band_rec + ((size_t)f * a.nslices + sl) * kPartials;
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) v[k] += __ldcg(rec + k);
+    }
+    fv[0] = make_uint4(0u, 0u, 0u, 0u);
+    fv[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __shared__ double red[kPartials][256];
+  __shared__ int any_block;
+  if (threadIdx.x == 0) any_block = 0;
+  __syncthreads();
+  if (any) atomicOr(&any_block, 1);
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) red[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int k = 0; k < kPartials; k++) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    a.band_tickets[f] = 0u;
+    if (any_block) {
+      if (a.out_s) a.out_s[f] += red[0][0];
+      if (a.out_virial)
+        for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += red[1 + k][0];
+      if (a.out_dparam)
+        for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += red[10 + k][0];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -370,9 +546,12 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
         const float dx = fixed_delta(qi.x, qp.x, sx), dy = fixed_delta(qi.y, qp.y, sy),
                     dz = fixed_delta(qi.z, qp.z, sz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 <= s32.dmax2) {
+        bool in = r2 <= s32.dmax2_lo;
+        if (!in && r2 <= s32.dmax2_hi)  // band: slot i is the reference's first atom
+          in = dmax_exact(a.pos + (fo + i) * 3, a.pos + (fo + j) * 3, &fc.pbc, a.do_pbc, s32.dmax_2);
+        if (in) {
           float sig, df;
-          sw32<NH>(sw, s32, r2, sig, df);
+          sw32<NH>(sw, s32, fminf(r2, s32.dmax2), sig, df);
           acc.add_s(sig);
           if (MODE >= EVAL_DERIV) {
             const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
@@ -384,7 +563,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
             atomicAdd(&accj[jl][2], ddz);
             acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
           }
-          if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
+          if (MODE == EVAL_PARAM) acc.add_param(s32, fminf(r2, s32.dmax2), sig, df);
         }
       }
       if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f))
@@ -443,9 +622,12 @@ template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, 
     const float dx = fixed_delta(q0.x, q1.x, fc.scale[0]), dy = fixed_delta(q0.y, q1.y, fc.scale[1]),
                 dz = fixed_delta(q0.z, q1.z, fc.scale[2]);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 <= s32.dmax2) {
+    bool in = r2 <= s32.dmax2_lo;
+    if (!in && r2 <= s32.dmax2_hi)  // band: pair i is (slot i, slot i+nA) in the reference's orientation
+      in = dmax_exact(a.pos + (fo + i) * 3, a.pos + (fo + i + a.nA) * 3, &fc.pbc, a.do_pbc, s32.dmax_2);
+    if (in) {
       float sig, df;
-      sw32<NH>(sw, s32, r2, sig, df);
+      sw32<NH>(sw, s32, fminf(r2, s32.dmax2), sig, df);
       acc.add_s(sig);
       if (MODE >= EVAL_DERIV) {
         const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
@@ -458,7 +640,7 @@ template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, 
         a1.z += ddz;
         acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
       }
-      if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
+      if (MODE == EVAL_PARAM) acc.add_param(s32, fminf(r2, s32.dmax2), sig, df);
     }
   }
   double part[kPartials];

@@ -65,6 +65,16 @@ void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s
   g_launches += 1;
 }
 
+void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s) {
+  if (!(s32.dmax2_lo < s32.dmax2_hi)) return;  // no d_max: nothing to decide
+  const int chunks = (a.nslices + 31) / 32;  // one warp per 32 slices
+  const dim3 g(std::max(1, std::min((chunks + 7) / 8, 64)), a.nframes);
+#define CALL(N, M) k_band_fix<N, M><<<g, 256, 0, s>>>(a, sw, s32)
+  NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
+#undef CALL
+  g_launches += 1;
+}
+
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s) {
   const bool tri = a.mode == MODE_SINGLE;

@@ -49,6 +49,11 @@ struct KArgs {
   int max_blocks;
   int cells_launch;             // blocks of the per-cell sort (cells per frame, when known)
   unsigned *tickets;            // [nframes]
+  // mixed NL pass: slices holding a pair whose FP32 r^2 lies in the band
+  // around d_max^2, for the FP64 fix-up pass (k_band_fix)
+  unsigned char *band_flag;     // [nframes][nslices]
+  double *band_rec;             // [nframes][nslices][kPartials] per flagged slice
+  unsigned *band_tickets;       // [nframes]
   double *out_s;                // [nframes]
   double *out_deriv;            // [nframes][ns][3] slot order
   double *out_virial;           // [nframes][9]
@@ -61,6 +66,10 @@ struct KArgs {
 struct SwitchF32 {
   float dmax2, invr0_2, stretch, shift, c;  // c = -NH * 2*invr0^2 * stretch
   float d0, invr0, c_r0, c_d0;
+  // band around d_max^2 inside which the FP32 r^2 cannot decide the
+  // reference's inclusive test r^2 <= d_max^2: such pairs are decided in FP64
+  float dmax2_lo, dmax2_hi;
+  double dmax_2;  // the reference's d_max^2 (FP64)
 };
 
 // What a pair kernel accumulates.

@@ -33,6 +33,9 @@ void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, dou
                       cudaStream_t s);
 
 // k_mixed.cu
+// FP64 decision of d_max for the pairs the mixed NL pass left in the band
+// around d_max^2 (after launch_eval_nl32, before the finalize kernel)
+void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s);
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
                       int unroll, cudaStream_t s);
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,

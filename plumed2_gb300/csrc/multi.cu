@@ -122,9 +122,13 @@ __global__ void __launch_bounds__(TILE) k_multi_pairs(MultiArgs m, SwitchParams 
         const float dx = fixed_delta(qi.x, qp.x, sx), dy = fixed_delta(qi.y, qp.y, sy),
                     dz = fixed_delta(qi.z, qp.z, sz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 <= s32.dmax2) {
+        bool in = r2 <= s32.dmax2_lo;
+        if (!in && r2 <= s32.dmax2_hi)  // band: the reference's FP64 test, slot i first
+          in = dmax_exact(m.pos + ((size_t)f * m.n_atoms + ai) * 3, m.pos + ((size_t)f * m.n_atoms + atj[jl]) * 3,
+                          &fc.pbc, 1, s32.dmax_2);
+        if (in) {
           float sig, df;
-          sw32<NH>(sw_generic, s32, r2, sig, df);
+          sw32<NH>(sw_generic, s32, fminf(r2, s32.dmax2), sig, df);
           acc.add_s(sig);
           const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
           ax -= ddx;
