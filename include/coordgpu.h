@@ -148,6 +148,18 @@ int coord_forward_device(coord_ctx *ctx, int n_frames, const double *pos, const 
 int coord_backward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, const double *g,
                           double *grad_pos, double *grad_box, double *grad_param, void *stream);
 
+/* Force application on the device (Colvar::apply, src/core/Colvar.cpp:50-60;
+ * ActionWithValue::checkForForces, src/core/ActionWithValue.cpp:337-411;
+ * ActionAtomistic::setForcesOnAtoms/setForcesOnCell, ActionAtomistic.cpp:
+ * 502-549) after a forward with COORD_FLAG_SAVE on the same frames: for every
+ * frame f and slot i, atom_forces[f][abs(i)][0..2] += ff[f] * ds/dx_i, and
+ * box_forces[f][0..8] += ff[f] * virial[f] (either output may be NULL).
+ * ff[f] is the force on the CV (-dV/ds); atom_forces is the engine's
+ * [n_frames][n_atoms][3] device array, indexed by the absolute atom indices
+ * of coord_set_groups.  Device arrays; consumes the saved state. */
+int coord_apply_forces(coord_ctx *ctx, int n_frames, const double *ff, int64_t n_atoms, double *atom_forces,
+                       double *box_forces, void *stream);
+
 /* ---- neighbour list introspection ------------------------------------------ */
 /* nl->size() of the last build for frame f (pairs processed per step,
  * CoordinationBase.cpp:163), including pairs skipped as self pairs. */

@@ -229,6 +229,17 @@ class Coordination:
                                            C.c_void_p(stream or None))
         check(self._L, self._ctx, rc)
 
+    def apply_forces(self, n_frames: int, ff_ptr: int, n_atoms: int, atom_forces_ptr: int = 0, box_forces_ptr: int = 0,
+                     stream: int = 0):
+        """coord_apply_forces: ff (force on the CV, -dV/ds, per frame) times the saved ds/dx added into the
+        engine's [n_frames][n_atoms][3] force array by absolute index, and times the virial into the box
+        force (device pointers)."""
+        self._ensure_groups()
+        rc = self._L.coord_apply_forces(self._ctx, int(n_frames), C.c_void_p(ff_ptr), int(n_atoms),
+                                        C.c_void_p(atom_forces_ptr or None), C.c_void_p(box_forces_ptr or None),
+                                        C.c_void_p(stream or None))
+        check(self._L, self._ctx, rc)
+
     # -- neighbour list ------------------------------------------------------
     def nl_size(self, frame: int = 0) -> int:
         n = C.c_int64()

@@ -1180,6 +1180,28 @@ int coord_last_kernel_ms(coord_ctx *c, double *ms, int *count) {
   return COORD_OK;
 }
 
+int coord_apply_forces(coord_ctx *c, int n_frames, const double *ff, int64_t n_atoms, double *atom_forces,
+                       double *box_forces, void *stream) {
+  if (!c) return COORD_ERR_ARG;
+  if (!ff || n_frames < 1 || n_atoms < 0) return c->fail(COORD_ERR_ARG, "null force or bad sizes");
+  if (!c->saved_valid || !c->acc_kept || c->saved_frames != n_frames)
+    return c->fail(COORD_ERR_STATE, "coord_apply_forces needs a forward with COORD_FLAG_SAVE on the same frames");
+  for (int64_t v : c->abs_host)
+    if (v >= n_atoms) return c->fail(COORD_ERR_ARG, "an atom index of the groups is beyond n_atoms");
+  cudaSetDevice(c->p.device);
+  DefaultStreamFence fence(c, stream);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  KArgs a = make_args(c, n_frames, nullptr, 0, nullptr, nullptr, nullptr, nullptr);
+  const bool nl_order = c->p.nlist != COORD_NL_NONE && c->mode != MODE_PAIR;
+  launch_apply_forces(a, c->p.precision == COORD_PREC_MIXED, nl_order ? 1 : 0, ff, (long long)n_atoms, atom_forces,
+                      c->sv_vir.p, box_forces, st);
+  c->acc_kept = false;
+  c->saved_valid = false;
+  cudaError_t e;
+  if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "force application");
+  return COORD_OK;
+}
+
 int coord_host_memory_access(int device, int *pageable, int *host_page_tables) {
   int a = 0, b = 0;
   if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) a = 0;

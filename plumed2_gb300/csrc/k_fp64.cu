@@ -61,6 +61,21 @@ void launch_copy(const double *src, double *dst, size_t n, cudaStream_t s) {
   g_launches += 1;
 }
 
+void launch_apply_forces(const KArgs &a, bool mixed, int rank_order, const double *ff, long long n_atoms,
+                         double *atom_forces, const double *vir, double *box_forces, cudaStream_t s) {
+  if (atom_forces && a.ns > 0) {
+    if (mixed)
+      k_apply_forces<float4><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order, ff, n_atoms, atom_forces);
+    else
+      k_apply_forces<double><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, rank_order, ff, n_atoms, atom_forces);
+    g_launches += 1;
+  }
+  if (box_forces) {
+    k_apply_box_forces<<<(a.nframes * 9 + 127) / 128, 128, 0, s>>>(a.nframes, ff, vir, box_forces);
+    g_launches += 1;
+  }
+}
+
 void launch_pair_flags(const KArgs &a, cudaStream_t s) {
   k_pair_flags<<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a);
   g_launches += 1;

@@ -391,6 +391,46 @@ __global__ void k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank
   if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Force application from a saved forward (Colvar::apply, core/Colvar.cpp:50-60,
+// with the daxpy of ActionWithValue::checkForForces, ActionWithValue.cpp:
+// 337-411, and ActionAtomistic::setForcesOnAtoms, ActionAtomistic.cpp:502-541):
+// atom_forces[frame][abs(slot)] += ff[frame] * ds/dx(slot), taken straight
+// from the kept accumulators (rank order through rank_of_slot), which are
+// cleared; atomics only when an absolute index occupies two slots.
+template <typename Acc>
+__global__ void k_apply_forces(KArgs a, int rank_order, const double *__restrict__ ff, long long n_atoms,
+                               double *__restrict__ atom_forces) {
+  const int f = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.ns) return;
+  const size_t fo = (size_t)f * a.ns;
+  const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+  double v[3];
+  if constexpr (sizeof(Acc) == sizeof(float4)) {
+    float4 *acc = reinterpret_cast<float4 *>(a.acc32) + fo + r;
+    const float4 x = *acc;
+    v[0] = x.x, v[1] = x.y, v[2] = x.z;
+    *acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  } else {
+    double *acc = a.acc64 + (fo + r) * 3;
+    v[0] = acc[0], v[1] = acc[1], v[2] = acc[2];
+    acc[0] = acc[1] = acc[2] = 0.0;
+  }
+  const double g = ff[f];
+  double *o = atom_forces + ((size_t)f * n_atoms + a.abs_of_slot[s]) * 3;
+  if (a.has_dup) {
+    for (int k = 0; k < 3; k++) atomicAdd(o + k, g * v[k]);
+  } else {
+    for (int k = 0; k < 3; k++) o[k] += g * v[k];
+  }
+}
+__global__ void k_apply_box_forces(int nframes, const double *__restrict__ ff, const double *__restrict__ vir,
+                                   double *__restrict__ box_forces) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nframes * 9) return;
+  box_forces[i] += ff[i / 9] * vir[i];
+}
+
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter
 // and the mixed kernels).  rank_order==0: slot order.
 __global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {

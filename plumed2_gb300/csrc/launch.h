@@ -17,6 +17,9 @@ void launch_bounds(const KArgs &a, unsigned long long *mm, double cutoff, int li
 // device can access (a pageable host array when the device uses the host
 // page tables)
 void launch_copy(const double *src, double *dst, size_t n, cudaStream_t s);
+// force application from a saved forward (k_apply_forces, k_apply_box_forces)
+void launch_apply_forces(const KArgs &a, bool mixed, int rank_order, const double *ff, long long n_atoms,
+                         double *atom_forces, const double *vir, double *box_forces, cudaStream_t s);
 // host-array calls: fixed-point positions from the caller's array straight
 // to rank order; derivatives from the accumulators straight to the caller's
 // array (mixed path)
