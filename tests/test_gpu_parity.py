@@ -276,3 +276,27 @@ def test_walkers_batched_device(orc):
             assert np.array_equal(_sorted(c.pairs(w)), pairs)
             ref = orc.coordination(spec, frames[w], box, pairs)
             _check(prec, (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy().reshape(3, 3)), ref, prec)
+
+
+def test_mixed_flat_slab_far_apart_ranks(orc):
+    """A flat periodic slab (99 x 20 x 3 cells, about 106k atoms): partners in
+    the neighbouring cell layer lie more than 32,767 ranks away, and two of
+    the three z cells wrap.  Pair set bit-exact, values within the mixed
+    tolerance, also on the step that reuses the list."""
+    from plumed2_gb300.action import Coordination
+    nx, ny, nz, a0 = 256, 52, 8, 0.31
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    sites = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1) * a0
+    pos = sites + np.random.default_rng(8).normal(0.0, 0.03, sites.shape)
+    box = np.diag([nx * a0, ny * a0, nz * a0])
+    n = len(pos)
+    spec = "RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6"
+    c = Coordination("GROUPA=1-%d SWITCH={%s} NLIST NL_CUTOFF=0.8 NL_STRIDE=10" % (n, spec), precision="mixed")
+    got = c.calculate(pos, box, 0)
+    pairs = orc.nl_classic_cells(0, n, 0, pos, box, True, 0.8)
+    assert np.array_equal(_sorted(c.pairs()), pairs)
+    ref = orc.coordination(spec, pos, box, pairs, nthreads=orc.max_threads())
+    _check("mixed", got, ref)
+    got = c.calculate(pos + 0.01, box, 1)  # the same list, without a rebuild
+    ref = orc.coordination(spec, pos + 0.01, box, pairs, nthreads=orc.max_threads())
+    _check("mixed", got, ref)
