@@ -574,6 +574,30 @@ __device__ __forceinline__ void nl_accept(const KArgs &a, const FrameConst &fc, 
   n++;
 }
 
+// bit i of v to bit 2i (i < 16)
+__device__ __forceinline__ uint32_t spread_even16(uint32_t v) {
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  return (v | (v << 1)) & 0x55555555u;
+}
+
+// Stores the accepted candidates of one staged batch (hit: bit j) in the
+// lane's row, in j order; every check that can drop a hit has been made.
+__device__ __forceinline__ int nl_store_row(const KArgs &a, uint32_t hit, int base, const uint4 *stage, int n, int sr,
+                                            bool ra, size_t slice_base) {
+  uint32_t *row = a.ell + slice_base;
+  const bool two = a.mode == MODE_TWO;
+  const int cap = a.cap;
+  for (; hit; hit &= hit - 1u) {
+    const int j = __ffs(hit) - 1;
+    const bool r_first = two ? ra : (sr < (int)stage[j].w);
+    if (n < cap) row[n * 32] = (uint32_t)(base + j) | (r_first ? kOrientBit : 0u);
+    n++;
+  }
+  return n;
+}
+
 // Classic lists with a fixed-point frame (orthorhombic box or no PBC).  The
 // slice's rows are processed one x-row of cells at a time; the candidates of a
 // row pass are the ranks of at most 9 row segments (ranks are cell-major, x
@@ -612,10 +636,11 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
         const int rb = start[rowcell + (it ? xa1 : xa0)], re = start[rowcell + (it ? xb1 : xb0) + 1];
         for (int base = rb; base < re; base += 32) {
           const int m = min(32, re - base);
+          int sp = 0;
           if (lane < m) {
             const int p = base + lane;
             const uint4 qp = a.q[fo + p];
-            const int sp = slot_of_rank[p];
+            sp = slot_of_rank[p];
             if (kRel)
               stage[lane] = make_uint4(__float_as_uint(fixed_delta(qref.x, qp.x, sx)),
                                        __float_as_uint(fixed_delta(qref.y, qp.y, sy)),
@@ -623,13 +648,14 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
             else
               stage[lane] = make_uint4(qp.x, qp.y, qp.z, (uint32_t)sp);
           }
+          // two lists: the batch's candidates of GROUPB (bit j)
+          const uint32_t in_b = __ballot_sync(0xffffffffu, lane < m && sp >= a.nA);
           __syncwarp();
+          // branch-free tests record the candidates within cut2_hi (hit) and
+          // those inside the band (band) as bits of j; the accepted ones are
+          // stored afterwards by the whole warp
+          uint32_t hit = 0u, band = 0u;
           if (mine) {
-            // branch-free tests record the candidates within cut2_hi (hit)
-            // and those inside the band (band) as bits of j; the accepted
-            // ones are handled afterwards, so the divergent accept path runs
-            // once per hit of the busiest lane rather than at every j
-            uint32_t hit = 0u, band = 0u;
             auto test = [&](int j) {
               const uint4 c = stage[j];
               float dx, dy, dz;
@@ -650,12 +676,37 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
               // the whole batch lies above r (owned when r + p is even) or
               // below it (owned when r + p is odd): every other candidate
               const int j0 = (r < base) ? ((r - base) & 1) : ((r - base + 1) & 1);
-              int j = j0;
-              for (; j + 2 < m; j += 4) {
-                test(j);
-                test(j + 2);
+              if (m == 32) {
+                // a full batch: 16 independent tests at j0 + 2i with
+                // compile-time bit positions, spread to bit j afterwards
+                uint32_t h16 = 0u, b16 = 0u;
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                  const uint4 c = stage[j0 + 2 * i];
+                  float dx, dy, dz;
+                  if (kRel) {
+                    dx = __uint_as_float(c.x) - mx;
+                    dy = __uint_as_float(c.y) - my;
+                    dz = __uint_as_float(c.z) - mz;
+                  } else {
+                    dx = fixed_delta(qr.x, c.x, sx);
+                    dy = fixed_delta(qr.y, c.y, sy);
+                    dz = fixed_delta(qr.z, c.z, sz);
+                  }
+                  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                  h16 |= (r2 <= hi2 ? 1u : 0u) << i;
+                  b16 |= (r2 < lo2 ? 0u : 1u) << i;
+                }
+                hit = spread_even16(h16) << j0;
+                band = (h16 & b16) ? spread_even16(h16 & b16) << j0 : 0u;
+              } else {
+                int j = j0;
+                for (; j + 2 < m; j += 4) {
+                  test(j);
+                  test(j + 2);
+                }
+                if (j < m) test(j);
               }
-              if (j < m) test(j);
             } else {
               for (int j = 0; j < m; j++) {
                 const int p = base + j;
@@ -663,12 +714,23 @@ __device__ __forceinline__ int nl_row_pass(const KArgs &a, const FrameConst &fc,
                 test(j);
               }
             }
-            while (hit) {
-              const int j = __ffs(hit) - 1;
-              hit &= hit - 1u;
-              nl_accept(a, fc, f, fo, r, sr, ra, base + j, (int)stage[j].w, (band >> j) & 1u, slice_base, n);
+            if (a.mode == MODE_TWO) hit &= ra ? in_b : ~in_b;
+            // hits inside the band: the reference's own FP64 test decides
+            for (uint32_t bh = hit & band; bh; bh &= bh - 1u) {
+              const int j = __ffs(bh) - 1;
+              const int p = base + j, sp_j = (int)stage[j].w;
+              const bool r_first = (a.mode == MODE_TWO) ? ra : (sr < sp_j);
+              if (!nl_exact(a.x64 + fo, &fc, a.do_pbc, r_first ? r : p, r_first ? p : r)) hit &= ~(1u << j);
+            }
+            if (a.has_dup) {
+              // duplicated atoms: self pairs are set aside one by one
+              for (; hit; hit &= hit - 1u) {
+                const int j = __ffs(hit) - 1;
+                nl_accept(a, fc, f, fo, r, sr, ra, base + j, (int)stage[j].w, false, slice_base, n);
+              }
             }
           }
+          if (hit) n = nl_store_row(a, hit, base, stage, n, sr, ra, slice_base);
           __syncwarp();
         }
       }
@@ -724,7 +786,7 @@ __device__ __forceinline__ void nl_slice_done(const KArgs &a, int f, int slice, 
 // Classic lists (NLIST) over frames with a fixed-point frame (orthorhombic
 // box or no PBC): one warp per slice of 32 ranks, one nl_row_pass per x-row of
 // cells that the slice's rows occupy (usually one).
-__global__ void __launch_bounds__(kSearchWarps * 32) k_nl_search(KArgs a) {
+__global__ void __launch_bounds__(kSearchWarps * 32, 8) k_nl_search(KArgs a) {
   const int f = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int slice = blockIdx.x * kSearchWarps + warp;
