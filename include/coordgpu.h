@@ -100,6 +100,37 @@ int coord_set_groups(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, const 
 /* Number of slots (n_a + n_b). */
 int coord_get_nslots(const coord_ctx *ctx, int64_t *nslots);
 
+/* ---- sibling CVs of CoordinationBase ---------------------------------------
+ * DHENERGY and GHBFIX run CoordinationBase::calculate's loop (groups, PAIR,
+ * NLIST/NLISTCELLS, NOPBC, derivatives and virial) with their own pairing()
+ * in place of the switching function.  A context becomes one of them through
+ * the calls below, after coord_create (whose switching-function keywords are
+ * then unused: give any valid set, e.g. r0 = 1).  FP64 precision only; the
+ * R_0/D_0 derivatives (COORD_FLAG_DR0, grad_param) are refused. */
+#define COORD_CV_COORDINATION 0
+#define COORD_CV_DHENERGY 1 /* colvar/DHEnergy.cpp:62 */
+#define COORD_CV_GHBFIX 2   /* colvar/GHBFIX.cpp:63   */
+
+/* DHENERGY keywords I, TEMP, EPSILON (DHEnergy.cpp:80-86) and the action's
+ * units (Units::getEnergy/getLength/getCharge; 1,1,1 for kJ/mol, nm, e).
+ * k = sqrt(I/(EPSILON*TEMP))*502.903741125*length and the prefactor
+ * 138.935458111/energy/length*charge^2 as DHEnergy.cpp:112-113; the pairing
+ * of DHEnergy.cpp:128-142.  Replaces DHEnergy::DHEnergy. */
+int coord_set_dhenergy(coord_ctx *ctx, double ionic_strength, double temp, double epsilon, double unit_energy,
+                       double unit_length, double unit_charge);
+/* DHENERGY's per-atom charges (Atoms::getCharge, in the action's charge
+ * unit), indexed by absolute atom index like the groups; n_atoms must cover
+ * every atom of the groups (checked at the next forward). */
+int coord_set_charges(coord_ctx *ctx, const double *charges, int64_t n_atoms);
+/* GHBFIX keywords D_0, D_MAX, C (GHBFIX.cpp:111-126) and its tables:
+ * types[a] = type id of absolute atom a (the TYPES file, ids in order of
+ * first appearance), eta = n_types x n_types scaling matrix (the PARAMS file,
+ * eta[n*t1+t2], already in the action's energy unit).  A group atom beyond
+ * n_atoms is an error at the next forward, with the message of
+ * GHBFIX.cpp:181-186.  Replaces GHBFIX::GHBFIX. */
+int coord_set_ghbfix(coord_ctx *ctx, double d0, double dmax, double c, const int32_t *types, int64_t n_atoms,
+                     const double *eta, int n_types);
+
 /* The context's switching function evaluated on the host:
  * SwitchingFunction::calculateSqr (squared != 0, x = r^2) or ::calculate
  * (x = r), SwitchingFunction.cpp:1163-1175.  f and df receive n values. */

@@ -62,6 +62,17 @@ class _Switch(C.Structure):
                 ("ref", C.c_double)]
 
 
+class _Pairing(C.Structure):
+    _fields_ = [("kind", C.c_int), ("sw", C.c_void_p), ("dh_k", C.c_double), ("dh_constant", C.c_double),
+                ("dh_epsilon", C.c_double), ("charge", C.c_void_p), ("gh_dmax_sq", C.c_double),
+                ("gh_d0", C.c_double), ("gh_c_dmax2", C.c_double), ("gh_A", C.c_double), ("gh_B", C.c_double),
+                ("gh_C", C.c_double), ("gh_D", C.c_double), ("gh_ntypes", C.c_int), ("type", C.c_void_p),
+                ("eta", C.c_void_p)]
+
+
+CV_COORDINATION, CV_DHENERGY, CV_GHBFIX = 0, 1, 2
+
+
 def _spec_is_r0(spec: str) -> bool:
     return spec.startswith("R0SYNTAX")
 
@@ -95,6 +106,13 @@ class Oracle:
         L.orc_coordination.argtypes = [C.POINTER(_Switch), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp,
                                        _u32p, C.c_int64, C.POINTER(C.c_double), _dp, _dp, C.c_int]
         L.orc_max_threads.restype = C.c_int
+        L.orc_dhenergy_constants.argtypes = [C.c_double] * 6 + [C.POINTER(C.c_double)] * 2
+        L.orc_ghbfix_constants.argtypes = [C.POINTER(_Pairing), C.c_double, C.c_double, C.c_double]
+        L.orc_pairing_eval.argtypes = [C.POINTER(_Pairing), C.c_double, C.POINTER(C.c_double), C.c_int64,
+                                       C.c_int64]
+        L.orc_pairing_eval.restype = C.c_double
+        L.orc_cv.argtypes = [C.POINTER(_Pairing), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp, _u32p,
+                             C.c_int64, C.POINTER(C.c_double), _dp, _dp, C.c_int]
 
     # -- pbc -----------------------------------------------------------------
     def pbc(self, box) -> _Pbc:
@@ -189,6 +207,58 @@ class Oracle:
         self.L.orc_coordination(C.byref(sw), C.byref(p), int(do_pbc), n, abs_index, pos.reshape(-1),
                                 pairs.reshape(-1) if len(pairs) else np.zeros(2, np.uint32), len(pairs),
                                 C.byref(s), deriv, vir, int(nthreads))
+        return s.value, deriv.reshape(n, 3), vir.reshape(3, 3)
+
+    # -- sibling CVs (DHENERGY, GHBFIX) -----------------------------------------
+    def dhenergy_constants(self, ionic, temp, epsilon, unit_energy=1.0, unit_length=1.0, unit_charge=1.0):
+        """(k, constant) of DHEnergy::DHEnergy (DHEnergy.cpp:112-113)."""
+        k, c = C.c_double(), C.c_double()
+        self.L.orc_dhenergy_constants(ionic, temp, epsilon, unit_energy, unit_length, unit_charge, C.byref(k),
+                                      C.byref(c))
+        return k.value, c.value
+
+    def pairing(self, kind, *, charges=None, dh=None, types=None, eta=None, ghbfix=None):
+        """A pairing descriptor.  DHENERGY: charges per slot and dh = (k, constant,
+        epsilon).  GHBFIX: types per slot, eta (n x n) and ghbfix = (d0, dmax, c).
+        The arrays are kept alive on the returned object."""
+        p = _Pairing()
+        p.kind = kind
+        keep = []
+        if kind == CV_DHENERGY:
+            q = np.ascontiguousarray(charges, np.float64)
+            keep.append(q)
+            p.charge = q.ctypes.data
+            p.dh_k, p.dh_constant, p.dh_epsilon = dh
+        elif kind == CV_GHBFIX:
+            t = np.ascontiguousarray(types, np.int32)
+            e = np.ascontiguousarray(eta, np.float64)
+            keep += [t, e]
+            p.type, p.eta = t.ctypes.data, e.ctypes.data
+            p.gh_ntypes = int(round(np.sqrt(e.size)))
+            self.L.orc_ghbfix_constants(C.byref(p), *[float(v) for v in ghbfix])
+        p._keep = keep
+        return p
+
+    def pairing_eval(self, p, r2, i, j):
+        df = C.c_double()
+        f = self.L.orc_pairing_eval(C.byref(p), float(r2), C.byref(df), int(i), int(j))
+        return f, df.value
+
+    def cv(self, p, pos, box, pairs, abs_index=None, do_pbc=True, nthreads=1):
+        """CoordinationBase::calculate with pairing p: s, derivatives, virial."""
+        pos = np.ascontiguousarray(np.asarray(pos, np.float64).reshape(-1, 3))
+        n = len(pos)
+        if abs_index is None:
+            abs_index = np.arange(n, dtype=np.int64)
+        abs_index = np.ascontiguousarray(abs_index, dtype=np.int64)
+        pairs = np.ascontiguousarray(np.asarray(pairs, np.uint32).reshape(-1, 2))
+        pb = self.pbc(box)
+        s = C.c_double()
+        deriv = np.zeros(3 * n)
+        vir = np.zeros(9)
+        self.L.orc_cv(C.byref(p), C.byref(pb), int(do_pbc), n, abs_index, pos.reshape(-1),
+                      pairs.reshape(-1) if len(pairs) else np.zeros(2, np.uint32), len(pairs), C.byref(s), deriv,
+                      vir, int(nthreads))
         return s.value, deriv.reshape(n, 3), vir.reshape(3, 3)
 
     def max_threads(self) -> int:

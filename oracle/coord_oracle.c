@@ -1094,9 +1094,77 @@ int64_t orc_nl_linkcells(int mode, int64_t n0, int64_t n1, const double *pos, co
 /* ------------------------------------------------------------------------ */
 /* CoordinationBase::calculate (CoordinationBase.cpp:142-231)               */
 /* ------------------------------------------------------------------------ */
+void orc_dhenergy_constants(double ionic, double temp, double epsilon, double unit_energy, double unit_length,
+                            double unit_charge, double *k, double *constant) {
+  /* DHEnergy.cpp:112-113, same operation order */
+  *constant = 138.935458111 / unit_energy / unit_length * unit_charge * unit_charge;
+  *k = sqrt(ionic / (epsilon * temp)) * 502.903741125 * unit_length;
+}
+
+void orc_ghbfix_constants(orc_pairing *p, double d0, double dmax, double c) {
+  /* GHBFIX.cpp:111-126 */
+  const double dmax2 = dmax - d0;
+  p->gh_dmax_sq = dmax * dmax;
+  p->gh_d0 = d0;
+  p->gh_c_dmax2 = c * dmax2;
+  p->gh_A = (-c * dmax2 * dmax2) / ((1 - c) * dmax2 * dmax2);
+  p->gh_B = (2 * dmax2) / ((1 - c) * dmax2 * dmax2);
+  p->gh_C = -1 / ((1 - c) * dmax2 * dmax2);
+  p->gh_D = 1 / (c * dmax2 * dmax2);
+}
+
+double orc_pairing_eval(const orc_pairing *p, double distance2, double *dfunc, int64_t i, int64_t j) {
+  if (p->kind == ORC_CV_DHENERGY) {
+    /* DHEnergy::pairing (DHEnergy.cpp:128-142); self pairs never reach it */
+    const double distance = sqrt(distance2);
+    const double invdistance = 1.0 / distance;
+    const double tmp = exp(-p->dh_k * distance) * invdistance * p->dh_constant * p->charge[i] * p->charge[j] /
+                       p->dh_epsilon;
+    const double dtmp = -(p->dh_k + invdistance) * tmp;
+    *dfunc = dtmp * invdistance;
+    return tmp;
+  }
+  if (p->kind == ORC_CV_GHBFIX) {
+    /* GHBFIX::pairing (GHBFIX.cpp:178-218) */
+    const double scale = p->eta[p->gh_ntypes * p->type[i] + p->type[j]];
+    if (distance2 > p->gh_dmax_sq) {
+      *dfunc = 0.0;
+      return 0.;
+    }
+    const double distance = sqrt(distance2);
+    const double rdist = distance - p->gh_d0;
+    double result = -1., df = 0.0;
+    if (rdist > 0.) {
+      if (rdist > p->gh_c_dmax2) {
+        result += (p->gh_A + p->gh_B * rdist + p->gh_C * rdist * rdist);
+        df += p->gh_B + 2 * p->gh_C * rdist;
+      } else {
+        result += p->gh_D * (rdist * rdist);
+        df += 2 * p->gh_D * rdist;
+      }
+      df /= distance;
+    }
+    result *= scale;
+    df *= scale;
+    *dfunc = df;
+    return result;
+  }
+  return orc_switch_calculate_sqr(p->sw, distance2, dfunc);
+}
+
 int orc_coordination(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t nslots,
                      const int64_t *abs_index, const double *pos, const uint32_t *pairs, int64_t npairs, double *s,
                      double *deriv, double virial[9], int nthreads) {
+  orc_pairing p;
+  memset(&p, 0, sizeof p);
+  p.kind = ORC_CV_COORDINATION;
+  p.sw = sw;
+  return orc_cv(&p, pbc, do_pbc, nslots, abs_index, pos, pairs, npairs, s, deriv, virial, nthreads);
+}
+
+int orc_cv(const orc_pairing *pr, const orc_pbc *pbc, int do_pbc, int64_t nslots, const int64_t *abs_index,
+           const double *pos, const uint32_t *pairs, int64_t npairs, double *s, double *deriv, double virial[9],
+           int nthreads) {
   double ncoord = 0.;
   for (int64_t i = 0; i < 3 * nslots; i++) deriv[i] = 0.0;
   for (int k = 0; k < 9; k++) virial[k] = 0.0;
@@ -1120,7 +1188,7 @@ int orc_coordination(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64
       double distance[3];
       pair_distance(pbc, do_pbc, pos, i0, i1, distance);
       double dfunc = 0.;
-      ncoord += orc_switch_calculate_sqr(sw, mod2(distance), &dfunc);
+      ncoord += orc_pairing_eval(pr, mod2(distance), &dfunc, i0, i1);
       double dd[3] = {dfunc * distance[0], dfunc * distance[1], dfunc * distance[2]};
       for (int k = 0; k < 3; k++) {
         dv[3 * i0 + k] -= dd[k];

@@ -111,6 +111,35 @@ int orc_coordination(const orc_switch *sw, const orc_pbc *pbc, int do_pbc,
                      const uint32_t *pairs, int64_t npairs,
                      double *s, double *deriv, double virial[9], int nthreads);
 
+/* ---- sibling CVs of CoordinationBase: the same loop, another pairing() --- */
+enum { ORC_CV_COORDINATION = 0, ORC_CV_DHENERGY = 1, ORC_CV_GHBFIX = 2 };
+
+typedef struct {
+  int kind;                 /* ORC_CV_* */
+  const orc_switch *sw;     /* COORDINATION: Coordination::pairing (Coordination.cpp:159-163) */
+  /* DHENERGY (DHEnergy.cpp:104-142) */
+  double dh_k, dh_constant, dh_epsilon;
+  const double *charge;     /* per slot */
+  /* GHBFIX (GHBFIX.cpp:111-218) */
+  double gh_dmax_sq, gh_d0, gh_c_dmax2, gh_A, gh_B, gh_C, gh_D;
+  int gh_ntypes;
+  const int *type;          /* per slot: index into the types table */
+  const double *eta;        /* gh_ntypes x gh_ntypes, eta[n*t1+t2] */
+} orc_pairing;
+
+/* DHEnergy::DHEnergy (DHEnergy.cpp:112-113): screening constant k and
+ * prefactor from I, TEMP, EPSILON and the energy/length/charge units. */
+void orc_dhenergy_constants(double ionic, double temp, double epsilon, double unit_energy, double unit_length,
+                            double unit_charge, double *k, double *constant);
+/* GHBFIX::GHBFIX (GHBFIX.cpp:111-126): dmax^2, c*(dmax-d0), A, B, C, D. */
+void orc_ghbfix_constants(orc_pairing *p, double d0, double dmax, double c);
+/* One pairing(distance2, dfunc, i, j) of the pairing's kind, slots i, j. */
+double orc_pairing_eval(const orc_pairing *p, double distance2, double *dfunc, int64_t i, int64_t j);
+/* CoordinationBase::calculate with any pairing (as orc_coordination). */
+int orc_cv(const orc_pairing *pr, const orc_pbc *pbc, int do_pbc, int64_t nslots, const int64_t *abs_index,
+           const double *pos, const uint32_t *pairs, int64_t npairs, double *s, double *deriv, double virial[9],
+           int nthreads);
+
 /* Number of OpenMP threads available (1 without OpenMP). */
 int orc_max_threads(void);
 

@@ -26,6 +26,7 @@ COORD_ERR_STATE = 7
 
 NL_NONE, NL_CLASSIC, NL_CELLS = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
+CV_COORDINATION, CV_DHENERGY, CV_GHBFIX = 0, 1, 2
 FLAG_REBUILD, FLAG_NO_DERIV, FLAG_DR0, FLAG_SAVE = 1, 2, 4, 8
 
 
@@ -75,6 +76,10 @@ def load() -> C.CDLL:
         L.coord_status_string.restype = C.c_char_p
         L.coord_set_groups.argtypes = [_vp, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_int64), C.c_int64]
         L.coord_get_nslots.argtypes = [_vp, C.POINTER(C.c_int64)]
+        L.coord_set_dhenergy.argtypes = [_vp] + [C.c_double] * 6
+        L.coord_set_charges.argtypes = [_vp, _dp, C.c_int64]
+        L.coord_set_ghbfix.argtypes = [_vp, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int32), C.c_int64, _dp,
+                                       C.c_int]
         L.coord_switch_eval.argtypes = [_vp, C.c_int, _dp, C.c_int, _dp, _dp]
         L.coord_switch_params.argtypes = [_vp, _dp]
         L.coord_forward.argtypes = [_vp, _dp, _dp, C.c_int64, C.c_uint, _dp, _dp, _dp]

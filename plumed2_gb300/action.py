@@ -25,7 +25,10 @@ from . import _lib
 from ._lib import CoordError, check, dptr
 
 _FLAGS = ("SERIAL", "PAIR", "NLIST", "NLISTCELLS", "NOPBC", "NUMERICAL_DERIVATIVES")
-_KEYS = ("GROUPA", "GROUPB", "NL_CUTOFF", "NL_STRIDE", "SWITCH", "R_0", "NN", "MM", "D_0", "LABEL")
+# CoordinationBase::registerKeywords (CoordinationBase.cpp:30-40)
+_BASE_KEYS = ("GROUPA", "GROUPB", "NL_CUTOFF", "NL_STRIDE", "LABEL")
+# Coordination::registerKeywords (Coordination.cpp:103-115)
+_KEYS = _BASE_KEYS + ("SWITCH", "R_0", "NN", "MM", "D_0")
 
 
 def parse_atom_list(text: str) -> List[int]:
@@ -73,6 +76,9 @@ def split_line(line: str) -> List[str]:
 class Coordination:
     """GPU COORDINATION behind the reference's keyword interface."""
 
+    DIRECTIVE = "COORDINATION"
+    KEYS = _KEYS
+
     def __init__(self, line: str = "", *, precision: str = "fp64", device: int = 0, **kw):
         words = split_line(line)
         opts = {}
@@ -82,7 +88,7 @@ class Coordination:
             if w.endswith(":") and not opts and not flags and label is None:
                 label = w[:-1]
                 continue
-            if w == "COORDINATION":
+            if w == self.DIRECTIVE:
                 continue
             if "=" in w:
                 k, v = w.split("=", 1)
@@ -100,7 +106,7 @@ class Coordination:
                 opts[k] = v
         self.label = opts.pop("LABEL", label)
         for k in opts:
-            if k not in _KEYS:
+            if k not in self.KEYS:
                 raise ValueError("cannot read keyword %s" % k)
         for f in flags:
             if f not in _FLAGS:
@@ -116,14 +122,8 @@ class Coordination:
         self._L = _lib.load()
         p = _lib.CoordParams()
         self._L.coord_params_default(C.byref(p))
-        sw = opts.get("SWITCH", "")
-        self._switch_bytes = sw.encode() if sw else None
-        p.switch_def = self._switch_bytes
-        if not sw:
-            p.r0 = float(opts.get("R_0", 0.0))
-            p.d0 = float(opts.get("D_0", 0.0))
-            p.nn = int(opts.get("NN", 6))
-            p.mm = int(opts.get("MM", 0))
+        self._switch_bytes = None
+        self._set_switch(p, opts)
         p.nopbc = int("NOPBC" in flags)
         p.pair = int("PAIR" in flags)
         p.serial = int("SERIAL" in flags)
@@ -142,6 +142,30 @@ class Coordination:
             self.close()
             raise ValueError(msg) if rc == _lib.COORD_ERR_ARG else CoordError(rc, msg)
         self._groups_set = False
+        try:
+            self._configure(opts)
+        except Exception:
+            self.close()
+            raise
+
+    def _set_switch(self, p, opts):
+        """SWITCH or R_0/NN/MM/D_0 (Coordination.cpp:128-157)."""
+        sw = opts.get("SWITCH", "")
+        self._switch_bytes = sw.encode() if sw else None
+        p.switch_def = self._switch_bytes
+        if not sw:
+            p.r0 = float(opts.get("R_0", 0.0))
+            p.d0 = float(opts.get("D_0", 0.0))
+            p.nn = int(opts.get("NN", 6))
+            p.mm = int(opts.get("MM", 0))
+
+    def _configure(self, opts):
+        """Set-up after coord_create (the sibling CVs' own keywords)."""
+
+    def _status(self, rc):
+        if rc == _lib.COORD_ERR_ARG:
+            raise ValueError(self._L.coord_last_error(self._ctx).decode())
+        check(self._L, self._ctx, rc)
 
     # -- groups ------------------------------------------------------------
     def _ensure_groups(self):
@@ -302,3 +326,78 @@ class Coordination:
             self.close()
         except Exception:
             pass
+
+
+class DHEnergy(Coordination):
+    """DHENERGY (colvar/DHEnergy.cpp:62): Debye-Hueckel energy between GROUPA and
+    GROUPB (or within GROUPA) with CoordinationBase's loop and keywords, plus
+    I (1.0 M), TEMP (300.0 K), EPSILON (80.0).  ``charges`` are the atoms'
+    charges by absolute atom index (Atoms::getCharge), ``units`` the action's
+    (energy, length, charge) units in kJ/mol, nm, e.  FP64 only."""
+
+    DIRECTIVE = "DHENERGY"
+    KEYS = _BASE_KEYS + ("I", "TEMP", "EPSILON")
+
+    def __init__(self, line: str = "", *, charges=None, units=(1.0, 1.0, 1.0), device: int = 0, **kw):
+        self._charges = charges
+        self._units = tuple(float(u) for u in units)
+        super().__init__(line, precision="fp64", device=device, **kw)
+
+    def _set_switch(self, p, opts):
+        p.r0 = 1.0  # the switching function is not used by this CV
+
+    def _configure(self, opts):
+        ionic = float(opts.get("I", 1.0))
+        temp = float(opts.get("TEMP", 300.0))
+        eps = float(opts.get("EPSILON", 80.0))
+        self.ionic, self.temp, self.epsilon = ionic, temp, eps
+        self._status(self._L.coord_set_dhenergy(self._ctx, ionic, temp, eps, *self._units))
+        if self._charges is not None:
+            self.set_charges(self._charges)
+
+    def set_charges(self, charges):
+        """Charges by absolute atom index, covering every atom of the groups."""
+        q = np.ascontiguousarray(charges, dtype=np.float64).reshape(-1)
+        self._status(self._L.coord_set_charges(self._ctx, dptr(q), len(q)))
+
+
+class GHBFIX(Coordination):
+    """GHBFIX (colvar/GHBFIX.cpp:63): the generalised hydrogen-bond fix energy
+    with CoordinationBase's loop and keywords, plus D_0, D_MAX, C (compulsory),
+    TYPES and PARAMS (table files, compulsory) and ENERGY_UNITS.  The tables
+    may be given as text (``types_text``/``params_text``) instead of files;
+    ``plumed_energy`` is the action's energy unit in kJ/mol.  FP64 only."""
+
+    DIRECTIVE = "GHBFIX"
+    KEYS = _BASE_KEYS + ("D_0", "D_MAX", "C", "TYPES", "PARAMS", "ENERGY_UNITS")
+
+    def __init__(self, line: str = "", *, types_text: Optional[str] = None, params_text: Optional[str] = None,
+                 plumed_energy: float = 1.0, device: int = 0, **kw):
+        self._texts = (types_text, params_text)
+        self._plumed_energy = float(plumed_energy)
+        super().__init__(line, precision="fp64", device=device, **kw)
+
+    def _set_switch(self, p, opts):
+        p.r0 = 1.0  # the switching function is not used by this CV
+
+    def _configure(self, opts):
+        from .siblings import ghbfix_tables
+        for k in ("D_0", "D_MAX", "C"):
+            if k not in opts:
+                raise ValueError("keyword %s is compulsory for this action" % k)
+        types_text, params_text = self._texts
+        if types_text is None or params_text is None:
+            for k in ("TYPES", "PARAMS"):
+                if k not in opts:
+                    raise ValueError("keyword %s is compulsory for this action" % k)
+            with open(opts["TYPES"]) as f:
+                types_text = f.read()
+            with open(opts["PARAMS"]) as f:
+                params_text = f.read()
+        types, eta = ghbfix_tables(types_text, params_text, opts.get("ENERGY_UNITS", "plumed"), self._plumed_energy)
+        self.types, self.eta = types, eta
+        d0, dmax, cc = float(opts["D_0"]), float(opts["D_MAX"]), float(opts["C"])
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        e = np.ascontiguousarray(eta, dtype=np.float64).reshape(-1)
+        self._status(self._L.coord_set_ghbfix(self._ctx, d0, dmax, cc, t.ctypes.data_as(C.POINTER(C.c_int32)),
+                                              len(t), dptr(e), eta.shape[0]))

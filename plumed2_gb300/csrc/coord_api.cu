@@ -76,6 +76,17 @@ struct coord_ctx {
   bool has_dup = false;           // an absolute index in two slots
   int host_direct = -1;           // kernels access pageable host arrays in place (-1: not probed)
   bool groups_set = false;
+  // the CV's pairing (COORD_CV_*); the sibling CVs' constants and per-atom
+  // data by absolute index, copied per slot to the device when needed
+  int cv = COORD_CV_COORDINATION;
+  double dh_k = 0.0, dh_const = 0.0, dh_eps = 1.0;
+  double gh_dmax_sq = 0.0, gh_d0 = 0.0, gh_c_dmax2 = 0.0, gh_A = 0.0, gh_B = 0.0, gh_C = 0.0, gh_D = 0.0;
+  std::vector<double> charges_abs, eta_host;
+  std::vector<int32_t> types_abs;
+  int n_types = 0;
+  bool sib_dirty = true;
+  DevBuf<double> d_charge, d_eta;
+  DevBuf<int> d_ptype;
   std::string err;
   cudaStream_t stream = nullptr;
   int nsm = 0;
@@ -282,6 +293,21 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.fc = c->fc.p;
   a.abs_of_slot = c->abs_of_slot.p;
   a.pos = d_pos;
+  a.cv = c->cv;
+  a.charge = c->d_charge.p;
+  a.ptype = c->d_ptype.p;
+  a.eta = c->d_eta.p;
+  a.n_types = c->n_types;
+  a.dh_k = c->dh_k;
+  a.dh_const = c->dh_const;
+  a.dh_eps = c->dh_eps;
+  a.gh_dmax_sq = c->gh_dmax_sq;
+  a.gh_d0 = c->gh_d0;
+  a.gh_c_dmax2 = c->gh_c_dmax2;
+  a.gh_A = c->gh_A;
+  a.gh_B = c->gh_B;
+  a.gh_C = c->gh_C;
+  a.gh_D = c->gh_D;
   a.cell_of_slot = c->cell_of_slot.p;
   a.cell_count = c->cell_count.p;
   a.cell_start = c->cell_start.p;
@@ -515,11 +541,55 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   cudaEventDestroy(t1);
 }
 
+// The sibling CVs' per-slot data on the device (after coord_set_groups or a
+// change of the data).  Every slot's atom must be covered by the data.
+int sibling_upload(coord_ctx *c) {
+  if (c->cv == COORD_CV_COORDINATION || !c->sib_dirty) return COORD_OK;
+  const size_t ns = (size_t)std::max<int64_t>(c->ns, 1);
+  cudaError_t e = cudaSuccess;
+  if (c->cv == COORD_CV_DHENERGY) {
+    if (c->charges_abs.empty()) return c->fail(COORD_ERR_STATE, "DHENERGY needs the atoms' charges (coord_set_charges)");
+    std::vector<double> q(ns, 0.0);
+    for (int64_t k = 0; k < c->ns; k++) {
+      const int64_t at = c->abs_host[k];
+      if (at < 0 || at >= (int64_t)c->charges_abs.size())
+        return c->fail(COORD_ERR_ARG, "the charges cover " + std::to_string(c->charges_abs.size()) +
+                                          " atoms, but atom number " + std::to_string(at + 1) + " is requested");
+      q[k] = c->charges_abs[at];
+    }
+    if ((e = c->d_charge.ensure(ns)) != cudaSuccess) return c->cuda_fail(e, "allocation");
+    if ((e = cudaMemcpy(c->d_charge.p, q.data(), ns * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return c->cuda_fail(e, "charge upload");
+  } else {
+    if (c->types_abs.empty()) return c->fail(COORD_ERR_STATE, "GHBFIX needs the types table (coord_set_ghbfix)");
+    std::vector<int> t(ns, 0);
+    for (int64_t k = 0; k < c->ns; k++) {
+      const int64_t at = c->abs_host[k];
+      // GHBFIX.cpp:180-186
+      if (at < 0 || at >= (int64_t)c->types_abs.size())
+        return c->fail(COORD_ERR_ARG, "your types table only covers " + std::to_string(c->types_abs.size()) +
+                                          " atoms, but you are trying to access atom number " + std::to_string(at + 1));
+      t[k] = c->types_abs[at];
+    }
+    const size_t ne = c->eta_host.size();
+    if ((e = c->d_ptype.ensure(ns)) != cudaSuccess || (e = c->d_eta.ensure(ne)) != cudaSuccess)
+      return c->cuda_fail(e, "allocation");
+    if ((e = cudaMemcpy(c->d_ptype.p, t.data(), ns * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(c->d_eta.p, c->eta_host.data(), ne * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return c->cuda_fail(e, "types upload");
+  }
+  c->sib_dirty = false;
+  return COORD_OK;
+}
+
 int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
                  double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream,
                  HostIO *hio = nullptr) {
   if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
   if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
+  if (c->cv != COORD_CV_COORDINATION && (flags & COORD_FLAG_DR0))
+    return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 derivatives belong to COORDINATION's switching function");
+  if (int rc = sibling_upload(c)) return rc;
   if (c->ns == 0) {
     // empty groups: s = 0, no derivatives
     if (s) cudaMemsetAsync(s, 0, sizeof(double) * n_frames, stream);
@@ -680,7 +750,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
 
 namespace coordgpu {
 int ctx_noalloc_view(const coord_ctx *c, const SwitchParams **sw, const coord_params **p) {
-  if (!c) return COORD_ERR_ARG;
+  if (!c || c->cv != COORD_CV_COORDINATION) return COORD_ERR_ARG;
   *sw = &c->sw;
   *p = &c->p;
   return COORD_OK;
@@ -826,6 +896,7 @@ int coord_destroy(coord_ctx *c) {
   c->cell_start.release();
   c->cell_fill.release();
   c->slot_of_rank.release();
+  c->rank_of_slot.release();
   c->cell_of_rank.release();
   c->scatter_tmp.release();
   c->row_len.release();
@@ -853,6 +924,9 @@ int coord_destroy(coord_ctx *c) {
   c->d_bpar.release();
   c->sv_vir.release();
   c->sv_par.release();
+  c->d_charge.release();
+  c->d_eta.release();
+  c->d_ptype.release();
   c->h_pos.release();
   c->h_out.release();
   c->h_fc.release();
@@ -898,9 +972,57 @@ int coord_set_groups(coord_ctx *c, const int64_t *a, int64_t na, const int64_t *
       cudaSuccess)
     return c->cuda_fail(e, "group upload");
   c->groups_set = true;
+  c->sib_dirty = true;
   c->firsttime = true;
   c->cap = 0;
   c->fc_uploaded.clear();
+  return COORD_OK;
+}
+
+int coord_set_dhenergy(coord_ctx *c, double ionic_strength, double temp, double epsilon, double unit_energy,
+                       double unit_length, double unit_charge) {
+  if (!c) return COORD_ERR_ARG;
+  if (c->p.precision != COORD_PREC_FP64) return c->fail(COORD_ERR_UNSUPPORTED, "DHENERGY: FP64 precision only");
+  if (!(unit_energy > 0.0) || !(unit_length > 0.0) || !(unit_charge > 0.0))
+    return c->fail(COORD_ERR_ARG, "DHENERGY cannot be used for calculations performed with natural units");
+  // DHEnergy::DHEnergy (DHEnergy.cpp:112-113), same operation order
+  c->dh_const = 138.935458111 / unit_energy / unit_length * unit_charge * unit_charge;
+  c->dh_k = std::sqrt(ionic_strength / (epsilon * temp)) * 502.903741125 * unit_length;
+  c->dh_eps = epsilon;
+  c->cv = COORD_CV_DHENERGY;
+  c->sib_dirty = true;
+  return COORD_OK;
+}
+
+int coord_set_charges(coord_ctx *c, const double *charges, int64_t n_atoms) {
+  if (!c) return COORD_ERR_ARG;
+  if (n_atoms < 1 || !charges) return c->fail(COORD_ERR_ARG, "empty charge array");
+  c->charges_abs.assign(charges, charges + n_atoms);
+  c->sib_dirty = true;
+  return COORD_OK;
+}
+
+int coord_set_ghbfix(coord_ctx *c, double d0, double dmax, double cc, const int32_t *types, int64_t n_atoms,
+                     const double *eta, int n_types) {
+  if (!c) return COORD_ERR_ARG;
+  if (c->p.precision != COORD_PREC_FP64) return c->fail(COORD_ERR_UNSUPPORTED, "GHBFIX: FP64 precision only");
+  if (n_atoms < 1 || !types || n_types < 1 || !eta) return c->fail(COORD_ERR_ARG, "empty GHBFIX tables");
+  for (int64_t k = 0; k < n_atoms; k++)
+    if (types[k] < 0 || types[k] >= n_types) return c->fail(COORD_ERR_ARG, "type id outside the eta table");
+  // GHBFIX::GHBFIX (GHBFIX.cpp:111-126), same operation order
+  const double dmax2 = dmax - d0;
+  c->gh_dmax_sq = dmax * dmax;
+  c->gh_d0 = d0;
+  c->gh_c_dmax2 = cc * dmax2;
+  c->gh_A = (-cc * dmax2 * dmax2) / ((1 - cc) * dmax2 * dmax2);
+  c->gh_B = (2 * dmax2) / ((1 - cc) * dmax2 * dmax2);
+  c->gh_C = -1 / ((1 - cc) * dmax2 * dmax2);
+  c->gh_D = 1 / (cc * dmax2 * dmax2);
+  c->types_abs.assign(types, types + n_atoms);
+  c->eta_host.assign(eta, eta + (size_t)n_types * n_types);
+  c->n_types = n_types;
+  c->cv = COORD_CV_GHBFIX;
+  c->sib_dirty = true;
   return COORD_OK;
 }
 
@@ -1022,6 +1144,9 @@ int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const d
   if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
   if (grad_param && !c->sw.grad_ok)
     return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
+  if (grad_param && c->cv != COORD_CV_COORDINATION)
+    return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 derivatives belong to COORDINATION's switching function");
+  if (int rc = sibling_upload(c)) return rc;
   cudaSetDevice(c->p.device);
   if (c->ns == 0) {
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;

@@ -58,7 +58,12 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
       const double4 xp4 = a.x64[fo + p];
       const double xp[3] = {xp4.x, xp4.y, xp4.z};
       double d[3], df;
-      const double sig = rfirst ? pair_fp64(sw, fc, a.do_pbc, xr, xp, d, df) : pair_fp64(sw, fc, a.do_pbc, xp, xr, d, df);
+      int sr = 0, sp = 0;  // slots, for the sibling CVs' per-atom data
+      if (a.cv != COORD_CV_COORDINATION) {
+        sr = a.slot_of_rank[fo + r];
+        sp = a.slot_of_rank[fo + p];
+      }
+      const double sig = rfirst ? pair_fp64(a, sw, fc, xr, xp, sr, sp, d, df) : pair_fp64(a, sw, fc, xp, xr, sp, sr, d, df);
       part[0] += sig;
       if (MODE >= EVAL_DERIV) {
         const double dd[3] = {df * d[0], df * d[1], df * d[2]};
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, i
         if (j >= jend || (diag && jl <= (int)threadIdx.x) || absj[jl] == absi) continue;
         double d[3], df;
         const double xjj[3] = {xj[jl][0], xj[jl][1], xj[jl][2]};
-        const double sig = pair_fp64(sw, fc, a.do_pbc, xi, xjj, d, df);
+        const double sig = pair_fp64(a, sw, fc, xi, xjj, i, j, d, df);
         part[0] += sig;
         if (MODE >= EVAL_DERIV) {
           const double dd[3] = {df * d[0], df * d[1], df * d[2]};
@@ -597,7 +602,7 @@ template <int MODE> __global__ void k_pairs64(KArgs a, SwitchParams sw, int use_
     const double *p0 = a.pos + (fo + i) * 3, *p1 = a.pos + (fo + i + a.nA) * 3;
     const double v1[3] = {p0[0], p0[1], p0[2]}, v2[3] = {p1[0], p1[1], p1[2]};
     double d[3], df;
-    part[0] = pair_fp64(sw, a.fc[f], a.do_pbc, v1, v2, d, df);
+    part[0] = pair_fp64(a, sw, a.fc[f], v1, v2, i, i + a.nA, d, df);
     if (MODE >= EVAL_DERIV) {
       const double dd[3] = {df * d[0], df * d[1], df * d[2]};
       for (int q = 0; q < 3; q++) {

@@ -59,6 +59,15 @@ struct KArgs {
   double *out_virial;           // [nframes][9]
   double *out_dparam;           // [nframes][2]
   const double *g;              // [nframes] upstream dV/ds (backward)
+  // the CV's pairing() (COORD_CV_*): the switching function for COORDINATION,
+  // or a sibling of CoordinationBase with its per-slot data
+  int cv;
+  const double *charge;         // [ns] DHENERGY: charge of each slot
+  const int *ptype;             // [ns] GHBFIX: type id of each slot
+  const double *eta;            // [n_types^2] GHBFIX scaling matrix
+  int n_types;
+  double dh_k, dh_const, dh_eps;                                    // DHEnergy.cpp:112-113
+  double gh_dmax_sq, gh_d0, gh_c_dmax2, gh_A, gh_B, gh_C, gh_D;     // GHBFIX.cpp:111-126
 };
 
 // FP32 parameters of a fixedRational<2*NH> switch (mixed path), plus the

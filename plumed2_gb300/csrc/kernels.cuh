@@ -993,12 +993,53 @@ __global__ void k_finalize32(KArgs a, int rank_order) {
 // FP64 pair math of one (first, second) pair: the reference's operations.
 // Returns sigma; d, dfunc out.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double pair_fp64(const SwitchParams &sw, const FrameConst &fc, int do_pbc,
-                                            const double v1[3], const double v2[3], double d[3], double &dfunc) {
-  if (do_pbc)
+// pairing(distance2, dfunc, i, j) of the sibling CVs of CoordinationBase,
+// slots s1 = first, s2 = second of the pair (the operation order of the
+// reference, built without FMA contraction):
+//   DHENERGY  DHEnergy::pairing (DHEnergy.cpp:128-142)
+//   GHBFIX    GHBFIX::pairing (GHBFIX.cpp:178-218)
+__device__ __noinline__ double sibling_pairing(const KArgs &a, double distance2, int s1, int s2, double &dfunc) {
+  if (a.cv == COORD_CV_DHENERGY) {
+    const double distance = sqrt(distance2);
+    const double invdistance = 1.0 / distance;
+    const double tmp = exp(-a.dh_k * distance) * invdistance * a.dh_const * a.charge[s1] * a.charge[s2] / a.dh_eps;
+    const double dtmp = -(a.dh_k + invdistance) * tmp;
+    dfunc = dtmp * invdistance;
+    return tmp;
+  }
+  const double scale = a.eta[a.n_types * a.ptype[s1] + a.ptype[s2]];
+  if (distance2 > a.gh_dmax_sq) {
+    dfunc = 0.0;
+    return 0.;
+  }
+  const double distance = sqrt(distance2);
+  const double rdist = distance - a.gh_d0;
+  double result = -1., df = 0.0;
+  if (rdist > 0.) {
+    if (rdist > a.gh_c_dmax2) {
+      result += (a.gh_A + a.gh_B * rdist + a.gh_C * rdist * rdist);
+      df += a.gh_B + 2 * a.gh_C * rdist;
+    } else {
+      result += a.gh_D * (rdist * rdist);
+      df += 2 * a.gh_D * rdist;
+    }
+    df /= distance;
+  }
+  dfunc = df * scale;
+  return result * scale;
+}
+
+// One pair of the FP64 path in the reference's orientation: d = min-image
+// of v2 - v1, the CV's pairing of r^2 = |d|^2.  s1, s2: slots of the first
+// and second atom (read only by the sibling CVs).
+__device__ __forceinline__ double pair_fp64(const KArgs &a, const SwitchParams &sw, const FrameConst &fc,
+                                            const double v1[3], const double v2[3], int s1, int s2, double d[3],
+                                            double &dfunc) {
+  if (a.do_pbc)
     pbc_distance(fc.pbc, v1, v2, d);
   else
     for (int k = 0; k < 3; k++) d[k] = v2[k] - v1[k];
+  if (a.cv != COORD_CV_COORDINATION) return sibling_pairing(a, mod2(d), s1, s2, dfunc);
   VD<double> r = sw_calculate_sqr<double>(sw, mod2(d));
   dfunc = r.d;
   return r.f;

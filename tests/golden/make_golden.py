@@ -17,6 +17,12 @@ so that the tests run where the reference tree is absent.  Sources:
   (forces and virial of a RESTRAINT with SLOPE=1 on c+d)
 * regtest/tools/rt-Neigbourlist         unitTest.reference / testNoNL.reference
   (exact neighbour sets on a simple-cubic lattice)
+* regtest/basic/rt-dhenergy, rt-dhenergy2  DHENERGY between atoms 1-3 and 4-10
+  of regtest/trajectories/trajectory.xyz, charges from test.pdb:
+  COLVAR.reference, deriv.reference (rt-dhenergy2: UNITS CHARGE=0.1)
+* regtest/basic/rt-ghbfix               GHBFIX PAIR of two atoms 0.002*i apart
+  (the regtest's own generated trajectory), typesTable.dat and
+  scalingParameters.dat as text: colvar.reference, der.reference
 """
 from __future__ import annotations
 
@@ -145,6 +151,46 @@ def main(ref):
                "lattice": "sc (AtomDistribution.cpp:205-240): integer sites i,j,k, x fastest; box = ceil(cbrt(N))",
                "cutoff_factor": 1.999, "sets": sets},
               open(os.path.join(HERE, "rt_neighbourlist.json"), "w"))
+    # --- rt-dhenergy / rt-dhenergy2 -----------------------------------------
+    ddh = os.path.join(reg, "basic", "rt-dhenergy")
+    frames, boxes = read_xyz(os.path.join(reg, "trajectories", "trajectory.xyz"))
+    charges = []
+    for line in open(os.path.join(ddh, "test.pdb")):
+        if line.startswith("ATOM"):
+            charges.append(float(line.split()[-1]))
+    colvar = read_table(os.path.join(ddh, "COLVAR.reference"))
+    deriv = read_table(os.path.join(ddh, "deriv.reference"))
+    nat = len(charges)
+    npar = 3 * nat + 9
+    der = [[r[2:] for r in deriv[f * npar:(f + 1) * npar]] for f in range(len(colvar))]
+    colvar2 = read_table(os.path.join(reg, "basic", "rt-dhenergy2", "COLVAR.reference"))
+    json.dump({"source": "regtest/basic/rt-dhenergy (plumed.dat, test.pdb, COLVAR.reference, deriv.reference), "
+                         "regtest/basic/rt-dhenergy2/COLVAR.reference, regtest/trajectories/trajectory.xyz",
+               "group_a": [1, 2, 3], "group_b": list(range(4, nat + 1)),
+               "actions": {"dh1": {"I": 0.1, "TEMP": 300.0, "EPSILON": 80.0},
+                           "dh2": {"I": 0.1, "TEMP": 300.0, "EPSILON": 80.0},
+                           "dh3": {"I": 0.0, "TEMP": 300.0, "EPSILON": 80.0},
+                           "dh4": {"I": 0.1, "TEMP": 10.0, "EPSILON": 200.0}},
+               "order": ["dh1", "dh2", "dh3", "dh4"], "charges": charges,
+               "frames": [fr[:nat] for fr in frames], "box": boxes,
+               "colvar": [r[1:] for r in colvar], "deriv": der,
+               "colvar_units_charge_0.1": [r[1:] for r in colvar2], "fmt": "%6.5f"},
+              open(os.path.join(HERE, "rt_dhenergy.json"), "w"))
+
+    # --- rt-ghbfix -----------------------------------------------------------
+    dgh = os.path.join(reg, "basic", "rt-ghbfix")
+    colvar = read_table(os.path.join(dgh, "colvar.reference"))
+    deriv = read_table(os.path.join(dgh, "der.reference"))
+    der = [[r[3] for r in deriv[f * 15:(f + 1) * 15]] for f in range(len(colvar))]
+    json.dump({"source": "regtest/basic/rt-ghbfix (plumed.dat, config, typesTable.dat, scalingParameters.dat, "
+                         "colvar.reference, der.reference)",
+               "line": "PAIR GROUPA=1 GROUPB=2 D_0=0.2 D_MAX=0.3 C=0.8 ENERGY_UNITS=kcal/mol",
+               "types_file": open(os.path.join(dgh, "typesTable.dat")).read(),
+               "params_file": open(os.path.join(dgh, "scalingParameters.dat")).read(),
+               "trajectory": "frame i = 1..150: atom 1 at (0,0,0), atom 2 at (0,0,0.002 i), box 100 100 100",
+               "c1_minus_ghbfix": 4.184, "colvar_c1": [r[2] for r in colvar], "deriv_ghbfix": der,
+               "fmt": "%8.4f"},
+              open(os.path.join(HERE, "rt_ghbfix.json"), "w"))
     print("fixtures written to", HERE)
 
 

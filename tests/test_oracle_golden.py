@@ -138,3 +138,50 @@ def test_cell_nl_equals_classic(orc):
             assert len(a) == len(b)
             a = a[np.lexsort((a[:, 1], a[:, 0]))]
             assert np.array_equal(a, b)
+
+
+def test_rt_dhenergy(orc, golden):
+    """regtest/basic/rt-dhenergy: DHENERGY GROUPA=1-3 GROUPB=4-10 with four
+    (I, TEMP, EPSILON) sets, COLVAR and DUMPDERIVATIVES at %6.5f; and
+    rt-dhenergy2 (UNITS CHARGE=0.1: charges x10 in plumed units, same values)."""
+    import oracle
+    g = golden("rt_dhenergy.json")
+    na, nb = len(g["group_a"]), len(g["group_b"])
+    pairs = orc.all_pairs(oracle.MODE_TWO, na, nb)
+    q = np.array(g["charges"])
+    assert len(g["frames"]) == len(g["colvar"]) == 5
+    for fi, (frame, box) in enumerate(zip(g["frames"], g["box"])):
+        B = np.diag(box)
+        der = np.array(g["deriv"][fi])
+        for ai, lab in enumerate(g["order"]):
+            act = g["actions"][lab]
+            k, c = orc.dhenergy_constants(act["I"], act["TEMP"], act["EPSILON"])
+            p = orc.pairing(oracle.CV_DHENERGY, charges=q, dh=(k, c, act["EPSILON"]))
+            s, d, v = orc.cv(p, frame, B, pairs)
+            assert abs(s - g["colvar"][fi][ai]) <= 5.01e-6, (fi, lab)
+            got = np.concatenate([d.reshape(-1), v.reshape(-1)])
+            assert np.abs(got - der[:, ai]).max() <= 5.01e-6, (fi, lab)
+            k2, c2 = orc.dhenergy_constants(act["I"], act["TEMP"], act["EPSILON"], unit_charge=0.1)
+            p2 = orc.pairing(oracle.CV_DHENERGY, charges=q / 0.1, dh=(k2, c2, act["EPSILON"]))
+            s2, _, _ = orc.cv(p2, frame, B, pairs)
+            assert abs(s2 - g["colvar_units_charge_0.1"][fi][ai]) <= 5.01e-6, (fi, lab)
+
+
+def test_rt_ghbfix(orc, golden):
+    """regtest/basic/rt-ghbfix: GHBFIX PAIR of atoms 1, 2 at 0.002 i nm apart
+    (i = 1..150), TYPES/PARAMS tables read by the product's parser, value
+    (colvar c1 = ghbfix + 4.184) and DUMPDERIVATIVES at %8.4f."""
+    import oracle
+    from plumed2_gb300.siblings import ghbfix_tables
+    g = golden("rt_ghbfix.json")
+    types, eta = ghbfix_tables(g["types_file"], g["params_file"], energy_units="kcal/mol")
+    # the PARAMS rows naming type0/type3 (absent from TYPES) alias id 0
+    assert np.allclose(eta, np.array([[5.0, 1.0], [6.0, 0.0]]) * 4.184)
+    p = orc.pairing(oracle.CV_GHBFIX, types=types[:2], eta=eta, ghbfix=(0.2, 0.3, 0.8))
+    B = np.diag([100.0, 100.0, 100.0])
+    for i in range(1, 151):
+        z = float("%.6g" % (i * 0.002))  # awk's default output format in the regtest's generator
+        s, d, v = orc.cv(p, [[0, 0, 0], [0, 0, z]], B, np.array([[0, 1]], np.uint32))
+        assert abs(s + g["c1_minus_ghbfix"] - g["colvar_c1"][i - 1]) <= 5.01e-5, i
+        got = np.concatenate([d.reshape(-1), v.reshape(-1)])
+        assert np.abs(got - np.array(g["deriv_ghbfix"][i - 1])).max() <= 5.01e-5, i
