@@ -179,6 +179,30 @@ int coord_forward_device(coord_ctx *ctx, int n_frames, const double *pos, const 
 int coord_backward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, const double *g,
                           double *grad_pos, double *grad_box, double *grad_param, void *stream);
 
+/* ---- per-atom coordination -------------------------------------------------
+ * COORDINATIONNUMBER (symfunc/CoordinationNumbers.cpp:247-309) is a
+ * CONTACT_MATRIX (adjmat/ContactMatrix.h:95-120) times a vector of ones:
+ * cn_i = sum_j sigma(r_ij) over the pairs of slot i.  Replaces that
+ * CONTACT_MATRIX + MATRIX_VECTOR_PRODUCT chain.  A pair with r^2 < DBL_EPSILON
+ * or sigma < DBL_EPSILON contributes nothing, as in ContactMatrix.h:99-107.
+ * Needs a COORDINATION context with NLIST or NLISTCELLS (the contact matrix's
+ * link cells have cutoff d_max; a classic list with NL_CUTOFF = d_max and
+ * NL_STRIDE = 1 holds exactly its nonzero pairs) and no PAIR.
+ * Single list (SPECIES): every slot's sum over its pairs.  Two lists
+ * (SPECIESA, SPECIESB): GROUPA slots get the row sums of the reference's
+ * matrix; GROUPB slots get the column sums, which the reference does not
+ * output.
+ * cn [frames][slots] and s [frames] (NULL allowed: sum of sigma over the
+ * pairs) are device pointers; flags: COORD_FLAG_REBUILD only. */
+int coord_peratom_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, int64_t step,
+                         unsigned flags, double *cn, double *s, void *stream);
+/* Vector-Jacobian product of the per-atom forward: g [frames][slots] is
+ * dV/dcn; grad_pos [frames][slots][3] receives dV/dx = sum over pairs of
+ * (g_i + g_j) dsigma_ij/dx, grad_box [frames][9] dV/dh (NULL allowed), on
+ * the neighbour lists of the last forward with the same frames. */
+int coord_peratom_backward_device(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes,
+                                  const double *g, double *grad_pos, double *grad_box, void *stream);
+
 /* Force application on the device (Colvar::apply, src/core/Colvar.cpp:50-60;
  * ActionWithValue::checkForForces, src/core/ActionWithValue.cpp:337-411;
  * ActionAtomistic::setForcesOnAtoms/setForcesOnCell, ActionAtomistic.cpp:

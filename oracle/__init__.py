@@ -113,6 +113,8 @@ class Oracle:
         L.orc_pairing_eval.restype = C.c_double
         L.orc_cv.argtypes = [C.POINTER(_Pairing), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp, _u32p,
                              C.c_int64, C.POINTER(C.c_double), _dp, _dp, C.c_int]
+        L.orc_peratom.argtypes = [C.POINTER(_Switch), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp, _u32p,
+                                  C.c_int64, C.c_void_p, _dp, C.c_void_p, C.c_void_p]
 
     # -- pbc -----------------------------------------------------------------
     def pbc(self, box) -> _Pbc:
@@ -260,6 +262,29 @@ class Oracle:
                       pairs.reshape(-1) if len(pairs) else np.zeros(2, np.uint32), len(pairs), C.byref(s), deriv,
                       vir, int(nthreads))
         return s.value, deriv.reshape(n, 3), vir.reshape(3, 3)
+
+    def peratom(self, spec, pos, box, pairs, abs_index=None, do_pbc=True, g=None):
+        """Per-atom coordination over the given pairs (CONTACT_MATRIX x ones):
+        cn per slot; with g (dV/dcn per slot) also (grad (nslots x 3), virial 3x3)."""
+        pos = np.ascontiguousarray(np.asarray(pos, np.float64).reshape(-1, 3))
+        n = len(pos)
+        if abs_index is None:
+            abs_index = np.arange(n, dtype=np.int64)
+        abs_index = np.ascontiguousarray(abs_index, dtype=np.int64)
+        pairs = np.ascontiguousarray(np.asarray(pairs, np.uint32).reshape(-1, 2))
+        sw = self.switch(spec)
+        pb = self.pbc(box)
+        cn = np.zeros(n)
+        grad = np.zeros(3 * n)
+        vir = np.zeros(9)
+        gg = None if g is None else np.ascontiguousarray(g, np.float64)
+        self.L.orc_peratom(C.byref(sw), C.byref(pb), int(do_pbc), n, abs_index, pos.reshape(-1),
+                           pairs.reshape(-1) if len(pairs) else np.zeros(2, np.uint32), len(pairs),
+                           None if gg is None else gg.ctypes.data, cn, None if gg is None else grad.ctypes.data,
+                           None if gg is None else vir.ctypes.data)
+        if gg is None:
+            return cn
+        return cn, grad.reshape(n, 3), vir.reshape(3, 3)
 
     def max_threads(self) -> int:
         return self.L.orc_max_threads()

@@ -1152,6 +1152,40 @@ double orc_pairing_eval(const orc_pairing *p, double distance2, double *dfunc, i
   return orc_switch_calculate_sqr(p->sw, distance2, dfunc);
 }
 
+int orc_peratom(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t nslots, const int64_t *abs_index,
+                const double *pos, const uint32_t *pairs, int64_t npairs, const double *g, double *cn, double *grad,
+                double virial[9]) {
+  for (int64_t i = 0; i < nslots; i++) cn[i] = 0.0;
+  if (g) {
+    for (int64_t i = 0; i < 3 * nslots; i++) grad[i] = 0.0;
+    for (int k = 0; k < 9; k++) virial[k] = 0.0;
+  }
+  for (int64_t i = 0; i < npairs; ++i) {
+    const int64_t i0 = pairs[2 * i], i1 = pairs[2 * i + 1];
+    if (abs_index[i0] == abs_index[i1]) continue;
+    double distance[3];
+    pair_distance(pbc, do_pbc, pos, i0, i1, distance);
+    const double m2 = mod2(distance);
+    if (m2 < DBL_EPSILON) continue; /* ContactMatrix.h:99-101 */
+    double dfunc = 0.;
+    const double sig = orc_switch_calculate_sqr(sw, m2, &dfunc);
+    if (sig < DBL_EPSILON) continue; /* ContactMatrix.h:104-107 */
+    cn[i0] += sig;
+    cn[i1] += sig;
+    if (g) {
+      const double w = g[i0] + g[i1];
+      const double dd[3] = {w * dfunc * distance[0], w * dfunc * distance[1], w * dfunc * distance[2]};
+      for (int k = 0; k < 3; k++) {
+        grad[3 * i0 + k] -= dd[k];
+        grad[3 * i1 + k] += dd[k];
+      }
+      for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) virial[3 * a + b] -= dd[a] * distance[b];
+    }
+  }
+  return 0;
+}
+
 int orc_coordination(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t nslots,
                      const int64_t *abs_index, const double *pos, const uint32_t *pairs, int64_t npairs, double *s,
                      double *deriv, double virial[9], int nthreads) {

@@ -140,6 +140,18 @@ int orc_cv(const orc_pairing *pr, const orc_pbc *pbc, int do_pbc, int64_t nslots
            const double *pos, const uint32_t *pairs, int64_t npairs, double *s, double *deriv, double virial[9],
            int nthreads);
 
+/* ---- per-atom coordination ------------------------------------------------
+ * COORDINATIONNUMBER (symfunc/CoordinationNumbers.cpp:268-309): the weights
+ * of CONTACT_MATRIX (adjmat/ContactMatrix.h:95-120) summed per atom over the
+ * given pairs, i.e. times a vector of ones.  A pair with r^2 < DBL_EPSILON or
+ * sigma < DBL_EPSILON has no weight and no derivative.  cn[slot] gets sigma
+ * from both atoms' sides.  With g (dV/dcn per slot) non-NULL, grad (nslots x
+ * 3) and virial receive the vector-Jacobian product: each pair's derivative
+ * weighted by g[i] + g[j]. */
+int orc_peratom(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t nslots, const int64_t *abs_index,
+                const double *pos, const uint32_t *pairs, int64_t npairs, const double *g, double *cn, double *grad,
+                double virial[9]);
+
 /* Number of OpenMP threads available (1 without OpenMP). */
 int orc_max_threads(void);
 

@@ -78,6 +78,8 @@ def load() -> C.CDLL:
         L.coord_get_nslots.argtypes = [_vp, C.POINTER(C.c_int64)]
         L.coord_set_dhenergy.argtypes = [_vp] + [C.c_double] * 6
         L.coord_set_charges.argtypes = [_vp, _dp, C.c_int64]
+        L.coord_peratom_device.argtypes = [_vp, C.c_int, _vp, _dp, C.c_int64, C.c_uint, _vp, _vp, _vp]
+        L.coord_peratom_backward_device.argtypes = [_vp, C.c_int, _vp, _dp, _vp, _vp, _vp, _vp]
         L.coord_set_ghbfix.argtypes = [_vp, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int32), C.c_int64, _dp,
                                        C.c_int]
         L.coord_switch_eval.argtypes = [_vp, C.c_int, _dp, C.c_int, _dp, _dp]

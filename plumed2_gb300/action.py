@@ -401,3 +401,117 @@ class GHBFIX(Coordination):
         e = np.ascontiguousarray(eta, dtype=np.float64).reshape(-1)
         self._status(self._L.coord_set_ghbfix(self._ctx, d0, dmax, cc, t.ctypes.data_as(C.POINTER(C.c_int32)),
                                               len(t), dptr(e), eta.shape[0]))
+
+
+class CoordinationNumbers:
+    """COORDINATIONNUMBER (symfunc/CoordinationNumbers.cpp:247-309): per-atom
+    coordination numbers cn_i = sum_j sigma(r_ij), the reference's
+    CONTACT_MATRIX (adjmat/ContactMatrix.h) times a vector of ones, on the GPU.
+
+        c = CoordinationNumbers("SPECIES=1-400 SWITCH={RATIONAL D_0=3.0 R_0=1.5 D_MAX=6.0}")
+        cn = c.calculate(positions, box)          # one value per SPECIES atom
+
+    Keywords: SPECIES, or SPECIESA with SPECIESB; SWITCH or R_0/NN/MM/D_0.  The
+    contact matrix's link cells have cutoff d_max, so the pairs are a
+    neighbour list with NL_CUTOFF = d_max rebuilt every call (the same
+    inclusive test).  A switch without D_MAX weighs every pair: the list
+    cutoff then covers every minimum-image distance of the box.  Positions
+    are the requested atoms in request order (SPECIES, or SPECIESA then
+    SPECIESB); the box is periodic."""
+
+    KEYS = ("SPECIES", "SPECIESA", "SPECIESB", "SWITCH", "R_0", "NN", "MM", "D_0", "LABEL")
+
+    def __init__(self, line: str = "", *, precision: str = "fp64", device: int = 0):
+        words = split_line(line)
+        opts = {}
+        for w in words:
+            if w.endswith(":") and not opts:
+                opts["LABEL"] = w[:-1]
+                continue
+            if w == "COORDINATIONNUMBER":
+                continue
+            if "=" not in w:
+                raise ValueError("cannot read flag %s" % w)
+            k, v = w.split("=", 1)
+            if v.startswith("{") and v.endswith("}"):
+                v = v[1:-1]
+            if k.upper() not in self.KEYS:
+                raise ValueError("cannot read keyword %s" % k)
+            opts[k.upper()] = v
+        if "SPECIES" in opts:
+            self.group_a, self.group_b = parse_atom_list(opts["SPECIES"]), []
+        elif "SPECIESA" in opts and "SPECIESB" in opts:
+            self.group_a, self.group_b = parse_atom_list(opts["SPECIESA"]), parse_atom_list(opts["SPECIESB"])
+        else:
+            raise ValueError("missing atoms input use SPECIES or SPECIESA/SPECIESB")
+        if "SWITCH" in opts:
+            self._switch = "SWITCH={%s}" % opts["SWITCH"]
+        elif "R_0" in opts:
+            self._switch = " ".join("%s=%s" % (k, opts[k]) for k in ("R_0", "NN", "MM", "D_0") if k in opts)
+        else:
+            raise ValueError("missing switching function parameters use SWITCH/R_0")
+        self.precision, self.device = precision, device
+        self._act = None
+        self._cut = None
+        # d_max of the switch (huge without D_MAX)
+        probe = Coordination("GROUPA=1 " + self._switch, precision="fp64", device=device)
+        self.dmax = probe.switch_params()["dmax"]
+        probe.close()
+
+    @property
+    def nslots(self) -> int:
+        return len(self.group_a) + len(self.group_b)
+
+    def _action(self, boxes):
+        """The Coordination context whose list holds the contact matrix's pairs."""
+        b = np.asarray(boxes, dtype=np.float64).reshape(-1, 3, 3)
+        reach = 0.5 * np.linalg.norm(b, axis=2).sum(axis=1).max() * (1.0 + 1e-9) + 1e-9
+        cut = self.dmax if self.dmax < reach else reach
+        if self._act is None or (self._cut < reach and cut != self._cut):
+            if self._act is not None:
+                self._act.close()
+            ga = ",".join(str(i + 1) for i in self.group_a)
+            gb = ",".join(str(i + 1) for i in self.group_b)
+            line = "GROUPA=%s%s %s NLIST NL_CUTOFF=%.17g NL_STRIDE=1" % (ga, " GROUPB=" + gb if gb else "",
+                                                                        self._switch, cut)
+            self._act = Coordination(line, precision=self.precision, device=self.device)
+            self._act._ensure_groups()
+            self._cut = cut
+        return self._act
+
+    def forward_device(self, pos_ptr: int, boxes, n_frames: int, cn_ptr: int, s_ptr: int = 0, stream: int = 0,
+                       step: int = 0):
+        """cn [frames][slots] (device) for device positions [frames][slots][3]."""
+        act = self._action(boxes)
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 9))
+        rc = act._L.coord_peratom_device(act._ctx, int(n_frames), C.c_void_p(pos_ptr), dptr(bx), int(step), 0,
+                                         C.c_void_p(cn_ptr), C.c_void_p(s_ptr or None), C.c_void_p(stream or None))
+        check(act._L, act._ctx, rc)
+
+    def backward_device(self, pos_ptr: int, boxes, n_frames: int, g_ptr: int, grad_pos_ptr: int,
+                        grad_box_ptr: int = 0, stream: int = 0):
+        """dV/dx [frames][slots][3] and dV/dh [frames][9] for dV/dcn = g [frames][slots]."""
+        act = self._action(boxes)
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 9))
+        rc = act._L.coord_peratom_backward_device(act._ctx, int(n_frames), C.c_void_p(pos_ptr), dptr(bx),
+                                                  C.c_void_p(g_ptr), C.c_void_p(grad_pos_ptr),
+                                                  C.c_void_p(grad_box_ptr or None), C.c_void_p(stream or None))
+        check(act._L, act._ctx, rc)
+
+    def calculate(self, positions, box, step: int = 0, all_slots: bool = False) -> np.ndarray:
+        """cn of the SPECIES (or SPECIESA) atoms; all_slots: also the SPECIESB
+        column sums."""
+        import torch
+        pos = torch.as_tensor(np.ascontiguousarray(np.asarray(positions, np.float64).reshape(1, -1, 3)),
+                              device="cuda:%d" % self.device)
+        if pos.shape[1] != self.nslots:
+            raise ValueError("expected %d positions, got %d" % (self.nslots, pos.shape[1]))
+        cn = torch.empty(1, self.nslots, dtype=torch.float64, device=pos.device)
+        self.forward_device(pos.data_ptr(), np.asarray(box, np.float64).reshape(1, 9), 1, cn.data_ptr(), step=step)
+        out = cn[0].cpu().numpy()
+        return out if all_slots else out[:len(self.group_a)]
+
+    def close(self):
+        if self._act is not None:
+            self._act.close()
+            self._act = None

@@ -80,3 +80,49 @@ def coordination(action, pos: torch.Tensor, box: torch.Tensor, r0: torch.Tensor 
         pos = pos.unsqueeze(0)
     s = CoordinationFunction.apply(pos, box, r0, d0, action, step)
     return s[0] if squeeze else s
+
+
+class CoordinationNumbersFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, box, cns, step):
+        if pos.dtype != torch.float64 or not pos.is_cuda:
+            raise TypeError("positions must be a float64 CUDA tensor of shape (frames, slots, 3)")
+        pos = pos.contiguous()
+        F = pos.shape[0]
+        boxes = _boxes_host(box, F)
+        cn = torch.empty(F, pos.shape[1], dtype=torch.float64, device=pos.device)
+        stream = torch.cuda.current_stream(pos.device).cuda_stream
+        cns.forward_device(pos.data_ptr(), boxes, F, cn.data_ptr(), stream=stream, step=step)
+        ctx.save_for_backward(pos)
+        ctx.cns = cns
+        ctx.boxes = boxes
+        ctx.box_shape = box.shape
+        ctx.box_device = box.device
+        return cn
+
+    @staticmethod
+    def backward(ctx, grad_cn):
+        (pos,) = ctx.saved_tensors
+        F = pos.shape[0]
+        g = grad_cn.detach().to(torch.float64).contiguous()
+        gpos = torch.empty_like(pos)
+        gbox = torch.empty(F, 9, dtype=torch.float64, device=pos.device)
+        stream = torch.cuda.current_stream(pos.device).cuda_stream
+        ctx.cns.backward_device(pos.data_ptr(), ctx.boxes, F, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(),
+                                stream=stream)
+        gb = gbox.reshape(F, 3, 3)
+        if len(ctx.box_shape) == 2:
+            gb = gb.sum(0)
+        gb = gb.reshape(ctx.box_shape).to(ctx.box_device)
+        return gpos, gb, None, None
+
+
+def coordination_numbers(cns, pos: torch.Tensor, box: torch.Tensor, step: int = 0) -> torch.Tensor:
+    """Per-slot coordination numbers (frames, slots) of a CoordinationNumbers
+    action, differentiable in positions and box (one vector-Jacobian product
+    over the forward's pairs)."""
+    squeeze = pos.dim() == 2
+    if squeeze:
+        pos = pos.unsqueeze(0)
+    cn = CoordinationNumbersFunction.apply(pos, box, cns, step)
+    return cn[0] if squeeze else cn

@@ -85,6 +85,7 @@ struct coord_ctx {
   std::vector<int32_t> types_abs;
   int n_types = 0;
   bool sib_dirty = true;
+  bool peratom_used = false;  // the per-atom calls have run (FP64: accw64 is kept)
   DevBuf<double> d_charge, d_eta;
   DevBuf<int> d_ptype;
   std::string err;
@@ -105,7 +106,7 @@ struct coord_ctx {
   DevBuf<uint32_t> ell, self_pairs;
   DevBuf<unsigned long long> nl_count, mm;
   DevBuf<unsigned char> pair_flag;
-  DevBuf<double> acc64, partials;
+  DevBuf<double> acc64, partials, accw64;
   DevBuf<float4> acc32;
   DevBuf<unsigned> tickets, band_tickets;
   DevBuf<unsigned char> band_flag;
@@ -126,8 +127,8 @@ struct coord_ctx {
   // tuning
   int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0, nl_unroll = 4;
   // mixed NL pass, tuned per evaluation mode (EVAL_S / EVAL_DERIV / EVAL_PARAM)
-  int nlm_blocks[3] = {0, 0, 0}, nlm_unroll[3] = {4, 4, 4};
-  bool nlm_tuned[3] = {false, false, false};
+  int nlm_blocks[5] = {0, 0, 0, 0, 0}, nlm_unroll[5] = {4, 4, 4, 4, 4};
+  bool nlm_tuned[5] = {false, false, false, false, false};
   int cells_launch = 0;  // cells per frame known on the host (0: use ncell_cap)
   bool tuned = false;
   // timing: one event pair per pair-kernel launch while enabled
@@ -252,6 +253,7 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->x64, F * ns);
   ENS(c->q, F * ns);
   ENS(c->acc64, F * ns * 3);
+  if (c->p.precision == COORD_PREC_FP64 && c->peratom_used) ENS(c->accw64, F * ns);
   ENS(c->acc32, F * ns);
   ENS(c->nl_count, F * 4);
   ENS(c->mm, F * 6);
@@ -293,6 +295,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.fc = c->fc.p;
   a.abs_of_slot = c->abs_of_slot.p;
   a.pos = d_pos;
+  a.accw64 = c->accw64.p;
   a.cv = c->cv;
   a.charge = c->d_charge.p;
   a.ptype = c->d_ptype.p;
@@ -466,7 +469,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
       launch_allpairs64(a, c->sw, mode, c->tile64, c->ap_blocks, c->stream);
   } else {
     if (mixed) {
-      const int m = std::min(std::max(mode, 0), 2);
+      const int m = std::min(std::max(mode, 0), 4);
       const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
       launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
       launch_band_fix(a, c->sw, c->s32, mode, c->stream);
@@ -502,7 +505,7 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   // blocks per SM: up to 8 all resident at once; 16 and 32 run in waves, so
   // a few frames at a time hold L2; 0: one slice per warp
   const int bps[7] = {2, 4, 6, 8, 16, 32, 0}, unr[3] = {2, 4, 8};
-  const int m = std::min(std::max(mode, 0), 2);
+  const int m = std::min(std::max(mode, 0), 4);
   float best = 1e30f;
   int bb = c->nl_blocks, bu = c->nl_unroll;
   const bool timing = c->timing;
@@ -584,7 +587,7 @@ int sibling_upload(coord_ctx *c) {
 
 int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *boxes, int64_t step, unsigned flags,
                  double *s, double *deriv, double *virial, double *dparam, cudaStream_t stream,
-                 HostIO *hio = nullptr) {
+                 HostIO *hio = nullptr, double *peratom = nullptr) {
   if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
   if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
   if (c->cv != COORD_CV_COORDINATION && (flags & COORD_FLAG_DR0))
@@ -659,6 +662,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   double *const k_dparam = save ? c->sv_par.p : dparam;
   KArgs a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
   a.keep_acc = save ? 1 : 0;
+  a.out_peratom = peratom;
   // fused host steps leave the device copy stale: the pair kernels' rare
   // exact d_max tests read the caller's array itself
   if (hio && hio->fused) a.pos = hio->pos;
@@ -712,6 +716,7 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
         if ((rc = ensure_buffers(c, n_frames))) return rc;
         a = make_args(c, n_frames, d_pos, flags, s, k_deriv, k_virial, k_dparam);
         a.keep_acc = save ? 1 : 0;
+        a.out_peratom = peratom;
         if (attempt == 7) return c->fail(COORD_ERR_NOMEM, "neighbour list did not fit after 8 attempts");
       }
     }
@@ -719,10 +724,11 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     c->built_frames = n_frames;
   }
 
-  const int mode = (flags & COORD_FLAG_NO_DERIV) ? EVAL_S : ((flags & COORD_FLAG_DR0) ? EVAL_PARAM : EVAL_DERIV);
+  const int mode = peratom ? EVAL_PERATOM
+                           : ((flags & COORD_FLAG_NO_DERIV) ? EVAL_S : ((flags & COORD_FLAG_DR0) ? EVAL_PARAM : EVAL_DERIV));
   if (mode == EVAL_PARAM && !c->sw.grad_ok)
     return c->fail(COORD_ERR_UNSUPPORTED, "R_0/D_0 gradients are not defined for CUBIC and Q switching functions");
-  if (!c->nlm_tuned[std::min(std::max(mode, 0), 2)] && mixed && nl && c->mode != MODE_PAIR) {
+  if (!c->nlm_tuned[std::min(std::max(mode, 0), 4)] && mixed && nl && c->mode != MODE_PAIR) {
     autotune_nl(c, a, mode);
     a.partials = c->partials.p;
     a.max_blocks = c->max_blocks;
@@ -909,6 +915,7 @@ int coord_destroy(coord_ctx *c) {
   c->mm.release();
   c->pair_flag.release();
   c->acc64.release();
+  c->accw64.release();
   c->partials.release();
   c->acc32.release();
   c->tickets.release();
@@ -1075,6 +1082,85 @@ int coord_forward_device(coord_ctx *c, int n_frames, const double *pos, const do
   cudaSetDevice(c->p.device);
   DefaultStreamFence fence(c, stream);
   return forward_impl(c, n_frames, pos, boxes, step, flags, s, deriv, virial, dparam, (cudaStream_t)stream);
+}
+
+// The per-atom calls work on a COORDINATION context with a neighbour list
+// (NLIST or NLISTCELLS; PAIR has no matrix rows).
+static int peratom_check(coord_ctx *c) {
+  if (!c->groups_set) return c->fail(COORD_ERR_STATE, "coord_set_groups has not been called");
+  if (c->cv != COORD_CV_COORDINATION)
+    return c->fail(COORD_ERR_UNSUPPORTED, "per-atom coordination needs a COORDINATION context");
+  if (c->p.nlist == COORD_NL_NONE || c->mode == MODE_PAIR)
+    return c->fail(COORD_ERR_UNSUPPORTED, "per-atom coordination needs NLIST or NLISTCELLS and no PAIR");
+  c->peratom_used = true;
+  return COORD_OK;
+}
+
+int coord_peratom_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes, int64_t step,
+                         unsigned flags, double *cn, double *s, void *stream) {
+  if (!c) return COORD_ERR_ARG;
+  if (!boxes || !cn || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions, boxes or cn");
+  if (flags & ~COORD_FLAG_REBUILD) return c->fail(COORD_ERR_ARG, "per-atom forward: COORD_FLAG_REBUILD only");
+  if (int rc = peratom_check(c)) return rc;
+  cudaSetDevice(c->p.device);
+  DefaultStreamFence fence(c, stream);
+  if (c->ns == 0) return COORD_OK;
+  cudaError_t e;
+  if (!s) {
+    if ((e = c->d_s.ensure((size_t)std::max(n_frames, 1))) != cudaSuccess) return c->cuda_fail(e, "allocation");
+    s = c->d_s.p;
+  }
+  return forward_impl(c, n_frames, pos, boxes, step, flags, s, nullptr, nullptr, nullptr, (cudaStream_t)stream,
+                      nullptr, cn);
+}
+
+int coord_peratom_backward_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes,
+                                  const double *g, double *grad_pos, double *grad_box, void *stream) {
+  if (!c) return COORD_ERR_ARG;
+  if (!boxes || !g || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions, boxes or g");
+  if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
+  if (int rc = peratom_check(c)) return rc;
+  if (c->built_frames != n_frames)
+    return c->fail(COORD_ERR_STATE, "backward needs the neighbour lists of a forward call with the same frames");
+  cudaSetDevice(c->p.device);
+  if (c->ns == 0) {
+    if (grad_box) cudaMemsetAsync(grad_box, 0, sizeof(double) * 9 * n_frames, stream ? (cudaStream_t)stream : c->stream);
+    return COORD_OK;
+  }
+  DefaultStreamFence fence(c, stream);
+  cudaStream_t saved = c->stream;
+  if (stream) c->stream = (cudaStream_t)stream;
+  struct Restore {
+    coord_ctx *c;
+    cudaStream_t s;
+    ~Restore() { c->stream = s; }
+  } restore{c, saved};
+  cudaError_t e;
+  if ((e = c->d_bvir.ensure((size_t)9 * n_frames)) != cudaSuccess) return c->cuda_fail(e, "allocation");
+  if (int rc = clear_kept_acc(c)) return rc;
+  c->saved_valid = false;
+  bool need_bounds = false;
+  if (int rc = upload_frames(c, n_frames, boxes, &need_bounds)) return rc;
+  KArgs a = make_args(c, n_frames, pos, 0, nullptr, grad_pos, c->d_bvir.p, nullptr);
+  a.gslot = g;  // dV/dcn per slot: the gather puts it beside each position
+  if (need_bounds && c->p.precision == COORD_PREC_MIXED) {
+    std::vector<unsigned long long> init(6 * (size_t)n_frames);
+    for (int f = 0; f < n_frames; f++)
+      for (int k = 0; k < 6; k++) init[6 * f + k] = k < 3 ? ~0ull : 0ull;
+    if ((e = cudaMemcpyAsync(c->mm.p, init.data(), sizeof(unsigned long long) * init.size(), cudaMemcpyHostToDevice,
+                             c->stream)))
+      return c->cuda_fail(e, "bounds init");
+    launch_bounds(a, c->mm.p, c->p.nl_cutoff, 0, c->stream);
+  }
+  if (!c->nlm_tuned[EVAL_VJP] && c->p.precision == COORD_PREC_MIXED) {
+    autotune_nl(c, a, EVAL_VJP);
+    a.partials = c->partials.p;
+    a.max_blocks = c->max_blocks;
+  }
+  launch_evaluation(c, a, EVAL_VJP);
+  if (grad_box) launch_grad_post(a, c->d_bvir.p, nullptr, grad_box, nullptr, c->stream);
+  if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "per-atom backward launch");
+  return COORD_OK;
 }
 
 int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t step, unsigned flags, double *s,

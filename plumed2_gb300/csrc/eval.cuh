@@ -16,6 +16,11 @@
 
 namespace coordgpu {
 namespace {
+// CONTACT_MATRIX's weights (adjmat/ContactMatrix.h:99-107): no bond when
+// r^2 < epsilon ("atoms can't be bonded to themselves") and none, nor a
+// derivative, when sigma < epsilon; epsilon is DBL_EPSILON (tools/Tools.h).
+constexpr double kBondEps = 2.220446049250313e-16;
+
 
 __device__ __forceinline__ void vir_sub(double v[kPartials], const double dd[3], const double d[3]) {
 #pragma unroll
@@ -47,9 +52,10 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
   if (r < a.ns) {
     const FrameConst &fc = a.fc[f];
     const int len = a.row_len[fo + r];
-    const double4 xr4 = a.x64[fo + r];
+    const double4 xr4 = a.x64[fo + r];  // .w: the row's upstream g in EVAL_VJP
     const double xr[3] = {xr4.x, xr4.y, xr4.z};
     double accr[3] = {0.0, 0.0, 0.0};
+    double accw = 0.0;
     const uint32_t *e = a.ell + ((size_t)f * a.nslices + (r >> 5)) * (size_t)a.cap * 32 + lane;
     for (int k = 0; k < len; k++) {
       const uint32_t ent = __ldg(e + (size_t)k * 32);
@@ -63,7 +69,16 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
         sr = a.slot_of_rank[fo + r];
         sp = a.slot_of_rank[fo + p];
       }
-      const double sig = rfirst ? pair_fp64(a, sw, fc, xr, xp, sr, sp, d, df) : pair_fp64(a, sw, fc, xp, xr, sp, sr, d, df);
+      double sig = rfirst ? pair_fp64(a, sw, fc, xr, xp, sr, sp, d, df) : pair_fp64(a, sw, fc, xp, xr, sp, sr, d, df);
+      if (MODE >= EVAL_PERATOM && (mod2(d) < kBondEps || sig < kBondEps)) {
+        sig = 0.0;
+        df = 0.0;
+      }
+      if (MODE == EVAL_VJP) df *= xr4.w + xp4.w;
+      if (MODE == EVAL_PERATOM && sig != 0.0) {
+        atomicAdd(a.accw64 + fo + p, sig);
+        accw += sig;
+      }
       part[0] += sig;
       if (MODE >= EVAL_DERIV) {
         const double dd[3] = {df * d[0], df * d[1], df * d[2]};
@@ -82,6 +97,7 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
       double *acc = a.acc64 + (fo + r) * 3;
       for (int q = 0; q < 3; q++) atomicAdd(acc + q, accr[q]);
     }
+    if (MODE == EVAL_PERATOM && accw != 0.0) atomicAdd(a.accw64 + fo + r, accw);
   }
   block_partials_finish(a, f, part, gridDim.x);
 }
@@ -178,11 +194,13 @@ __device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) 
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Fire-and-forget vector reduction into a float4 accumulator (16-byte aligned).
-__device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z), "f"(0.f)
+// Fire-and-forget vector reduction into a float4 accumulator (16-byte aligned);
+// w carries the per-atom sums of sigma in EVAL_PERATOM.
+__device__ __forceinline__ void red_add_v4(float4 *p, float x, float y, float z, float w = 0.f) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z), "f"(w)
                : "memory");
 }
+
 
 // Bytes per frame of band_flag: slices rounded up to 32 (16-byte vector loads).
 __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)a.nslices + 31) & ~(size_t)31; }
@@ -230,20 +248,32 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
       if (wn > 0) prefetch_l2_bulk(ell_f + (size_t)(slice + nw) * slice_words, (uint32_t)wn * 128u);
     }
     const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+    const float gr = __uint_as_float(qr.w);  // EVAL_VJP: the row's upstream g
     const uint32_t *__restrict__ e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
     // one pair inside d_max: s, the two derivatives (d = x_p - x_r:
-    // deriv[r] -= df d, deriv[p] += df d, either orientation), the virial
-    auto pair = [&](int p, float dx, float dy, float dz, float r2) {
+    // deriv[r] -= df d, deriv[p] += df d, either orientation), the virial;
+    // gpw: the partner's q.w
+    auto pair = [&](int p, float dx, float dy, float dz, float r2, uint32_t gpw) {
       float sig, df;
       sw32<NH>(sw, s32, r2, sig, df);
+      if (MODE >= EVAL_PERATOM && (r2 < (float)kBondEps || sig < (float)kBondEps)) {
+        sig = 0.f;
+        df = 0.f;
+      }
+      if (MODE == EVAL_VJP) df *= gr + __uint_as_float(gpw);
       acc.add_s(sig);
       if (MODE >= EVAL_DERIV) {
         const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
         ax -= ddx;
         ay -= ddy;
         az -= ddz;
-        red_add_v4(acc4 + p, ddx, ddy, ddz);
+        if (MODE == EVAL_PERATOM) {
+          aw += sig;
+          red_add_v4(acc4 + p, ddx, ddy, ddz, sig);
+        } else {
+          red_add_v4(acc4 + p, ddx, ddy, ddz);
+        }
         acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
       }
       if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
@@ -271,13 +301,13 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
         const float dz = fixed_delta(qr.z, qp[u].z, sz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         if (p[u] >= 0 && r2 <= s32.dmax2_lo)
-          pair(p[u], dx, dy, dz, r2);
+          pair(p[u], dx, dy, dz, r2, qp[u].w);
         else
           band_min = min(band_min, __float_as_uint(r2) - band_lo);
       }
     }
     if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
-    if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az);
+    if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
   }
   double part[kPartials];
   acc.to_partials(part);
@@ -319,7 +349,7 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
     const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
     const uint32_t *e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
     Acc32 acc;
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
     constexpr int kU = 8;  // entries and partner positions in flight per lane
     for (int k0 = 0; k0 < len; k0 += kU) {
       uint32_t en[kU];
@@ -342,19 +372,26 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
         if (!in) continue;
         float sig, df;
         sw32<NH>(sw, s32, s32.dmax2, sig, df);
+        if (MODE >= EVAL_PERATOM && sig < (float)kBondEps) {
+          sig = 0.f;
+          df = 0.f;
+        }
+        if (MODE == EVAL_VJP) df *= __uint_as_float(qr.w) + __uint_as_float(qq[u].w);
         acc.add_s(sig);
         if (MODE >= EVAL_DERIV) {
           const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
           ax -= ddx;
           ay -= ddy;
           az -= ddz;
-          red_add_v4(acc4 + p, ddx, ddy, ddz);
+          aw += sig;
+          red_add_v4(acc4 + p, ddx, ddy, ddz, MODE == EVAL_PERATOM ? sig : 0.f);
           acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
         }
         if (MODE == EVAL_PARAM) acc.add_param(s32, s32.dmax2, sig, df);
       }
     }
-    if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f)) red_add_v4(acc4 + r, ax, ay, az);
+    if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f || aw != 0.f))
+      red_add_v4(acc4 + r, ax, ay, az, MODE == EVAL_PERATOM ? aw : 0.f);
     double part[kPartials];
     acc.to_partials(part);
     double *rec = a.band_rec + ((size_t)f * a.nslices + slice) * kPartials;
@@ -661,7 +698,7 @@ template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, 
 __global__ void k_grad_post(KArgs a, const double *vir, const double *dpar, double *grad_box, double *grad_param) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= a.nframes) return;
-  const double g = a.g[f];
+  const double g = a.g ? a.g[f] : 1.0;
   const FrameConst &fc = a.fc[f];
   if (grad_box) {
     const double *B = vir + (size_t)f * 9;

@@ -95,7 +95,12 @@ void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaSt
 
 void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStream_t s) {
 #define CALL(M) k_eval_nl64<M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw)
-  MODE_DISPATCH(mode, CALL)
+  if (mode == EVAL_PERATOM)
+    CALL(EVAL_PERATOM);
+  else if (mode == EVAL_VJP)
+    CALL(EVAL_VJP);
+  else
+    MODE_DISPATCH(mode, CALL)
 #undef CALL
   g_launches += 1;
 }

@@ -38,6 +38,22 @@ int mixed_nh(const SwitchParams &sw) {
     }                                        \
   } while (0)
 
+// The neighbour-list kernels also run the per-atom modes, compiled for
+// fixedRational<6> and the generic evaluator only.
+#define NH_MODE_DISPATCH_NL(NHV, M, CALL)                 \
+  do {                                                   \
+    const int nhn_ = (NHV), mn_ = (M);                   \
+    if (mn_ == EVAL_PERATOM) {                           \
+      if (nhn_ == 3) CALL(3, EVAL_PERATOM);              \
+      else CALL(0, EVAL_PERATOM);                        \
+    } else if (mn_ == EVAL_VJP) {                        \
+      if (nhn_ == 3) CALL(3, EVAL_VJP);                  \
+      else CALL(0, EVAL_VJP);                            \
+    } else {                                             \
+      NH_MODE_DISPATCH(nhn_, mn_, CALL);                 \
+    }                                                    \
+  } while (0)
+
 static int nh_compiled(const SwitchParams &sw) {
   const int nh = mixed_nh(sw);
   return (nh == 2 || nh == 3 || nh == 4 || nh == 6) ? nh : 0;
@@ -51,15 +67,15 @@ void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s
   const dim3 g(per_frame, a.nframes);
   if (unroll >= 8) {
 #define CALL(N, M) k_eval_nl32<N, M, 8><<<g, 256, 0, s>>>(a, sw, s32)
-    NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
+    NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);
 #undef CALL
   } else if (unroll <= 2) {
 #define CALL(N, M) k_eval_nl32<N, M, 2><<<g, 256, 0, s>>>(a, sw, s32)
-    NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
+    NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);
 #undef CALL
   } else {
 #define CALL(N, M) k_eval_nl32<N, M, 4><<<g, 256, 0, s>>>(a, sw, s32)
-    NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
+    NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);
 #undef CALL
   }
   g_launches += 1;
@@ -70,7 +86,7 @@ void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s3
   const int chunks = (a.nslices + 31) / 32;  // one warp per 32 slices
   const dim3 g(std::max(1, std::min((chunks + 7) / 8, 64)), a.nframes);
 #define CALL(N, M) k_band_fix<N, M><<<g, 256, 0, s>>>(a, sw, s32)
-  NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
+  NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);
 #undef CALL
   g_launches += 1;
 }

@@ -59,6 +59,10 @@ struct KArgs {
   double *out_virial;           // [nframes][9]
   double *out_dparam;           // [nframes][2]
   const double *g;              // [nframes] upstream dV/ds (backward)
+  // per-atom coordination (EVAL_PERATOM / EVAL_VJP)
+  double *out_peratom;          // [nframes][ns] slot order: sum of sigma over the slot's pairs
+  double *accw64;               // [nframes][ns] FP64 path: those sums in rank order
+  const double *gslot;          // [nframes][ns] slot order: upstream dV/dcn per slot (EVAL_VJP)
   // the CV's pairing() (COORD_CV_*): the switching function for COORDINATION,
   // or a sibling of CoordinationBase with its per-slot data
   int cv;
@@ -83,9 +87,11 @@ struct SwitchF32 {
 
 // What a pair kernel accumulates.
 enum EvalMode : int {
-  EVAL_S = 0,      // s only
-  EVAL_DERIV = 1,  // s, ds/dx, virial
-  EVAL_PARAM = 2   // s, ds/dx, virial, ds/dR_0, ds/dD_0
+  EVAL_S = 0,        // s only
+  EVAL_DERIV = 1,    // s, ds/dx, virial
+  EVAL_PARAM = 2,    // s, ds/dx, virial, ds/dR_0, ds/dD_0
+  EVAL_PERATOM = 3,  // EVAL_DERIV plus the per-atom sums of sigma (coordination numbers)
+  EVAL_VJP = 4       // per-atom backward: each pair's derivative weighted by g_i + g_j
 };
 
 } // namespace coordgpu

@@ -441,10 +441,14 @@ __global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wan
   if (wantcell) a.cell_of_rank[(size_t)f * a.ns + r] = a.cell_of_slot[(size_t)f * a.ns + s];
   const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
   const double x0 = x[0], x1 = x[1], x2 = x[2];
-  if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, 0.0);
+  // the per-atom backward's upstream g rides in the spare fourth component
+  const double gw = a.gslot ? a.gslot[(size_t)f * a.ns + s] : 0.0;
+  if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, gw);
   if (wantq) {
     const double xx[3] = {x0, x1, x2};
-    a.q[(size_t)f * a.ns + r] = fixed_of(a.fc[f], xx);
+    uint4 qq = fixed_of(a.fc[f], xx);
+    qq.w = __float_as_uint((float)gw);
+    a.q[(size_t)f * a.ns + r] = qq;
   }
 }
 
@@ -965,6 +969,10 @@ __global__ void k_finalize64(KArgs a, int rank_order) {
     o[1] = g * acc[1];
     o[2] = g * acc[2];
   }
+  if (a.out_peratom) {
+    a.out_peratom[fo + s] = a.accw64[fo + r];
+    a.accw64[fo + r] = 0.0;
+  }
   if (!a.keep_acc) {
     acc[0] = 0.0;
     acc[1] = 0.0;
@@ -985,6 +993,7 @@ __global__ void k_finalize32(KArgs a, int rank_order) {
     o[1] = g * (double)v.y;
     o[2] = g * (double)v.z;
   }
+  if (a.out_peratom) a.out_peratom[fo + s] = (double)v.w;
   if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 

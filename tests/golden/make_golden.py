@@ -23,6 +23,10 @@ so that the tests run where the reference tree is absent.  Sources:
 * regtest/basic/rt-ghbfix               GHBFIX PAIR of two atoms 0.002*i apart
   (the regtest's own generated trajectory), typesTable.dat and
   scalingParameters.dat as text: colvar.reference, der.reference
+* regtest/symfunc/rt-dumpmulti          COORDINATIONNUMBER SPECIES=1-64 of
+  regtest/trajectories/64.xyz: coordination.xyz.reference (per-atom values)
+* regtest/symfunc/rt-single-groupb      COORDINATIONNUMBER SPECIESA=1-5
+  SPECIESB=6 over trajectory.xyz: colvar.reference
 """
 from __future__ import annotations
 
@@ -191,6 +195,22 @@ def main(ref):
                "c1_minus_ghbfix": 4.184, "colvar_c1": [r[2] for r in colvar], "deriv_ghbfix": der,
                "fmt": "%8.4f"},
               open(os.path.join(HERE, "rt_ghbfix.json"), "w"))
+    # --- COORDINATIONNUMBER: rt-dumpmulti, rt-single-groupb ---------------------
+    f64, b64 = read_xyz(os.path.join(reg, "trajectories", "64.xyz"))
+    cref = [float(l.split()[4]) for l in open(os.path.join(reg, "symfunc", "rt-dumpmulti",
+                                                           "coordination.xyz.reference")).read().split("\n")[2:]
+            if l.strip()]
+    ftr, btr = read_xyz(os.path.join(reg, "trajectories", "trajectory.xyz"))
+    sg = read_table(os.path.join(reg, "symfunc", "rt-single-groupb", "colvar.reference"))
+    json.dump({"source": "regtest/symfunc/rt-dumpmulti (plumed.dat, coordination.xyz.reference), "
+                         "regtest/trajectories/64.xyz, regtest/symfunc/rt-single-groupb (plumed.dat, "
+                         "colvar.reference), regtest/trajectories/trajectory.xyz",
+               "dumpmulti": {"spec": "RATIONAL D_0=3.0 R_0=1.5", "species": "1-64", "pos": f64[0], "box": b64[0],
+                             "cn": cref, "fmt": "%.4f"},
+               "single_groupb": {"spec": "RATIONAL R_0=1.0", "speciesa": "1-5", "speciesb": "6",
+                                 "frames": [fr[:6] for fr in ftr], "box": btr, "cn": [r[1:] for r in sg],
+                                 "fmt": "%8.4f"}},
+              open(os.path.join(HERE, "rt_peratom.json"), "w"))
     print("fixtures written to", HERE)
 
 

@@ -185,3 +185,19 @@ def test_rt_ghbfix(orc, golden):
         assert abs(s + g["c1_minus_ghbfix"] - g["colvar_c1"][i - 1]) <= 5.01e-5, i
         got = np.concatenate([d.reshape(-1), v.reshape(-1)])
         assert np.abs(got - np.array(g["deriv_ghbfix"][i - 1])).max() <= 5.01e-5, i
+
+
+def test_rt_peratom_coordination(orc, golden):
+    """regtest/symfunc/rt-dumpmulti (64 per-atom coordination numbers, %.4f)
+    and rt-single-groupb (SPECIESA=1-5 SPECIESB=6 over five frames, %8.4f):
+    CONTACT_MATRIX times ones, every pair (no D_MAX)."""
+    import oracle
+    g = golden("rt_peratom.json")
+    d = g["dumpmulti"]
+    cn = orc.peratom(d["spec"], d["pos"], np.diag(d["box"]), orc.all_pairs(oracle.MODE_SINGLE, 64))
+    assert np.abs(cn - np.array(d["cn"])).max() <= 5.01e-5
+    sgb = g["single_groupb"]
+    assert len(sgb["frames"]) == 5
+    for fi, (fr, bx) in enumerate(zip(sgb["frames"], sgb["box"])):
+        cn = orc.peratom(sgb["spec"], fr, np.diag(bx), orc.all_pairs(oracle.MODE_TWO, 5, 1))
+        assert np.abs(cn[:5] - np.array(sgb["cn"][fi])).max() <= 5.01e-5, fi
