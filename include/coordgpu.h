@@ -242,6 +242,37 @@ int coord_multi_forward_device(coord_multi *m, int n_frames, const double *pos, 
 int coord_multi_use_graph(coord_multi *m, int enable);
 const char *coord_multi_last_error(const coord_multi *m);
 
+/* ---- CONTACTMAP (colvar/ContactMap.cpp:149-365) ----------------------------
+ * Explicit contacts i = (ATOMSi[0], ATOMSi[1]), each with its switching
+ * function (one SWITCH for all, or SWITCHi), REFERENCEi (default 0) and
+ * WEIGHTi (default 1):  c_i = w_i (sigma_i(|d|) - ref_i), sigma from
+ * SwitchingFunction::calculate of the minimum-image distance.
+ *   COORD_CMAP_COMPONENTS  value[f][i] = c_i (components contact-i),
+ *                          virial[f][i][9] the box derivatives of c_i
+ *   COORD_CMAP_SUM         value[f] = sum_i c_i, virial[f][9]
+ *   COORD_CMAP_CMDIST      value[f] = sum_i c_i^2, virial[f][9]
+ * Positions are [frames][2n][3]: the first atoms of all contacts, then the
+ * second atoms (the reference's request order); deriv [frames][2n][3] gets
+ * the derivative of the contact's value (components) or of the sum for each
+ * slot.  boxes: host [frames][9].  FP64.  Replaces ContactMap::ContactMap
+ * and ContactMap::calculate. */
+#define COORD_CMAP_COMPONENTS 0
+#define COORD_CMAP_SUM 1
+#define COORD_CMAP_CMDIST 2
+typedef struct coord_cmap coord_cmap;
+int coord_cmap_create(int64_t n_contacts, const char *const *switch_defs, int n_switch_defs, const double *reference,
+                      const double *weight, int mode, int nopbc, int device, coord_cmap **out);
+int coord_cmap_destroy(coord_cmap *m);
+const char *coord_cmap_last_error(const coord_cmap *m);
+/* value and virial as above; deriv and virial may be NULL.  Calls on one
+ * context are ordered on their stream (NULL: the legacy default stream). */
+int coord_cmap_forward_device(coord_cmap *m, int n_frames, const double *pos, const double *boxes, double *value,
+                              double *deriv, double *virial, void *stream);
+/* One frame from host arrays (the plugin's call): pos (2n x 3), box[9];
+ * value, deriv (2n x 3) and virial as above, on the host. */
+int coord_cmap_forward(coord_cmap *m, const double *pos, const double box[9], double *value, double *deriv,
+                       double *virial);
+
 /* ---- forward without device allocation ------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they call in (an MD engine that reserves its whole device pool

@@ -113,6 +113,8 @@ class Oracle:
         L.orc_pairing_eval.restype = C.c_double
         L.orc_cv.argtypes = [C.POINTER(_Pairing), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp, _u32p,
                              C.c_int64, C.POINTER(C.c_double), _dp, _dp, C.c_int]
+        L.orc_contactmap.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, C.c_int, C.POINTER(_Pbc), C.c_int, _dp,
+                                     _dp, _dp, _dp]
         L.orc_peratom.argtypes = [C.POINTER(_Switch), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp, _u32p,
                                   C.c_int64, C.c_void_p, _dp, C.c_void_p, C.c_void_p]
 
@@ -285,6 +287,25 @@ class Oracle:
         if gg is None:
             return cn
         return cn, grad.reshape(n, 3), vir.reshape(3, 3)
+
+    def contactmap(self, specs, pos, box, reference=None, weight=None, mode=0, do_pbc=True):
+        """CONTACTMAP over contacts (slot i, slot n + i) of pos (2n x 3): (value, deriv
+        (2n x 3), virial (n x 3 x 3) for components, (3 x 3) otherwise).  specs: one
+        switch definition or one per contact."""
+        pos = np.ascontiguousarray(np.asarray(pos, np.float64).reshape(-1, 3))
+        n = len(pos) // 2
+        specs = [specs] if isinstance(specs, str) else list(specs)
+        sws = (_Switch * len(specs))(*[self.switch(sp) for sp in specs])
+        ref = np.ascontiguousarray(np.zeros(n) if reference is None else reference, np.float64)
+        w = np.ascontiguousarray(np.ones(n) if weight is None else weight, np.float64)
+        pb = self.pbc(box)
+        nv = n if mode == 0 else 1
+        value = np.zeros(nv)
+        deriv = np.zeros(6 * n)
+        vir = np.zeros(9 * nv)
+        self.L.orc_contactmap(C.cast(sws, C.c_void_p), len(specs), n, ref, w, int(mode), C.byref(pb), int(do_pbc),
+                              pos.reshape(-1), value, deriv, vir)
+        return value, deriv.reshape(2 * n, 3), (vir.reshape(n, 3, 3) if mode == 0 else vir.reshape(3, 3))
 
     def max_threads(self) -> int:
         return self.L.orc_max_threads()

@@ -1186,6 +1186,43 @@ int orc_peratom(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t ns
   return 0;
 }
 
+int orc_contactmap(const orc_switch *sw, int nsw, int64_t n, const double *reference, const double *weight, int mode,
+                   const orc_pbc *pbc, int do_pbc, const double *pos, double *value, double *deriv, double *vir) {
+  const int nv = mode == 0 ? (int)n : 1;
+  for (int64_t i = 0; i < (mode == 0 ? n : 1); i++) value[i] = 0.0;
+  for (int64_t i = 0; i < 6 * n; i++) deriv[i] = 0.0;
+  for (int64_t i = 0; i < 9 * (int64_t)nv; i++) vir[i] = 0.0;
+  double ncoord = 0.;
+  for (int64_t i = 0; i < n; i++) {
+    const int64_t i0 = i, i1 = n + i;
+    double distance[3];
+    pair_distance(pbc, do_pbc, pos, i0, i1, distance);
+    double dfunc = 0.;
+    const double coord = weight[i] * (orc_switch_calculate(&sw[nsw == 1 ? 0 : i], sqrt(mod2(distance)), &dfunc) -
+                                      reference[i]);
+    double tmpder[3], tmpvir[9];
+    for (int k = 0; k < 3; k++) tmpder[k] = weight[i] * dfunc * distance[k];
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) tmpvir[3 * a + b] = weight[i] * dfunc * (distance[a] * distance[b]);
+    if (mode == 2) {
+      for (int k = 0; k < 3; k++) tmpder[k] *= 2. * coord;
+      for (int k = 0; k < 9; k++) tmpvir[k] *= 2. * coord;
+    }
+    for (int k = 0; k < 3; k++) {
+      deriv[3 * i0 + k] -= tmpder[k];
+      deriv[3 * i1 + k] += tmpder[k];
+    }
+    double *v = vir + (mode == 0 ? 9 * i : 0);
+    for (int k = 0; k < 9; k++) v[k] -= tmpvir[k];
+    if (mode == 0)
+      value[i] = coord;
+    else
+      ncoord += mode == 2 ? coord * coord : coord;
+  }
+  if (mode != 0) value[0] = ncoord;
+  return 0;
+}
+
 int orc_coordination(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t nslots,
                      const int64_t *abs_index, const double *pos, const uint32_t *pairs, int64_t npairs, double *s,
                      double *deriv, double virial[9], int nthreads) {

@@ -152,6 +152,17 @@ int orc_peratom(const orc_switch *sw, const orc_pbc *pbc, int do_pbc, int64_t ns
                 const double *pos, const uint32_t *pairs, int64_t npairs, const double *g, double *cn, double *grad,
                 double virial[9]);
 
+/* ---- CONTACTMAP (colvar/ContactMap.cpp:149-365) ----------------------------
+ * n contacts (first, second) = slots (i, n + i); contact i uses switch
+ * sw[nsw == 1 ? 0 : i], reference[i], weight[i]:
+ *   c_i = weight_i * (sigma_i(|d|) - reference_i)   (SwitchingFunction::calculate)
+ * mode 0 (components): value[i] = c_i, vir[9 i..] = -tmpvir of contact i;
+ * mode 1 (SUM): value[0] = sum c_i; mode 2 (CMDIST): value[0] = sum c_i^2
+ * (derivatives times 2 c_i).  deriv is (2n x 3): -/+ tmpder for the two slots;
+ * vir is 9 values per contact (mode 0) or 9 in total. */
+int orc_contactmap(const orc_switch *sw, int nsw, int64_t n, const double *reference, const double *weight, int mode,
+                   const orc_pbc *pbc, int do_pbc, const double *pos, double *value, double *deriv, double *vir);
+
 /* Number of OpenMP threads available (1 without OpenMP). */
 int orc_max_threads(void);
 

@@ -27,6 +27,7 @@ COORD_ERR_STATE = 7
 NL_NONE, NL_CLASSIC, NL_CELLS = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 CV_COORDINATION, CV_DHENERGY, CV_GHBFIX = 0, 1, 2
+CMAP_COMPONENTS, CMAP_SUM, CMAP_CMDIST = 0, 1, 2
 FLAG_REBUILD, FLAG_NO_DERIV, FLAG_DR0, FLAG_SAVE = 1, 2, 4, 8
 
 
@@ -78,6 +79,12 @@ def load() -> C.CDLL:
         L.coord_get_nslots.argtypes = [_vp, C.POINTER(C.c_int64)]
         L.coord_set_dhenergy.argtypes = [_vp] + [C.c_double] * 6
         L.coord_set_charges.argtypes = [_vp, _dp, C.c_int64]
+        L.coord_cmap_create.argtypes = [C.c_int64, C.POINTER(C.c_char_p), C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(_vp)]
+        L.coord_cmap_destroy.argtypes = [_vp]
+        L.coord_cmap_last_error.argtypes = [_vp]
+        L.coord_cmap_last_error.restype = C.c_char_p
+        L.coord_cmap_forward_device.argtypes = [_vp, C.c_int, _vp, _dp, _vp, _vp, _vp, _vp]
         L.coord_peratom_device.argtypes = [_vp, C.c_int, _vp, _dp, C.c_int64, C.c_uint, _vp, _vp, _vp]
         L.coord_peratom_backward_device.argtypes = [_vp, C.c_int, _vp, _dp, _vp, _vp, _vp, _vp]
         L.coord_set_ghbfix.argtypes = [_vp, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int32), C.c_int64, _dp,

@@ -515,3 +515,146 @@ class CoordinationNumbers:
         if self._act is not None:
             self._act.close()
             self._act = None
+
+
+class ContactMap:
+    """CONTACTMAP (colvar/ContactMap.cpp:149-365) on the GPU.
+
+        cm = ContactMap("ATOMS1=1,2 ATOMS2=5,9 SWITCH={RATIONAL R_0=0.5} SUM")
+        value, deriv, virial = cm.calculate(positions, box)
+
+    Keywords as the reference reads them: ATOMSn (two atoms each, numbered
+    from 1 until one is missing); SWITCHn for every contact, or one SWITCH;
+    REFERENCEn or REFERENCE (default 0); WEIGHTn or WEIGHT (default 1); flags
+    SUM, CMDIST (not both), NOPBC, SERIAL.  positions are the requested atoms:
+    the first atoms of all contacts, then the second atoms.  Without SUM or
+    CMDIST, value holds one component per contact (contact-n) and virial one
+    box derivative per contact."""
+
+    FLAGS = ("SUM", "CMDIST", "NOPBC", "SERIAL")
+
+    def __init__(self, line: str = "", *, device: int = 0):
+        opts, flags = {}, set()
+        for w in split_line(line):
+            if w.endswith(":") and not opts and not flags:
+                opts["LABEL"] = w[:-1]
+                continue
+            if w == "CONTACTMAP":
+                continue
+            if "=" in w:
+                k, v = w.split("=", 1)
+                if v.startswith("{") and v.endswith("}"):
+                    v = v[1:-1]
+                opts[k.upper()] = v
+            else:
+                if w.upper() not in self.FLAGS:
+                    raise ValueError("cannot read flag %s" % w)
+                flags.add(w.upper())
+        self.label = opts.pop("LABEL", None)
+        dosum, docmdist = "SUM" in flags, "CMDIST" in flags
+        if dosum and docmdist:
+            raise ValueError("You cannot use SUM and CMDIST together")
+        first, second = [], []
+        i = 1
+        while "ATOMS%d" % i in opts:
+            at = parse_atom_list(opts.pop("ATOMS%d" % i))
+            if len(at) != 2:
+                raise ValueError("ATOMS%d keyword has the wrong number of atoms" % i)
+            first.append(at[0])
+            second.append(at[1])
+            i += 1
+        n = len(first)
+        if n == 0:
+            raise ValueError("no contacts: use ATOMS1, ATOMS2, ...")
+        sws = []
+        for i in range(1, n + 1):
+            if "SWITCH%d" % i not in opts:
+                break
+            sws.append(opts.pop("SWITCH%d" % i))
+        if not sws:
+            if "SWITCH" not in opts:
+                raise ValueError("no switching function specified use SWITCH keyword")
+            sws = [opts.pop("SWITCH")]
+        elif len(sws) != n:
+            raise ValueError("missing SWITCH%d keyword" % (len(sws) + 1))
+        ref = np.zeros(n)
+        counted = 0
+        for i in range(1, n + 1):
+            if "REFERENCE%d" % i not in opts:
+                break
+            ref[i - 1] = float(opts.pop("REFERENCE%d" % i))
+            counted += 1
+        if counted == 0:
+            ref[:] = float(opts.pop("REFERENCE", 0.0))
+            counted = n - 1  # the reference copies REFERENCE into contacts 2..n
+        if counted == 0 and docmdist:
+            raise ValueError("with CMDIST one must use REFERENCE to setup the reference contact map")
+        w = np.ones(n)
+        counted = 0
+        for i in range(1, n + 1):
+            if "WEIGHT%d" % i not in opts:
+                break
+            w[i - 1] = float(opts.pop("WEIGHT%d" % i))
+            counted += 1
+        if counted == 0:
+            w[:] = float(opts.pop("WEIGHT", 1.0))
+        for k in opts:
+            raise ValueError("cannot read keyword %s" % k)
+        self.first, self.second = first, second
+        self.n = n
+        self.mode = _lib.CMAP_CMDIST if docmdist else (_lib.CMAP_SUM if dosum else _lib.CMAP_COMPONENTS)
+        self.reference, self.weight = ref, w
+        self.switches = sws
+        self.device = device
+        self._L = _lib.load()
+        self._m = C.c_void_p()
+        defs = (C.c_char_p * len(sws))(*[s.encode() for s in sws])
+        rc = self._L.coord_cmap_create(n, defs, len(sws), dptr(ref), dptr(w), self.mode, int("NOPBC" in flags), device,
+                                       C.byref(self._m))
+        if rc:
+            msg = self._L.coord_cmap_last_error(self._m).decode()
+            self.close()
+            raise ValueError(msg) if rc == _lib.COORD_ERR_ARG else CoordError(rc, msg)
+
+    @property
+    def requested_atoms(self) -> List[int]:
+        return list(self.first) + list(self.second)
+
+    def forward_device(self, pos_ptr: int, boxes, n_frames: int, value_ptr: int, deriv_ptr: int = 0,
+                       virial_ptr: int = 0, stream: int = 0):
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 9))
+        rc = self._L.coord_cmap_forward_device(self._m, int(n_frames), C.c_void_p(pos_ptr), dptr(bx),
+                                               C.c_void_p(value_ptr), C.c_void_p(deriv_ptr or None),
+                                               C.c_void_p(virial_ptr or None), C.c_void_p(stream or None))
+        if rc:
+            raise CoordError(rc, self._L.coord_cmap_last_error(self._m).decode())
+
+    def calculate(self, positions, box):
+        """(value, deriv (2n x 3), virial): value and virial per contact
+        without SUM/CMDIST ((n,), (n, 3, 3)), else a float and (3, 3)."""
+        import torch
+        dev = "cuda:%d" % self.device
+        pos = torch.as_tensor(np.ascontiguousarray(np.asarray(positions, np.float64).reshape(1, -1, 3)), device=dev)
+        if pos.shape[1] != 2 * self.n:
+            raise ValueError("expected %d positions, got %d" % (2 * self.n, pos.shape[1]))
+        nv = self.n if self.mode == _lib.CMAP_COMPONENTS else 1
+        value = torch.empty(nv, dtype=torch.float64, device=dev)
+        deriv = torch.empty(2 * self.n, 3, dtype=torch.float64, device=dev)
+        vir = torch.empty(nv, 9, dtype=torch.float64, device=dev)
+        self.forward_device(pos.data_ptr(), np.asarray(box, np.float64).reshape(1, 9), 1, value.data_ptr(),
+                            deriv.data_ptr(), vir.data_ptr())
+        v, d, w = value.cpu().numpy(), deriv.cpu().numpy(), vir.cpu().numpy().reshape(nv, 3, 3)
+        if self.mode == _lib.CMAP_COMPONENTS:
+            return v, d, w
+        return float(v[0]), d, w[0]
+
+    def close(self):
+        if getattr(self, "_m", None) is not None and self._m.value:
+            self._L.coord_cmap_destroy(self._m)
+            self._m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

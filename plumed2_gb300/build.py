@@ -30,6 +30,7 @@ SOURCES = {
     "peaks.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "bias.cu": ["-fmad=false"],
+    "contactmap.cu": ["-fmad=false"],
     "host_setup.cpp": [],
 }
 HEADERS = ["coord_internal.h", "switch_eval.cuh", "kargs.h", "kernels.cuh", "eval.cuh", "launch.h"]

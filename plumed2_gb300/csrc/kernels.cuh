@@ -23,6 +23,7 @@
 //             (orthorhombic) or of a bounding frame (no pbc): differences
 //             wrap modulo 2^32, which is exactly the minimum image.
 #pragma once
+#include "coordgpu.h"
 #include "coord_internal.h"
 #include "switch_eval.cuh"
 #include "kargs.h"

@@ -387,5 +387,155 @@ GHBFIXGPU::GHBFIXGPU(const ActionOptions &ao) : Action(ao), PairLoopGPU(ao) {
   check(coord_set_ghbfix(ctx, d0, dmax, c, table.data(), (int64_t)table.size(), eta.data(), n), "GHBFIX");
 }
 
+// ---- CONTACTMAP (colvar/ContactMap.cpp:118-365) ------------------------------
+class ContactMapGPU : public Colvar {
+  coord_cmap *cm = nullptr;
+  unsigned n = 0;
+  bool docomp = true;
+  std::vector<double> pos, value, deriv, vir;
+
+public:
+  explicit ContactMapGPU(const ActionOptions &);
+  ~ContactMapGPU() override { coord_cmap_destroy(cm); }
+  static void registerKeywords(Keywords &keys);
+  void calculate() override;
+};
+
+PLUMED_REGISTER_ACTION(ContactMapGPU, "CONTACTMAP")
+PLUMED_REGISTER_ACTION(ContactMapGPU, "CONTACTMAP_GPU")
+
+// ContactMap::registerKeywords (ContactMap.cpp:120-145)
+void ContactMapGPU::registerKeywords(Keywords &keys) {
+  Colvar::registerKeywords(keys);
+  keys.add("numbered", "ATOMS", "the atoms involved in each of the contacts you wish to calculate");
+  keys.reset_style("ATOMS", "atoms");
+  keys.add("numbered", "SWITCH", "the switching function of each contact, or one SWITCH for all");
+  keys.add("numbered", "REFERENCE", "the reference value of each contact (default 0.0), or one REFERENCE for all");
+  keys.add("numbered", "WEIGHT", "the weight of each contact (default 1.0), or one WEIGHT for all");
+  keys.reset_style("SWITCH", "compulsory");
+  keys.addFlag("SUM", false, "calculate the sum of all the contacts in the input");
+  keys.addFlag("CMDIST", false, "calculate the distance with respect to the provided reference contact map");
+  keys.addFlag("SERIAL", false, "Perform the calculation in serial - for debug purpose");
+  keys.add("compulsory", "DEVICE", "0", "CUDA device");
+  keys.addOutputComponent("contact", "default", "scalar", "By not using SUM or CMDIST each contact will be stored in a component");
+  keys.setValueDescription("scalar", "the sum of all the switching function on all the distances");
+}
+
+// ContactMap::ContactMap (ContactMap.cpp:147-287): the same reading order,
+// defaults and messages
+ContactMapGPU::ContactMapGPU(const ActionOptions &ao) : PLUMED_COLVAR_INIT(ao) {
+  bool serial = false, dosum = false, docmdist = false, nopbc = false;
+  parseFlag("SERIAL", serial);
+  parseFlag("SUM", dosum);
+  parseFlag("CMDIST", docmdist);
+  if (docmdist && dosum) error("You cannot use SUM and CMDIST together");
+  parseFlag("NOPBC", nopbc);
+  std::vector<AtomNumber> t, ga, gb;
+  for (int i = 1;; ++i) {
+    parseAtomList("ATOMS", i, t);
+    if (t.empty()) break;
+    if (t.size() != 2) error("ATOMS" + std::to_string(i) + " keyword has the wrong number of atoms");
+    ga.push_back(t[0]);
+    gb.push_back(t[1]);
+    t.resize(0);
+    if (!dosum && !docmdist) {
+      addComponentWithDerivatives("contact-" + std::to_string(i));
+      componentIsNotPeriodic("contact-" + std::to_string(i));
+    }
+  }
+  n = ga.size();
+  std::vector<std::string> sws;
+  for (unsigned i = 0; i < n; ++i) {
+    std::string sw1;
+    if (!parseNumbered("SWITCH", i + 1, sw1)) break;
+    sws.push_back(sw1);
+  }
+  if (sws.empty()) {
+    std::string sw;
+    parse("SWITCH", sw);
+    if (sw.empty()) error("no switching function specified use SWITCH keyword");
+    sws.push_back(sw);
+  } else if (sws.size() != n) {
+    error("missing SWITCH" + std::to_string(sws.size() + 1) + " keyword");
+  }
+  std::vector<double> reference(n, 0.), weight(n, 1.0);
+  unsigned counted = 0;
+  for (unsigned i = 0; i < n; ++i) {
+    if (!parseNumbered("REFERENCE", i + 1, reference[i])) break;
+    counted++;
+  }
+  if (counted == 0) {
+    parse("REFERENCE", reference[0]);
+    for (unsigned i = 1; i < n; ++i) {
+      reference[i] = reference[0];
+      counted++;
+    }
+  }
+  if (counted == 0 && docmdist) error("with CMDIST one must use REFERENCE to setup the reference contact map");
+  counted = 0;
+  for (unsigned i = 0; i < n; ++i) {
+    if (!parseNumbered("WEIGHT", i + 1, weight[i])) break;
+    counted++;
+  }
+  if (counted == 0) {
+    parse("WEIGHT", weight[0]);
+    for (unsigned i = 1; i < n; ++i) weight[i] = weight[0];
+  }
+  int device = 0;
+  parse("DEVICE", device);
+  if (dosum || docmdist) {
+    addValueWithDerivatives();
+    setNotPeriodic();
+  }
+  docomp = !(dosum || docmdist);
+  std::vector<AtomNumber> full = ga;
+  full.insert(full.end(), gb.begin(), gb.end());
+  requestAtoms(full);
+  checkRead();
+  std::vector<const char *> defs;
+  for (const auto &s : sws) defs.push_back(s.c_str());
+  const int mode = docmdist ? COORD_CMAP_CMDIST : (dosum ? COORD_CMAP_SUM : COORD_CMAP_COMPONENTS);
+  if (coord_cmap_create((int64_t)n, defs.data(), (int)defs.size(), reference.data(), weight.data(), mode, nopbc, device,
+                        &cm) != COORD_OK)
+    error(coord_cmap_last_error(cm));
+  const unsigned nv = docomp ? n : 1;
+  pos.assign(6 * n, 0.0);
+  value.assign(nv, 0.0);
+  deriv.assign(6 * n, 0.0);
+  vir.assign(9 * nv, 0.0);
+}
+
+void ContactMapGPU::calculate() {
+  const auto &positions = getPositions();
+  for (unsigned s = 0; s < 2 * n; s++)
+    for (int k = 0; k < 3; k++) pos[3 * s + k] = positions[s][k];
+  double box[9];
+  const Tensor &b = getPbc().getBox();
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) box[3 * i + j] = b(i, j);
+  if (coord_cmap_forward(cm, pos.data(), box, value.data(), deriv.data(), vir.data()) != COORD_OK)
+    error(std::string("CONTACTMAP: ") + coord_cmap_last_error(cm));
+  auto vec = [&](unsigned s) { return Vector(deriv[3 * s], deriv[3 * s + 1], deriv[3 * s + 2]); };
+  auto ten = [&](unsigned i) {
+    Tensor t;
+    for (int x = 0; x < 3; x++)
+      for (int y = 0; y < 3; y++) t(x, y) = vir[9 * i + 3 * x + y];
+    return t;
+  };
+  if (docomp) {
+    for (unsigned i = 0; i < n; i++) {
+      Value *val = getPntrToComponent(i);
+      setAtomsDerivatives(val, i, vec(i));
+      setAtomsDerivatives(val, n + i, vec(n + i));
+      setBoxDerivatives(val, ten(i));
+      val->set(value[i]);
+    }
+  } else {
+    for (unsigned s = 0; s < 2 * n; s++) setAtomsDerivatives(s, vec(s));
+    setValue(value[0]);
+    setBoxDerivatives(ten(0));
+  }
+}
+
 } // namespace coordgpu_plugin
 } // namespace PLMD

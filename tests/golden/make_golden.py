@@ -27,6 +27,9 @@ so that the tests run where the reference tree is absent.  Sources:
   regtest/trajectories/64.xyz: coordination.xyz.reference (per-atom values)
 * regtest/symfunc/rt-single-groupb      COORDINATIONNUMBER SPECIESA=1-5
   SPECIESB=6 over trajectory.xyz: colvar.reference
+* regtest/basic/rt28, rt72              CONTACTMAP (CMDIST and components over
+  the regtest's trajectory.xyz; SUM of 278 Q contacts on trpcage.gro):
+  colvar.reference, deriv.reference; the contacts are parsed from plumed.dat
 """
 from __future__ import annotations
 
@@ -51,6 +54,41 @@ def read_xyz(path):
         boxes.append(box)
         i += n + 2
     return frames, boxes
+
+
+def read_gro(path):
+    lines = open(path).read().split("\n")
+    n = int(lines[1].split()[0])
+    pos = [[float(lines[2 + k][20 + 8 * j:28 + 8 * j]) for j in range(3)] for k in range(n)]
+    v = [float(x) for x in lines[2 + n].split()]
+    if len(v) == 3:
+        v += [0.0] * 6
+    # v1(x) v2(y) v3(z) v1(y) v1(z) v2(x) v2(z) v3(x) v3(y): rows are lattice vectors
+    box = [v[0], v[3], v[4], v[5], v[1], v[6], v[7], v[8], v[2]]
+    return pos, box
+
+
+def contactmap_blocks(plumed_dat):
+    """The CONTACTMAP ... blocks of a plumed.dat: label, flags, contacts."""
+    text = open(plumed_dat).read()
+    out = []
+    for blk in re.findall(r"CONTACTMAP \.\.\.(.*?)\.\.\. CONTACTMAP", text, re.S):
+        cm = {"label": re.search(r"LABEL=(\S+)", blk).group(1), "sum": bool(re.search(r"^\s*SUM\s*$", blk, re.M)),
+              "cmdist": bool(re.search(r"^\s*CMDIST\s*$", blk, re.M)), "contacts": []}
+        i = 1
+        while True:
+            m = re.search(r"ATOMS%d=(\d+),(\d+)" % i, blk)
+            if not m:
+                break
+            sw = re.search(r"SWITCH%d=\{([^}]*)\}" % i, blk).group(1)
+            ref = re.search(r"REFERENCE%d=(\S+)" % i, blk)
+            w = re.search(r"WEIGHT%d=(\S+)" % i, blk)
+            cm["contacts"].append({"atoms": [int(m.group(1)), int(m.group(2))], "switch": " ".join(sw.split()),
+                                   "reference": float(ref.group(1)) if ref else 0.0,
+                                   "weight": float(w.group(1)) if w else 1.0})
+            i += 1
+        out.append(cm)
+    return out
 
 
 def read_table(path):
@@ -211,6 +249,29 @@ def main(ref):
                                  "frames": [fr[:6] for fr in ftr], "box": btr, "cn": [r[1:] for r in sg],
                                  "fmt": "%8.4f"}},
               open(os.path.join(HERE, "rt_peratom.json"), "w"))
+    # --- CONTACTMAP: rt28, rt72 ------------------------------------------------
+    d28 = os.path.join(reg, "basic", "rt28")
+    fr28, bx28 = read_xyz(os.path.join(d28, "trajectory.xyz"))
+    col28 = read_table(os.path.join(d28, "colvar.reference"))
+    der28 = read_table(os.path.join(d28, "deriv.reference"))
+    maps28 = contactmap_blocks(os.path.join(d28, "plumed.dat"))
+    atoms28 = sorted({a for cm in maps28 for c in cm["contacts"] for a in c["atoms"]})
+    npar = 3 * 2 * len(maps28[0]["contacts"]) + 9
+    d72 = os.path.join(reg, "basic", "rt72")
+    pos72, box72 = read_gro(os.path.join(d72, "trpcage.gro"))
+    col72 = read_table(os.path.join(d72, "colvar.reference"))
+    der72 = read_table(os.path.join(d72, "deriv.reference"))
+    maps72 = contactmap_blocks(os.path.join(d72, "plumed.dat"))
+    json.dump({"source": "regtest/basic/rt28 (plumed.dat, trajectory.xyz, colvar.reference, deriv.reference), "
+                         "regtest/basic/rt72 (plumed.dat, trpcage.gro, colvar.reference, deriv.reference)",
+               "rt28": {"maps": maps28, "atoms": atoms28,
+                        "frames": [[fr[a - 1] for a in atoms28] for fr in fr28], "box": bx28,
+                        "colvar": [r[1:] for r in col28], "colvar_fields": ["a", "c.contact-1", "c.contact-5"],
+                        "deriv_a": [[r[2] for r in der28[f * npar:(f + 1) * npar]] for f in range(len(col28))],
+                        "fmt": "colvar %f, deriv %8.6f"},
+               "rt72": {"map": maps72[0], "pos": pos72, "box": box72, "value": col72[0][1],
+                        "deriv": [r[2] for r in der72], "fmt": "colvar %f, deriv %12.8f"}},
+              open(os.path.join(HERE, "rt_contactmap.json"), "w"))
     print("fixtures written to", HERE)
 
 

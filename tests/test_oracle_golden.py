@@ -201,3 +201,41 @@ def test_rt_peratom_coordination(orc, golden):
     for fi, (fr, bx) in enumerate(zip(sgb["frames"], sgb["box"])):
         cn = orc.peratom(sgb["spec"], fr, np.diag(bx), orc.all_pairs(oracle.MODE_TWO, 5, 1))
         assert np.abs(cn[:5] - np.array(sgb["cn"][fi])).max() <= 5.01e-5, fi
+
+
+def _cmap_inputs(m, coords):
+    cs = m["contacts"]
+    pos = np.array([coords(c["atoms"][0]) for c in cs] + [coords(c["atoms"][1]) for c in cs])
+    mode = 2 if m["cmdist"] else (1 if m["sum"] else 0)
+    return cs, pos, mode
+
+
+def test_rt_contactmap(orc, golden):
+    """regtest/basic/rt28 (CMDIST and components, per-contact switches,
+    references and weights; colvar %f, deriv %8.6f) and rt72 (SUM of 278 Q
+    contacts in a triclinic box; colvar %f, deriv %12.8f)."""
+    g = golden("rt_contactmap.json")
+    r = g["rt28"]
+    idx = {a: k for k, a in enumerate(r["atoms"])}
+    assert len(r["frames"]) == 5
+    for fi, (fr, bx) in enumerate(zip(r["frames"], r["box"])):
+        B = np.diag(bx)
+        res = []
+        for m in r["maps"]:
+            cs, pos, mode = _cmap_inputs(m, lambda a: fr[idx[a]])
+            res.append(orc.contactmap([c["switch"] for c in cs], pos, B, [c["reference"] for c in cs],
+                                      [c["weight"] for c in cs], mode))
+        (va, da, wa), (vc, _, _) = res
+        assert abs(va[0] - r["colvar"][fi][0]) <= 5.01e-7
+        assert abs(vc[0] - r["colvar"][fi][1]) <= 5.01e-7 and abs(vc[4] - r["colvar"][fi][2]) <= 5.01e-7
+        got = np.concatenate([da.reshape(-1), wa.reshape(-1)])
+        assert np.abs(got - np.array(r["deriv_a"][fi])).max() <= 5.01e-7, fi
+    r = g["rt72"]
+    P = np.array(r["pos"])
+    cs, pos, mode = _cmap_inputs(r["map"], lambda a: P[a - 1])
+    assert mode == 1 and len(cs) == 278
+    v, d, w = orc.contactmap([c["switch"] for c in cs], pos, np.array(r["box"]).reshape(3, 3),
+                             [c["reference"] for c in cs], [c["weight"] for c in cs], mode)
+    assert abs(v[0] - r["value"]) <= 5.01e-7
+    got = np.concatenate([d.reshape(-1), w.reshape(-1)])
+    assert np.abs(got - np.array(r["deriv"])).max() <= 5.01e-9
