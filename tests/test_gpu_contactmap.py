@@ -37,8 +37,8 @@ def test_rt28_golden(orc, golden):
     a, c = ContactMap(_line(ma)), ContactMap(_line(mc))
     for fi, (fr, bx) in enumerate(zip(r["frames"], r["box"])):
         B = np.diag(bx)
-        pa = np.array([fr[idx[x]] for x in a.requested_atoms])
-        pc = np.array([fr[idx[x]] for x in c.requested_atoms])
+        pa = np.array([fr[idx[x + 1]] for x in a.requested_atoms])  # 0-based indices, 1-based serials
+        pc = np.array([fr[idx[x + 1]] for x in c.requested_atoms])
         va, da, wa = a.calculate(pa, B)
         vc, dc, wc = c.calculate(pc, B)
         assert abs(va - r["colvar"][fi][0]) <= 5.01e-7
@@ -63,7 +63,7 @@ def test_rt72_golden_triclinic(orc, golden):
     r = golden("rt_contactmap.json")["rt72"]
     cm = ContactMap(_line(r["map"]))
     P = np.array(r["pos"])
-    pos = P[np.array(cm.requested_atoms) - 1]
+    pos = P[np.array(cm.requested_atoms)]
     B = np.array(r["box"]).reshape(3, 3)
     v, d, w = cm.calculate(pos, B)
     assert abs(v - r["value"]) <= 5.01e-7
@@ -103,7 +103,7 @@ def test_contactmap_batched_parity(orc, mode):
     L = 4.0
     frames = rng.uniform(0, L, (F, natoms, 3))
     boxes = np.stack([np.diag([L, L * 1.1, L * 0.9])] * F)
-    req = np.array(cm.requested_atoms) - 1
+    req = np.array(cm.requested_atoms)
     pos = np.ascontiguousarray(frames[:, req, :])
     dev = torch.device("cuda:0")
     tp = torch.as_tensor(pos, device=dev)
