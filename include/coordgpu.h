@@ -156,6 +156,14 @@ int coord_switch_params(const coord_ctx *ctx, double out[7]);
  * with COORD_FLAG_NO_DERIV); virial: 9 (may be NULL). */
 int coord_forward(coord_ctx *ctx, const double *pos, const double box[9], int64_t step, unsigned flags, double *s,
                   double *deriv, double *virial);
+/* coord_forward for n_frames frames (walkers or trajectory frames) of one
+ * context in one call: pos [frames][slots][3], boxes [frames][9], s
+ * [frames], deriv [frames][slots][3] and virial [frames][9] are host arrays.
+ * Same host paths as coord_forward; every frame has its own neighbour list.
+ * No reference counterpart: a host that drives several walkers in one
+ * process can make one call instead of one per walker. */
+int coord_forward_batch(coord_ctx *ctx, int n_frames, const double *pos, const double *boxes, int64_t step,
+                        unsigned flags, double *s, double *deriv, double *virial);
 
 /* Batched form for walkers / trajectory frames sharing one action definition:
  * n_frames independent frames, each with its own neighbour list.  Device

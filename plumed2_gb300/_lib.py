@@ -79,6 +79,7 @@ def load() -> C.CDLL:
         L.coord_get_nslots.argtypes = [_vp, C.POINTER(C.c_int64)]
         L.coord_set_dhenergy.argtypes = [_vp] + [C.c_double] * 6
         L.coord_set_charges.argtypes = [_vp, _dp, C.c_int64]
+        L.coord_forward_batch.argtypes = [_vp, C.c_int, _vp, _vp, C.c_int64, C.c_uint, _vp, _vp, _vp]
         L.coord_cmap_create.argtypes = [C.c_int64, C.POINTER(C.c_char_p), C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
                                         C.POINTER(_vp)]
         L.coord_cmap_destroy.argtypes = [_vp]

@@ -225,6 +225,17 @@ class Coordination:
         if rc:
             check(self._L, self._ctx, rc)
 
+    def forward_host_batch(self, n_frames: int, pos_addr: int, boxes_addr: int, step: int, flags: int, s_addr: int,
+                           deriv_addr: int, virial_addr: int):
+        """coord_forward_batch with plain addresses of host arrays: positions
+        [frames][slots][3], boxes [frames][9], s [frames], derivatives
+        [frames][slots][3], virial [frames][9]."""
+        self._ensure_groups()
+        rc = self._L.coord_forward_batch(self._ctx, int(n_frames), pos_addr, boxes_addr, int(step), int(flags), s_addr,
+                                         deriv_addr or None, virial_addr or None)
+        if rc:
+            check(self._L, self._ctx, rc)
+
     def calculate_system(self, system_positions, box, step: int = 0, **kw):
         """Gather the requested atoms from a full system array and calculate."""
         sp = np.asarray(system_positions, dtype=np.float64).reshape(-1, 3)

@@ -1222,6 +1222,64 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   return COORD_OK;
 }
 
+int coord_forward_batch(coord_ctx *c, int n_frames, const double *pos, const double *boxes, int64_t step,
+                        unsigned flags, double *s, double *deriv, double *virial) {
+  if (!c) return COORD_ERR_ARG;
+  if (n_frames < 1) return c->fail(COORD_ERR_ARG, "n_frames must be >= 1");
+  if (n_frames == 1) return coord_forward(c, pos, boxes, step, flags, s, deriv, virial);
+  if (!boxes || !s || (!pos && c->ns > 0)) return c->fail(COORD_ERR_ARG, "null positions, boxes or s");
+  const bool want_d = !(flags & COORD_FLAG_NO_DERIV);
+  if (want_d && !deriv && c->ns > 0) return c->fail(COORD_ERR_ARG, "null deriv");
+  if (flags & COORD_FLAG_SAVE) return c->fail(COORD_ERR_ARG, "COORD_FLAG_SAVE needs the device call");
+  cudaSetDevice(c->p.device);
+  const size_t n3 = (size_t)c->ns * 3 * n_frames;
+  cudaError_t e;
+  if (c->ns == 0) {
+    for (int f = 0; f < n_frames; f++) s[f] = 0.0;
+    if (want_d && virial) std::memset(virial, 0, 9 * sizeof(double) * n_frames);
+    return COORD_OK;
+  }
+  if (c->host_direct < 0) {
+    int pageable = 0, tables = 0;
+    coord_host_memory_access(c->p.device, &pageable, &tables);
+    const char *staged = std::getenv("COORD_HOST_STAGED");
+    c->host_direct = (pageable && tables && !(staged && staged[0] == '1')) ? 1 : 0;
+  }
+  if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3))) return c->cuda_fail(e, "staging allocation");
+  if (c->host_direct) {
+    // as coord_forward: the kernels read and write the caller's arrays in place
+    HostIO hio{pos, want_d ? deriv : nullptr, false};
+    int rc = forward_impl(c, n_frames, c->d_pos.p, boxes, step, flags, s, want_d ? c->d_deriv.p : nullptr,
+                          want_d ? virial : nullptr, nullptr, nullptr, &hio);
+    if (rc) return rc;
+    if ((e = cudaStreamSynchronize(c->stream))) return c->cuda_fail(e, "forward");
+    return COORD_OK;
+  }
+  const size_t nf = (size_t)n_frames;
+  if ((e = c->d_s.ensure(nf)) || (e = c->d_virial.ensure(9 * nf)) || (e = c->h_pos.ensure(n3)) ||
+      (e = c->h_out.ensure(n3 + 10 * nf)))
+    return c->cuda_fail(e, "staging allocation");
+  std::memcpy(c->h_pos.p, pos, n3 * sizeof(double));
+  if ((e = cudaMemcpyAsync(c->d_pos.p, c->h_pos.p, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
+    return c->cuda_fail(e, "H2D positions");
+  int rc = forward_impl(c, n_frames, c->d_pos.p, boxes, step, flags, c->d_s.p, want_d ? c->d_deriv.p : nullptr,
+                        want_d ? c->d_virial.p : nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  double *hs = c->h_out.p, *hv = hs + nf, *hd = hv + 9 * nf;
+  cudaMemcpyAsync(hs, c->d_s.p, nf * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (want_d) {
+    cudaMemcpyAsync(hv, c->d_virial.p, 9 * nf * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(hd, c->d_deriv.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  }
+  if ((e = cudaStreamSynchronize(c->stream))) return c->cuda_fail(e, "forward");
+  std::memcpy(s, hs, nf * sizeof(double));
+  if (want_d) {
+    if (virial) std::memcpy(virial, hv, 9 * nf * sizeof(double));
+    std::memcpy(deriv, hd, n3 * sizeof(double));
+  }
+  return COORD_OK;
+}
+
 int coord_backward_device(coord_ctx *c, int n_frames, const double *pos, const double *boxes, const double *g,
                           double *grad_pos, double *grad_box, double *grad_param, void *stream) {
   if (!c) return COORD_ERR_ARG;

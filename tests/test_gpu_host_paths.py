@@ -65,3 +65,44 @@ def test_self_pair_only_host_call():
     c = Coordination("GROUPA=1 GROUPB=1 R_0=0.3")
     s, d, v = c.calculate(np.zeros((2, 3)), np.diag([3.0] * 3))
     assert s == 0.0 and np.all(d == 0) and np.all(v == 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("staged", [False, True])
+def test_batched_host_call_equals_device_call(prec, staged):
+    """coord_forward_batch: three walkers' host arrays in one call, on a
+    rebuild step and on a plain step, equal the batched device call."""
+    from plumed2_gb300.action import Coordination
+    from plumed2_gb300._lib import addr
+    n, F, L = 2000, 3, 13 * 0.31
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=10" % n
+    pos = np.ascontiguousarray(np.stack([jittered_lattice(n, 0.31, 0.03, 80 + f) for f in range(F)]))
+    boxes = np.ascontiguousarray(np.stack([np.diag([L] * 3).reshape(9)] * F))
+    if staged:
+        os.environ["COORD_HOST_STAGED"] = "1"
+    try:
+        c = Coordination(line, precision=prec)
+        got = []
+        for step in (0, 1):
+            s, d, v = np.zeros(F), np.zeros((F, n, 3)), np.zeros((F, 9))
+            c.forward_host_batch(F, addr(pos), addr(boxes), step, 0, addr(s), addr(d), addr(v))
+            got.append((s, d, v))
+        c.close()
+    finally:
+        os.environ.pop("COORD_HOST_STAGED", None)
+    c = Coordination(line, precision=prec)
+    dev = torch.device("cuda:0")
+    tp = torch.tensor(pos, dtype=torch.float64, device=dev)
+    s = torch.zeros(F, dtype=torch.float64, device=dev)
+    d = torch.zeros(F, n, 3, dtype=torch.float64, device=dev)
+    v = torch.zeros(F, 9, dtype=torch.float64, device=dev)
+    c.forward_device(tp.data_ptr(), boxes, F, s.data_ptr(), d.data_ptr(), v.data_ptr(), step=0)
+    torch.cuda.synchronize()
+    ref = (s.cpu().numpy(), d.cpu().numpy(), v.cpu().numpy())
+    c.close()
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    for g in got:
+        for f in range(F):
+            assert abs(g[0][f] - ref[0][f]) <= tol * abs(ref[0][f])
+            assert np.abs(g[1][f] - ref[1][f]).max() <= tol * np.abs(ref[1][f]).max()
+            assert np.abs(g[2][f] - ref[2][f]).max() <= tol * np.abs(ref[2][f]).max()
