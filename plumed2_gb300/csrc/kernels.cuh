@@ -362,34 +362,60 @@ __global__ void k_cell_sort(KArgs a) {
   }
 }
 
+// Block-staged contiguous copies between a slot-ordered AoS array of 3
+// doubles per slot and shared memory: every warp access covers 32
+// consecutive doubles (whole lines, also across a CPU-GPU link), where one
+// thread per slot touching its own 3 doubles would leave holes in every
+// access.
+constexpr int kSlotBlock = 256;
+__device__ __forceinline__ void stage_in3(double *sh, const double *src, int nb) {
+  for (int k = threadIdx.x; k < 3 * nb; k += blockDim.x) sh[k] = src[k];
+}
+__device__ __forceinline__ void stage_out3(double *dst, const double *sh, int nb) {
+  for (int k = threadIdx.x; k < 3 * nb; k += blockDim.x) dst[k] = sh[k];
+}
+
 // Host-array calls on devices that access pageable host memory in place:
 // positions read from the caller's array in slot order (coalesced across the
 // link) and written as fixed-point values straight to rank order, replacing
 // a copy and k_gather; derivatives read through rank_of_slot and written to
 // the caller's array in slot order, replacing k_finalize32 and a copy.
-__global__ void k_prep_host(KArgs a, const double *__restrict__ hpos, int rank_order) {
+__global__ void __launch_bounds__(kSlotBlock) k_prep_host(KArgs a, const double *__restrict__ hpos, int rank_order) {
   const int f = blockIdx.y;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.ns) return;
+  const int s0 = blockIdx.x * kSlotBlock;
+  const int nb = min(kSlotBlock, a.ns - s0);
+  if (nb <= 0) return;
   const size_t fo = (size_t)f * a.ns;
-  const double *x = hpos + (fo + s) * 3;
-  const double xx[3] = {x[0], x[1], x[2]};
+  __shared__ double sx[3 * kSlotBlock];
+  stage_in3(sx, hpos + (fo + s0) * 3, nb);
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= nb) return;
+  const int s = s0 + t;
+  const double xx[3] = {sx[3 * t], sx[3 * t + 1], sx[3 * t + 2]};
   const int r = rank_order ? a.rank_of_slot[fo + s] : s;
   a.q[fo + r] = fixed_of(a.fc[f], xx);
 }
-__global__ void k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
+__global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
   const int f = blockIdx.y;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.ns) return;
+  const int s0 = blockIdx.x * kSlotBlock;
+  const int nb = min(kSlotBlock, a.ns - s0);
+  if (nb <= 0) return;
   const size_t fo = (size_t)f * a.ns;
-  const int r = rank_order ? a.rank_of_slot[fo + s] : s;
-  const float4 v = a.acc32[fo + r];
-  const double g = a.g ? a.g[f] : 1.0;
-  double *o = hderiv + (fo + s) * 3;
-  o[0] = g * (double)v.x;
-  o[1] = g * (double)v.y;
-  o[2] = g * (double)v.z;
-  if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __shared__ double sd[3 * kSlotBlock];
+  const int t = threadIdx.x;
+  if (t < nb) {
+    const int s = s0 + t;
+    const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+    const float4 v = a.acc32[fo + r];
+    const double g = a.g ? a.g[f] : 1.0;
+    sd[3 * t] = g * (double)v.x;
+    sd[3 * t + 1] = g * (double)v.y;
+    sd[3 * t + 2] = g * (double)v.z;
+    if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  stage_out3(hderiv + (fo + s0) * 3, sd, nb);
 }
 
 // Force application from a saved forward (Colvar::apply, core/Colvar.cpp:50-60,
@@ -433,15 +459,23 @@ __global__ void k_apply_box_forces(int nframes, const double *__restrict__ ff, c
 }
 
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter
-// and the mixed kernels).  rank_order==0: slot order.
-__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
+// and the mixed kernels).  rank_order==0: slot order.  Slot-major: a block
+// reads its 256 slots' positions as one contiguous range and each thread
+// writes its slot's 16 or 32 bytes at the slot's rank.
+__global__ void __launch_bounds__(kSlotBlock) k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
   const int f = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.ns) return;
-  const int s = rank_order ? a.slot_of_rank[(size_t)f * a.ns + r] : r;
+  const int s0 = blockIdx.x * kSlotBlock;
+  const int nb = min(kSlotBlock, a.ns - s0);
+  if (nb <= 0) return;
+  __shared__ double sx[3 * kSlotBlock];
+  stage_in3(sx, a.pos + ((size_t)f * a.ns + s0) * 3, nb);
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= nb) return;
+  const int s = s0 + t;
+  const int r = rank_order ? a.rank_of_slot[(size_t)f * a.ns + s] : s;
   if (wantcell) a.cell_of_rank[(size_t)f * a.ns + r] = a.cell_of_slot[(size_t)f * a.ns + s];
-  const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
-  const double x0 = x[0], x1 = x[1], x2 = x[2];
+  const double x0 = sx[3 * t], x1 = sx[3 * t + 1], x2 = sx[3 * t + 2];
   // the per-atom backward's upstream g rides in the spare fourth component
   const double gw = a.gslot ? a.gslot[(size_t)f * a.ns + s] : 0.0;
   if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, gw);
@@ -980,22 +1014,30 @@ __global__ void k_finalize64(KArgs a, int rank_order) {
     acc[2] = 0.0;
   }
 }
-__global__ void k_finalize32(KArgs a, int rank_order) {
+// Slot-major: each thread reads its slot's accumulator at the slot's rank;
+// the block writes its 256 slots' derivatives as one contiguous range.
+__global__ void __launch_bounds__(kSlotBlock) k_finalize32(KArgs a, int rank_order) {
   const int f = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.ns) return;
+  const int s0 = blockIdx.x * kSlotBlock;
+  const int nb = min(kSlotBlock, a.ns - s0);
+  if (nb <= 0) return;
   const size_t fo = (size_t)f * a.ns;
-  const int s = rank_order ? a.slot_of_rank[fo + r] : r;
-  const float4 v = a.acc32[fo + r];
-  if (a.out_deriv) {
+  __shared__ double sd[3 * kSlotBlock];
+  const int t = threadIdx.x;
+  if (t < nb) {
+    const int s = s0 + t;
+    const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+    const float4 v = a.acc32[fo + r];
     const double g = a.g ? a.g[f] : 1.0;
-    double *o = a.out_deriv + (fo + s) * 3;
-    o[0] = g * (double)v.x;
-    o[1] = g * (double)v.y;
-    o[2] = g * (double)v.z;
+    sd[3 * t] = g * (double)v.x;
+    sd[3 * t + 1] = g * (double)v.y;
+    sd[3 * t + 2] = g * (double)v.z;
+    if (a.out_peratom) a.out_peratom[fo + s] = (double)v.w;
+    if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  if (a.out_peratom) a.out_peratom[fo + s] = (double)v.w;
-  if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!a.out_deriv) return;  // uniform
+  __syncthreads();
+  stage_out3(a.out_deriv + (fo + s0) * 3, sd, nb);
 }
 
 
