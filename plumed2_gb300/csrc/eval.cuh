@@ -114,7 +114,8 @@ __device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s,
     float xp = 1.0f;
 #pragma unroll
     for (int i = 0; i < NH - 1; i++) xp *= x;
-    const float s0 = __frcp_rn(fmaf(xp, x, 1.0f));
+    // 1/(1 + x^N): the hardware reciprocal (2 ulp), the argument is >= 1
+    const float s0 = __fdividef(1.0f, fmaf(xp, x, 1.0f));
     sig = fmaf(s0, s.stretch, s.shift);
     df = s.c * xp * s0 * s0;
   } else {
@@ -129,6 +130,15 @@ struct Acc32 {
   float cv = 0.f, cvc = 0.f;
   float vxx = 0.f, vyy = 0.f, vzz = 0.f, vxy = 0.f, vxz = 0.f, vyz = 0.f;
   float pr0 = 0.f, pd0 = 0.f;
+  // the neighbour-list pass: a plain FP32 sum over one slice's pairs of a
+  // row (tens of terms), flushed into an FP64 lane total after every slice
+  float cvs = 0.f;
+  double cv64 = 0.0;
+  __device__ __forceinline__ void add_s_slice(float sig) { cvs += sig; }
+  __device__ __forceinline__ void flush_s() {
+    cv64 += (double)cvs;
+    cvs = 0.f;
+  }
   __device__ __forceinline__ void add_s(float sig) {
     const float yk = sig - cvc;
     const float tk = cv + yk;
@@ -149,7 +159,7 @@ struct Acc32 {
     pd0 = fmaf(-df, r, fmaf(s.c_d0, sig - 1.f, pd0));
   }
   __device__ __forceinline__ void to_partials(double part[kPartials]) const {
-    part[0] = (double)cv - (double)cvc;
+    part[0] = ((double)cv - (double)cvc) + (cv64 + (double)cvs);
     part[1] = vxx;
     part[2] = vxy;
     part[3] = vxz;
@@ -262,7 +272,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
         df = 0.f;
       }
       if (MODE == EVAL_VJP) df *= gr + __uint_as_float(gpw);
-      acc.add_s(sig);
+      acc.add_s_slice(sig);
       if (MODE >= EVAL_DERIV) {
         const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
         ax -= ddx;
@@ -308,6 +318,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
     }
     if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
+    acc.flush_s();
   }
   double part[kPartials];
   acc.to_partials(part);
