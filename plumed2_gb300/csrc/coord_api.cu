@@ -90,6 +90,10 @@ struct coord_ctx {
   DevBuf<int> d_ptype;
   std::string err;
   cudaStream_t stream = nullptr;
+  // host-array calls over several frames: a second stream and the events of
+  // the two-half pipeline (launch_evaluation_split)
+  cudaStream_t stream2 = nullptr, stream3 = nullptr;
+  cudaEvent_t ev_split[9] = {};
   int nsm = 0;
   // neighbour-list state
   bool firsttime = true;
@@ -428,7 +432,66 @@ struct HostIO {
   const double *pos;  // caller's positions (slot order)
   double *deriv;      // caller's derivatives (slot order) or nullptr
   bool fused;         // prep/finalize straight from/to the caller's arrays
+  bool pinned;        // both arrays are page-locked: copy-engine transfers can overlap the kernels
 };
+
+// Host-array call over several frames with page-locked arrays, on the mixed
+// neighbour-list path: the frames in up to four chunks, whose transfers run
+// on the copy engines beside the kernels of other chunks,
+//   stream 2 (H2D):  pos(0) pos(1) pos(2) ...
+//   stream 1:              pair(0)+finalize(0) pair(1)+finalize(1) ...
+//   stream 3 (D2H):                            deriv(0)            deriv(1) ...
+// (the persistent pair kernel fills every SM, so transfers by kernels could
+// not overlap it).  Returns false (nothing launched) without the streams.
+bool launch_evaluation_chunked(coord_ctx *c, const KArgs &a, int mode, const HostIO *io) {
+  if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+    c->stream2 = nullptr;
+    return false;
+  }
+  if (!c->stream3 && cudaStreamCreateWithFlags(&c->stream3, cudaStreamNonBlocking) != cudaSuccess) {
+    c->stream3 = nullptr;
+    return false;
+  }
+  for (cudaEvent_t &ev : c->ev_split)
+    if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return false;
+  const int F = a.nframes, K = std::min(F, 4);
+  const size_t per = (size_t)a.ns * 3;
+  cudaStream_t s1 = c->stream, s2 = c->stream2, s3 = c->stream3;
+  const int m = std::min(std::max(mode, 0), 4);
+  const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
+  double *dpos = const_cast<double *>(c->d_pos.p);
+  cudaEvent_t *evH = c->ev_split, *evC = c->ev_split + 4;
+  cudaEventRecord(evC[0], s1);  // the other streams follow what stream 1 holds so far
+  cudaStreamWaitEvent(s2, evC[0], 0);
+  cudaStreamWaitEvent(s3, evC[0], 0);
+  for (int k = 0; k < K; k++) {
+    const int f0 = a.frame0 + F * k / K, f1 = a.frame0 + F * (k + 1) / K;
+    cudaMemcpyAsync(dpos + f0 * per, io->pos + f0 * per, (f1 - f0) * per * sizeof(double), cudaMemcpyHostToDevice,
+                    s2);
+    cudaEventRecord(evH[k], s2);
+  }
+  for (int k = 0; k < K; k++) {
+    const int f0 = a.frame0 + F * k / K, f1 = a.frame0 + F * (k + 1) / K;
+    KArgs ak = a;
+    ak.frame0 = f0;
+    ak.nframes = f1 - f0;
+    ak.pos = dpos;
+    cudaStreamWaitEvent(s1, evH[k], 0);
+    launch_prep_host(ak, dpos, 1, s1);
+    launch_eval_nl32(ak, c->sw, c->s32, mode, nb, c->nlm_unroll[m], s1);
+    launch_band_fix(ak, c->sw, c->s32, mode, s1);
+    if (io->deriv) {
+      launch_finalize32(ak, 1, s1);
+      cudaEventRecord(evC[k], s1);
+      cudaStreamWaitEvent(s3, evC[k], 0);
+      cudaMemcpyAsync(io->deriv + f0 * per, ak.out_deriv + f0 * per, (f1 - f0) * per * sizeof(double),
+                      cudaMemcpyDeviceToHost, s3);
+    }
+  }
+  cudaEventRecord(c->ev_split[8], s3);
+  cudaStreamWaitEvent(s1, c->ev_split[8], 0);  // stream 1 ends after the last copy
+  return true;
+}
 
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
@@ -436,6 +499,9 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
   const bool nl = c->p.nlist != COORD_NL_NONE;
   const bool mixed = c->p.precision == COORD_PREC_MIXED;
   const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  if (io && io->fused && io->pinned && nl && mixed && c->mode != MODE_PAIR && a.nframes >= 2 && !c->timing &&
+      (!io->deriv || a.out_deriv) && launch_evaluation_chunked(c, a, mode, io))
+    return;
   // positions for the pair kernel: fixed-point (mixed) or FP64 in rank order
   if (io && io->fused) {
     launch_prep_host(a, io->pos, rank_order, c->stream);
@@ -945,6 +1011,10 @@ int coord_destroy(coord_ctx *c) {
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->stream3) cudaStreamDestroy(c->stream3);
+  for (cudaEvent_t &ev : c->ev_split)
+    if (ev) cudaEventDestroy(ev);
   delete c;
   return COORD_OK;
 }
@@ -1191,7 +1261,7 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
     // the virial are written by the pair pass straight into the caller's
     // variables.
     if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3))) return c->cuda_fail(e, "staging allocation");
-    HostIO hio{pos, want_d ? deriv : nullptr, false};
+    HostIO hio{pos, want_d ? deriv : nullptr, false, false};
     int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, s, want_d ? c->d_deriv.p : nullptr,
                           want_d ? virial : nullptr, nullptr, nullptr, &hio);
     if (rc) return rc;
@@ -1247,8 +1317,17 @@ int coord_forward_batch(coord_ctx *c, int n_frames, const double *pos, const dou
   }
   if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3))) return c->cuda_fail(e, "staging allocation");
   if (c->host_direct) {
-    // as coord_forward: the kernels read and write the caller's arrays in place
-    HostIO hio{pos, want_d ? deriv : nullptr, false};
+    // as coord_forward: the kernels read and write the caller's arrays in
+    // place; page-locked arrays move on the copy engines, chunk by chunk
+    auto locked = [](const void *p) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      return at.type == cudaMemoryTypeHost;
+    };
+    HostIO hio{pos, want_d ? deriv : nullptr, false, locked(pos) && (!want_d || locked(deriv))};
     int rc = forward_impl(c, n_frames, c->d_pos.p, boxes, step, flags, s, want_d ? c->d_deriv.p : nullptr,
                           want_d ? virial : nullptr, nullptr, nullptr, &hio);
     if (rc) return rc;

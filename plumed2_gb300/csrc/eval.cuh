@@ -226,7 +226,7 @@ __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)
 // block barrier costs more than the locality gains.)
 template <int NH, int MODE, int kUnroll>
 __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
-  const int f = blockIdx.y;
+  const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int nw = gridDim.x * wpb;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
 // byte per slice.
 template <int NH, int MODE>
 __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
-  const int f = blockIdx.y;
+  const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];

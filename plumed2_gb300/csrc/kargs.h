@@ -24,6 +24,7 @@ struct KArgs {
   int flags;      // COORD_FLAG_* of the call
   int has_dup;    // some absolute index appears in two slots (self pairs possible)
   int keep_acc;   // finalize leaves the derivative accumulators in place (saved forward)
+  int frame0;     // first frame of a launch over a range of the frames (host-array pipeline)
   FrameConst *fc;               // [nframes]
   const int64_t *abs_of_slot;   // [ns]
   const double *pos;            // [nframes][ns][3]   input, slot order

@@ -381,7 +381,7 @@ __device__ __forceinline__ void stage_out3(double *dst, const double *sh, int nb
 // a copy and k_gather; derivatives read through rank_of_slot and written to
 // the caller's array in slot order, replacing k_finalize32 and a copy.
 __global__ void __launch_bounds__(kSlotBlock) k_prep_host(KArgs a, const double *__restrict__ hpos, int rank_order) {
-  const int f = blockIdx.y;
+  const int f = blockIdx.y + a.frame0;
   const int s0 = blockIdx.x * kSlotBlock;
   const int nb = min(kSlotBlock, a.ns - s0);
   if (nb <= 0) return;
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(kSlotBlock) k_prep_host(KArgs a, const double 
   a.q[fo + r] = fixed_of(a.fc[f], xx);
 }
 __global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
-  const int f = blockIdx.y;
+  const int f = blockIdx.y + a.frame0;
   const int s0 = blockIdx.x * kSlotBlock;
   const int nb = min(kSlotBlock, a.ns - s0);
   if (nb <= 0) return;
@@ -459,23 +459,15 @@ __global__ void k_apply_box_forces(int nframes, const double *__restrict__ ff, c
 }
 
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter
-// and the mixed kernels).  rank_order==0: slot order.  Slot-major: a block
-// reads its 256 slots' positions as one contiguous range and each thread
-// writes its slot's 16 or 32 bytes at the slot's rank.
-__global__ void __launch_bounds__(kSlotBlock) k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
+// and the mixed kernels).  rank_order==0: slot order.
+__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
   const int f = blockIdx.y;
-  const int s0 = blockIdx.x * kSlotBlock;
-  const int nb = min(kSlotBlock, a.ns - s0);
-  if (nb <= 0) return;
-  __shared__ double sx[3 * kSlotBlock];
-  stage_in3(sx, a.pos + ((size_t)f * a.ns + s0) * 3, nb);
-  __syncthreads();
-  const int t = threadIdx.x;
-  if (t >= nb) return;
-  const int s = s0 + t;
-  const int r = rank_order ? a.rank_of_slot[(size_t)f * a.ns + s] : s;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.ns) return;
+  const int s = rank_order ? a.slot_of_rank[(size_t)f * a.ns + r] : r;
   if (wantcell) a.cell_of_rank[(size_t)f * a.ns + r] = a.cell_of_slot[(size_t)f * a.ns + s];
-  const double x0 = sx[3 * t], x1 = sx[3 * t + 1], x2 = sx[3 * t + 2];
+  const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
+  const double x0 = x[0], x1 = x[1], x2 = x[2];
   // the per-atom backward's upstream g rides in the spare fourth component
   const double gw = a.gslot ? a.gslot[(size_t)f * a.ns + s] : 0.0;
   if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, gw);
@@ -1017,7 +1009,7 @@ __global__ void k_finalize64(KArgs a, int rank_order) {
 // Slot-major: each thread reads its slot's accumulator at the slot's rank;
 // the block writes its 256 slots' derivatives as one contiguous range.
 __global__ void __launch_bounds__(kSlotBlock) k_finalize32(KArgs a, int rank_order) {
-  const int f = blockIdx.y;
+  const int f = blockIdx.y + a.frame0;
   const int s0 = blockIdx.x * kSlotBlock;
   const int nb = min(kSlotBlock, a.ns - s0);
   if (nb <= 0) return;

@@ -68,25 +68,32 @@ def test_self_pair_only_host_call():
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-@pytest.mark.parametrize("staged", [False, True])
-def test_batched_host_call_equals_device_call(prec, staged):
+@pytest.mark.parametrize("path", ["direct", "staged", "pinned"])
+def test_batched_host_call_equals_device_call(prec, path):
     """coord_forward_batch: three walkers' host arrays in one call, on a
-    rebuild step and on a plain step, equal the batched device call."""
+    rebuild step and on a plain step, equal the batched device call
+    (pinned: page-locked arrays, moved chunk by chunk on the copy engines on
+    the mixed path)."""
     from plumed2_gb300.action import Coordination
     from plumed2_gb300._lib import addr
     n, F, L = 2000, 3, 13 * 0.31
     line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.9} NLIST NL_CUTOFF=1.0 NL_STRIDE=10" % n
-    pos = np.ascontiguousarray(np.stack([jittered_lattice(n, 0.31, 0.03, 80 + f) for f in range(F)]))
+    if path == "pinned":
+        arr = lambda *shape: torch.zeros(*shape, dtype=torch.float64, pin_memory=True).numpy()
+    else:
+        arr = lambda *shape: np.zeros(shape)
+    pos = arr(F, n, 3)
+    pos[:] = np.stack([jittered_lattice(n, 0.31, 0.03, 80 + f) for f in range(F)])
     boxes = np.ascontiguousarray(np.stack([np.diag([L] * 3).reshape(9)] * F))
-    if staged:
+    if path == "staged":
         os.environ["COORD_HOST_STAGED"] = "1"
     try:
         c = Coordination(line, precision=prec)
         got = []
-        for step in (0, 1):
-            s, d, v = np.zeros(F), np.zeros((F, n, 3)), np.zeros((F, 9))
+        for step in (0, 1, 2):
+            s, d, v = arr(F), arr(F, n, 3), arr(F, 9)
             c.forward_host_batch(F, addr(pos), addr(boxes), step, 0, addr(s), addr(d), addr(v))
-            got.append((s, d, v))
+            got.append((s.copy(), d.copy(), v.copy()))
         c.close()
     finally:
         os.environ.pop("COORD_HOST_STAGED", None)
