@@ -408,7 +408,7 @@ def run_ours(args):
         e2e_v, h2d, d2h = None, 0, 0
         pageable, tables = _lib.host_memory_access(local)
         host_path = ("direct: kernels read the positions from and write s, virial and forces into the caller's "
-                     "pageable host arrays through the host page tables" if pageable and tables and
+                     "host arrays through the host page tables" if pageable and tables and
                      os.environ.get("COORD_HOST_STAGED") != "1" else "staged through pinned host buffers")
         e2e_walker = None
         if args.e2e_steps > 0:
