@@ -23,7 +23,7 @@ void launch_nl_build(const KArgs &a, bool classic, cudaStream_t s) {
   k_bin<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
   k_scan_cells<<<a.nframes, 1024, 0, s>>>(a);
   k_scatter<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a);
-  k_cell_sort<<<dim3(std::max(1, std::min(a.cells_launch, 65535)), a.nframes), 64, 0, s>>>(a);
+  k_cell_sort<<<dim3(std::max(1, std::min((a.cells_launch + 7) / 8, 65535)), a.nframes), 256, 0, s>>>(a);
   k_gather<<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, 1, 1, 1, 1);
   const dim3 sgrid((a.nslices + kSearchWarps - 1) / kSearchWarps, a.nframes);
   if (classic)

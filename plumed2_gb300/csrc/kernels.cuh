@@ -342,22 +342,35 @@ __global__ void k_scatter(KArgs a) {
 }
 
 // Orders each cell's members by slot index (rank = number of smaller
-// members), which makes the sorted order independent of atomic timing.
-__global__ void k_cell_sort(KArgs a) {
+// members), which makes the sorted order independent of atomic timing.  One
+// warp per cell: a cell of up to 32 members ranks them by shuffles, a larger
+// one by a loop over its members.
+__global__ void __launch_bounds__(256) k_cell_sort(KArgs a) {
   const int f = blockIdx.y;
   const int n = min(max(a.fc[f].grid.ncells, 0), a.ncell_cap);
   const int *start = a.cell_start + (size_t)f * (a.ncell_cap + 1);
   const int *tmp = a.scatter_tmp + (size_t)f * a.ns;
   int *out = a.slot_of_rank + (size_t)f * a.ns;
   int *inv = a.rank_of_slot + (size_t)f * a.ns;
-  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c = blockIdx.x * nw + (threadIdx.x >> 5); c < n; c += gridDim.x * nw) {  // warp-uniform
     const int b = start[c], m = start[c + 1] - b;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      const int v = tmp[b + i];
+    if (m <= 32) {
+      const int v = lane < m ? tmp[b + lane] : 0x7fffffff;
       int r = 0;
-      for (int j = 0; j < m; j++) r += (tmp[b + j] < v);
-      out[b + r] = v;
-      inv[v] = b + r;
+      for (int j = 0; j < m; j++) r += (__shfl_sync(0xffffffffu, v, j) < v) ? 1 : 0;
+      if (lane < m) {
+        out[b + r] = v;
+        inv[v] = b + r;
+      }
+    } else {
+      for (int i = lane; i < m; i += 32) {
+        const int v = tmp[b + i];
+        int r = 0;
+        for (int j = 0; j < m; j++) r += (tmp[b + j] < v);
+        out[b + r] = v;
+        inv[v] = b + r;
+      }
     }
   }
 }
