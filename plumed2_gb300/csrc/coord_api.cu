@@ -495,7 +495,9 @@ bool launch_evaluation_chunked(coord_ctx *c, const KArgs &a, int mode, const Hos
 
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
-void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io = nullptr) {
+// gathered: the list build of this call already left the positions in rank
+// order (k_gather in launch_nl_build).
+void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io = nullptr, bool gathered = false) {
   const bool nl = c->p.nlist != COORD_NL_NONE;
   const bool mixed = c->p.precision == COORD_PREC_MIXED;
   const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
@@ -507,7 +509,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
     launch_prep_host(a, io->pos, rank_order, c->stream);
   } else if (c->mode == MODE_PAIR || !nl) {
     if (mixed) launch_gather(a, 0, 0, 1, c->stream);
-  } else {
+  } else if (!gathered) {
     launch_gather(a, 1, mixed ? 0 : 1, mixed ? 1 : 0, c->stream);
   }
   // the pair kernel alone, between the timing events
@@ -799,7 +801,8 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     a.partials = c->partials.p;
     a.max_blocks = c->max_blocks;
   }
-  launch_evaluation(c, a, mode, hio);
+  // a rebuild of this call has just gathered the positions into rank order
+  launch_evaluation(c, a, mode, hio, rebuild && c->mode != MODE_PAIR && !(hio && hio->fused));
   if (hio && !hio->fused && hio->deriv && k_deriv)
     launch_copy(k_deriv, hio->deriv, (size_t)n_frames * c->ns * 3, c->stream);
   if (save) {
