@@ -22,9 +22,10 @@ Workload (the 262,144-atom configuration the headline target is quoted on):
            region, lists rebuilt every 10th step); e2e.per_walker_call is the
            plugin's call (coord_forward, one context and one call per walker).
 
-  --impl reference : the reference's algorithm on the host cores (oracle/_ref
-  where it was built from the reference sources, else the C restatement in
-  oracle/), OpenMP over all threads, one walker per step.
+  --impl reference : the reference's algorithm on the host cores (the C
+  restatement in oracle/, pinned in the tests against the reference's own code
+  built as oracle/_ref), OpenMP over all threads, one walker per step, each
+  step charged its pair loop + 1/10 of the serial cell-list build.
 """
 from __future__ import annotations
 
@@ -176,7 +177,7 @@ def make_walkers(n_walkers, n_atoms, first):
     return out, np.diag([BOX * (n_atoms / N_ATOMS) ** (1 / 3)] * 3)
 
 
-def cpu_baseline(frames, box, budget_s=10.0, use_reference=False):
+def cpu_baseline(frames, box, budget_s=10.0):
     """The reference algorithm on this host's cores: classic neighbour list once
     (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop."""
     import oracle
@@ -189,13 +190,6 @@ def cpu_baseline(frames, box, budget_s=10.0, use_reference=False):
     t_build = time.perf_counter() - t0
     kind = "port"
     nthreads = orc.max_threads()
-    if use_reference:
-        try:
-            ref = oracle.Reference()
-            kind = "reference"
-            nthreads = ref.max_threads()
-        except Exception:
-            ref = None
     reps, t_loop = 0, 0.0
     while t_loop < budget_s or reps == 0:
         t0 = time.perf_counter()
@@ -216,32 +210,32 @@ def run_reference(args):
     import oracle
     oracle.build()
     orc = oracle.Oracle()
-    ref = None
     kind = "port"
-    if oracle.Reference.available():
-        try:
-            ref = oracle.Reference()
-            kind = "reference"
-        except Exception:
-            ref = None
     n = args.atoms if not args.quick else 32768
     frames, box = make_walkers(1, n, 0)
     pos = frames[0]
     nthreads = orc.max_threads()
+    # Each timed step is charged its pair loop plus a tenth of the latest list
+    # build (NL_STRIDE=10), so the figure does not depend on how many rebuilds
+    # fall inside the timed window.  The build is the reference's serial
+    # cell-list update (NLISTCELLS, NeighborList.cpp:177-231), the faster of its
+    # two builders; its default NLIST build tests all N(N-1)/2 pairs.  The
+    # reference's own code (oracle/_ref) builds a list inside every call, so it
+    # pins the port in the tests rather than being timed here.
     pairs = None
+    t_build = 0.0
     total_pairs, total_t, step = 0, 0.0, 0
     for it in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
         if pairs is None or step % 10 == 0:
+            t0 = time.perf_counter()
             pairs = orc.nl_classic_cells(0, n, 0, pos, box, True, 0.8)
-        if ref is not None and n <= 60000:
-            ref.coordination(SPEC, 0, n, 0, pos, box, nl_cutoff=0.8, nthreads=nthreads)
-        else:
-            orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
+            t_build = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             total_pairs += len(pairs)
-            total_t += dt
+            total_t += dt + t_build / 10.0
         step += 1
     v = total_pairs / total_t
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pair-evals/s", "n_gpus": ws,
@@ -250,7 +244,9 @@ def run_reference(args):
             "config": {"workload": "1 walker per step of %d atoms, single list, %s, NLIST NL_CUTOFF=0.8 "
                                    "NL_STRIDE=10 (rebuild every 10th step)" % (n, SPEC)},
             "cpu_baseline": {"value": v, "unit": "pair-evals/s", "cores": nthreads, "kind": kind,
-                             "sample": "%d walker-steps of %d atoms, %d NL pairs each" % (args.steps, n, len(pairs))},
+                             "sample": "%d walker-steps of %d atoms, %d NL pairs each, each step charged its "
+                                       "pair loop + 1/10 of the serial list build (%.2f s)"
+                                       % (args.steps, n, len(pairs), t_build)},
             "e2e": {"value": v, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
