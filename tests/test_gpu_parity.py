@@ -108,6 +108,41 @@ def test_nlist_semantics_over_steps(orc, prec, mode, pbc):
         pos = pos + rng.normal(0, 0.01, pos.shape)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["single", "two"])
+@pytest.mark.parametrize("pbc", [True, False])
+def test_nlist_pairs_crossing_dmax_between_rebuilds(orc, prec, mode, pbc):
+    """D_MAX below NL_CUTOFF: steps of 0.04 nm per coordinate between rebuilds
+    carry thousands of listed pairs across D_MAX both ways (1,273 into it
+    after one step, 5,831 after three).  s, the derivatives and the virial
+    follow the oracle on the last rebuild's list at each step, and the pair
+    set is the oracle's at each rebuild."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.6"
+    n = 4096
+    L = 16 * 0.31
+    box = np.diag([L] * 3)
+    if mode == "single":
+        line, m, n0, n1 = "GROUPA=1-4096", 0, n, 0
+    else:
+        line, m, n0, n1 = "GROUPA=1-2048 GROUPB=2049-4096", 1, 2048, 2048
+    c = Coordination("%s SWITCH={%s} NLIST NL_CUTOFF=0.9 NL_STRIDE=4%s" % (line, spec, "" if pbc else " NOPBC"),
+                     precision=prec)
+    rng = np.random.default_rng(11)
+    pos = jittered_lattice(n, 0.31, 0.03, 6)
+    nl_ref = None
+    for step in range(9):
+        if step % 4 == 0:
+            nl_ref = orc.nl_classic_cells(m, n0, n1, pos, box, pbc, 0.9)
+        got = c.calculate(pos, box, step)
+        if step % 4 == 0:
+            assert np.array_equal(_sorted(c.pairs()), nl_ref), step
+            assert c.nl_size() == len(nl_ref)
+        ref = orc.coordination(spec, pos, box, nl_ref, do_pbc=pbc)
+        _check(prec, got, ref, "step %d" % step)
+        pos = pos + rng.normal(0, 0.04, pos.shape)
+
+
 @pytest.mark.parametrize("mode", ["single", "two"])
 @pytest.mark.parametrize("pbc", [True, False])
 def test_nlistcells_pair_set(orc, mode, pbc):
