@@ -471,10 +471,12 @@ def run_ours(args):
             "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "call": "coord_forward_batch (C ABI, pinned host arrays of all %d walkers by address), steps "
                             "1..%d (lists rebuilt on multiples of 10)" % (W, args.e2e_steps),
-                    "host_path": host_path,
+                    "host_path": "copy engines: the walkers in four chunks, positions in and derivatives out "
+                                 "by cudaMemcpyAsync on two copy streams beside the kernels of the other chunks",
                     "per_walker_call": {"value": e2e_walker, "unit": "pair-evals/s",
                                         "call": "coord_forward per walker and step (the plugin's call), one context "
-                                                "per walker, pageable host arrays"}},
+                                                "per walker, pageable host arrays",
+                                        "host_path": host_path}},
             "gpu_launches": launches, "clocks": clk,
         }
         print(json.dumps(line_out), flush=True)

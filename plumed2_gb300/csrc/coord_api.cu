@@ -90,8 +90,9 @@ struct coord_ctx {
   DevBuf<int> d_ptype;
   std::string err;
   cudaStream_t stream = nullptr;
-  // host-array calls over several frames: a second stream and the events of
-  // the two-half pipeline (launch_evaluation_split)
+  // host-array calls over several frames with page-locked arrays: the copy
+  // streams (H2D, D2H) and the events of the chunked pipeline
+  // (launch_evaluation_chunked)
   cudaStream_t stream2 = nullptr, stream3 = nullptr;
   cudaEvent_t ev_split[9] = {};
   int nsm = 0;
