@@ -35,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -89,7 +90,9 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        # the raw samples (summarised in the JSON line); COORD_BENCH_CLOCKS_DIR keeps them elsewhere
+        out_dir = os.environ.get("COORD_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, "clocks_bench_%d.csv" % os.getpid())
 
     def start(self):
         try:

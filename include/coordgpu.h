@@ -47,7 +47,7 @@ extern "C" {
 #define COORD_ERR_ARG 1         /* invalid argument / keyword error          */
 #define COORD_ERR_CUDA 2        /* CUDA runtime error                        */
 #define COORD_ERR_BOX 3         /* box not usable (see Pbc::setBox)          */
-#define COORD_ERR_UNSUPPORTED 4 /* valid input this build does not handle    */
+#define COORD_ERR_UNSUPPORTED 4 /* valid input the library does not handle   */
 #define COORD_ERR_NOMEM 5       /* device allocation failed                  */
 #define COORD_ERR_TIMEOUT 6     /* a bounded device-side wait expired        */
 #define COORD_ERR_STATE 7       /* call out of order (e.g. no groups set)    */

@@ -1,7 +1,7 @@
 /*
  * coord_oracle.c -- FP64 CPU restatement of PLUMED's COORDINATION hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  See coord_oracle.h.  Compile with
+ * TEST INFRASTRUCTURE ONLY (the oracle).  See coord_oracle.h.  Compile with
  * -ffp-contract=off: the reference is compiled the same way, and an FMA
  * contraction anywhere below would change the low bits of the results.
  *

@@ -1,8 +1,9 @@
 /*
  * coord_oracle.h -- CPU restatement of PLUMED's COORDINATION hot path (FP64).
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: only tests/,
- * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.  The
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU results are
+ * compared with: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg may load it.  The
  * product (libcoordgpu.so) never links or calls it.
  *
  * Every function restates a reference routine with the same floating-point
