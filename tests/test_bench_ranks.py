@@ -57,3 +57,34 @@ def test_single_process_identity():
     import bench
     assert bench.reduce_over_ranks(2.5, "max") == 2.5
     assert bench.rank_walkers(0, 3) == [0, 1, 2]
+
+
+def _run_reference(env_extra, steps, warmup):
+    import json
+    import subprocess
+    env = dict(os.environ, **env_extra)
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--quick",
+                        "--steps", str(steps), "--warmup", str(warmup)], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
+    return [json.loads(x) for x in lines]
+
+
+def test_reference_arm_line():
+    """--impl reference on the host cores: one JSON line with the arm's own
+    metric, a cpu_baseline describing the run and an e2e with no transfers;
+    each step carries a tenth of the list build whatever the timed window."""
+    sys.path.insert(0, ROOT)
+    import bench
+    (d,) = _run_reference({}, 2, 1)
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "pair-evals/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["cores"] >= 1 and "1/10 of the serial list build" in d["cpu_baseline"]["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "pair-evals/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_silent():
+    assert _run_reference({"RANK": "1", "WORLD_SIZE": "2"}, 1, 1) == []
