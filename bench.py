@@ -385,8 +385,19 @@ def run_ours(args):
         frac_hbm = achieved_gbs / hbm_peak if achieved_gbs else None
         # the stored-list pair pass has no tensor-core work: its roof is HBM (the
         # list stream); the FP32 pipe's fraction is reported beside it
+        # the pair-list layout's own count above; the count for a list of two
+        # 4-byte indices per pair with FP32 derivatives (16 N + 8 P + 12 N)
+        # beside it, for comparison
+        bytes_2idx = 8 * pairs_launch + 16 * W * n + 12 * W * n
+        gbs_2idx = bytes_2idx / (kern_ms * 1e-3) / 1e9 if kern_ms > 0 else None
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": frac_hbm,
                 "traffic": None,
+                "alg_bytes_basis": "4 B per stored pair (one half-list entry: partner rank + orientation bit) "
+                                   "+ 16 B fixed-point position + 16 B FP32 accumulator per atom",
+                "two_index_list": {"bytes_per_launch": bytes_2idx, "achieved": gbs_2idx,
+                                   "frac": gbs_2idx / hbm_peak if gbs_2idx else None,
+                                   "basis": "16 B/atom positions + 8 B/pair (two 4-byte indices) "
+                                            "+ 12 B/atom FP32 derivatives"},
                 "peak_source": ("MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if mp.get("hbm_gbs")
                                 else "coord_measure_peaks copy microbenchmark (measured live)")}
         traffic = eval_traffic(pairs_launch)
