@@ -15,6 +15,10 @@ so that the tests run where the reference tree is absent.  Sources:
 * regtest/basic/rt42, rt42c             108-atom COORDINATION in a triclinic
   box: check_{c,e,g}.reference, colvar.reference, ff.reference
   (forces and virial of a RESTRAINT with SLOPE=1 on c+d)
+* regtest/basic/rt42-cells{,-cos,-gauss}  108 atoms, GROUPA=GROUPB=1-108,
+  NLIST against NLISTCELLS (NL_STRIDE=4, NL_CUTOFF=2.0) for RATIONAL D_MAX=1.5,
+  COSINUS and GAUSSIAN D_MAX=1.5: check_diff.reference (d - c at %8.4f) and
+  ff.reference (forces of SLOPE=0.001 on d - c at %10.5f, all zero)
 * regtest/tools/rt-Neigbourlist         unitTest.reference / testNoNL.reference
   (exact neighbour sets on a simple-cubic lattice)
 * regtest/basic/rt-dhenergy, rt-dhenergy2  DHENERGY between atoms 1-3 and 4-10
@@ -178,6 +182,31 @@ def main(ref):
                           "g": "EXP R_0=1", "c_single": "R0SYNTAX 6 0 1.0 0.0 single",
                           "forces": "-(dc+dd) - 0.001*(dc - 0.5 dd - 0.5 dfast + de - df + dg - dh)"}},
               open(os.path.join(HERE, "rt42.json"), "w"))
+
+    # --- rt42-cells, rt42-cells-cos, rt42-cells-gauss -------------------------
+    variants = {}
+    for name in ("rt42-cells", "rt42-cells-cos", "rt42-cells-gauss"):
+        dd = os.path.join(reg, "basic", name)
+        coord = {}
+        for line in open(os.path.join(dd, "plumed.dat")):
+            m = re.match(r"\s*(\w+):\s*COORDINATION\s+(.*\S)\s*$", line)
+            if m:
+                coord[m.group(1)] = " ".join(m.group(2).split())
+        ff, lines, i = [], open(os.path.join(dd, "ff.reference")).read().split("\n"), 0
+        while i < len(lines) and lines[i].strip():  # per frame: count, virial, one force line per atom
+            n = int(lines[i])
+            ff += [float(x) for x in lines[i + 1].split()]
+            ff += [float(x) for k in range(n) for x in lines[i + 2 + k].split()[1:4]]
+            i += n + 2
+        variants[name] = {"c": coord["c"], "d": coord["d"],
+                          "check_diff": [r[1] for r in read_table(os.path.join(dd, "check_diff.reference"))],
+                          "ff_max_abs": max(abs(x) for x in ff)}
+    frames, boxes = read_xyz(os.path.join(reg, "basic", "rt42-cells", "trajectory.xyz"))
+    json.dump({"source": "regtest/basic/rt42-cells{,-cos,-gauss} (plumed.dat COORDINATION lines, trajectory.xyz "
+                         "shared by the three, check_diff.reference, ff.reference)",
+               "frames": frames, "box": boxes, "variants": variants,
+               "fmt": "check_diff %8.4f; forces and virial %10.5f"},
+              open(os.path.join(HERE, "rt42_cells.json"), "w"))
 
     # --- rt-Neigbourlist ---------------------------------------------------
     dnl = os.path.join(reg, "tools", "rt-Neigbourlist")

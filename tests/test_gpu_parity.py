@@ -163,6 +163,39 @@ def test_nlistcells_pair_set(orc, mode, pbc):
     _check("fp64", got, ref)
 
 
+@pytest.mark.parametrize("variant", ["rt42-cells", "rt42-cells-cos", "rt42-cells-gauss"])
+def test_rt42_cells_golden(orc, golden, variant):
+    """regtest/basic/rt42-cells{,-cos,-gauss} through the C ABI: the NLIST and
+    NLISTCELLS actions of each input (GROUPA=GROUPB=1-108, triclinic box,
+    NL_STRIDE=4) over the 27 frames.  d - c against check_diff.reference
+    (%8.4f), the forces and virial of SLOPE=0.001 on d - c against
+    ff.reference (%10.5f, all zero), and each action against the oracle on
+    the lists of its own last rebuild (FP64 tolerances above)."""
+    from plumed2_gb300.action import Coordination
+    import re
+    g = golden("rt42_cells.json")
+    v = g["variants"][variant]
+    spec = re.search(r"SWITCH=\{([^}]*)\}", v["c"]).group(1).strip()
+    c, d = Coordination(v["c"]), Coordination(v["d"])
+    n = 108
+    absi = _abs_index(c)
+    assert np.array_equal(absi, _abs_index(d))
+    for step, (fr, bx) in enumerate(zip(g["frames"], g["box"])):
+        pos = np.array(fr)[absi]
+        box = np.array(bx).reshape(3, 3)
+        if step % 4 == 0:
+            pc = orc.nl_classic(1, n, n, pos, box, True, 2.0)
+            pd = orc.nl_linkcells(1, n, n, pos, box, True, 2.0)
+        got_c = c.calculate(pos, box, step)
+        got_d = d.calculate(pos, box, step)
+        _check("fp64", got_c, orc.coordination(spec, pos, box, pc, abs_index=absi), "c step %d" % step)
+        _check("fp64", got_d, orc.coordination(spec, pos, box, pd, abs_index=absi), "d step %d" % step)
+        assert abs((got_d[0] - got_c[0]) - v["check_diff"][step]) <= 5.01e-5, step
+        fd = np.zeros((n, 3))
+        np.add.at(fd, absi, 0.001 * (got_d[1] - got_c[1]))
+        assert np.abs(fd).max() <= 5.01e-6 and np.abs(0.001 * (got_d[2] - got_c[2])).max() <= 5.01e-6, step
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 @pytest.mark.parametrize("nl", [False, True])
 def test_pair_mode(orc, prec, nl):

@@ -83,6 +83,47 @@ def test_rt42_values_forces_virial(orc, golden):
         assert np.abs(V - np.array(g["ff_virial"][fi]).reshape(3, 3)).max() <= 5.01e-6
 
 
+def _rt42_cells_steps(orc, g, spec):
+    """The two CVs of an rt42-cells input over its trajectory, lists rebuilt
+    on steps that are multiples of NL_STRIDE=4: (s, derivatives per atom,
+    virial) of the NLIST one (c) and of the NLISTCELLS one (d) per step."""
+    n = len(g["frames"][0])
+    absi = np.concatenate([np.arange(n), np.arange(n)])
+    out = []
+    for step, (fr, bx) in enumerate(zip(g["frames"], g["box"])):
+        pos = np.array(fr)
+        box = np.array(bx).reshape(3, 3)
+        pos2 = np.concatenate([pos, pos])
+        if step % 4 == 0:
+            pc = orc.nl_classic(1, n, n, pos2, box, True, 2.0)
+            pd = orc.nl_linkcells(1, n, n, pos2, box, True, 2.0)
+        res = []
+        for pairs in (pc, pd):
+            s, d, v = orc.coordination(spec, pos2, box, pairs, abs_index=absi)
+            res.append((s, d[:n] + d[n:], v))
+        out.append(res)
+    return out
+
+
+@pytest.mark.parametrize("variant", ["rt42-cells", "rt42-cells-cos", "rt42-cells-gauss"])
+def test_rt42_cells_nlist_vs_nlistcells(orc, golden, variant):
+    """regtest/basic/rt42-cells{,-cos,-gauss}: GROUPA=GROUPB=1-108 in a
+    triclinic box, NLIST against NLISTCELLS with D_MAX (or the COSINUS cutoff)
+    below NL_CUTOFF.  d - c at %8.4f (check_diff.reference) and the forces and
+    virial of RESTRAINT SLOPE=0.001 on d - c at %10.5f (ff.reference) are zero
+    on every one of the 27 frames."""
+    import re
+    g = golden("rt42_cells.json")
+    v = g["variants"][variant]
+    spec = re.search(r"SWITCH=\{([^}]*)\}", v["c"]).group(1).strip()
+    assert v["ff_max_abs"] == 0.0
+    for step, ((sc, dc, vc), (sd, dd, vd)) in enumerate(_rt42_cells_steps(orc, g, spec)):
+        assert abs((sd - sc) - v["check_diff"][step]) <= 5.01e-5, step
+        assert np.abs(0.001 * (dd - dc)).max() <= 5.01e-6, step
+        assert np.abs(0.001 * (vd - vc)).max() <= 5.01e-6, step
+        assert sc > 0
+
+
 def _neigh_sets(pairs, nslots):
     out = [set() for _ in range(nslots)]
     for a, b in pairs:
