@@ -33,16 +33,21 @@ _KEYS = _BASE_KEYS + ("SWITCH", "R_0", "NN", "MM", "D_0")
 
 def parse_atom_list(text: str) -> List[int]:
     """GROUPA/GROUPB value: comma-separated serials and ranges a-b or a-b:stride
-    (1-based, as Tools::interpretRanges); returns 0-based absolute indices."""
+    (1-based, as Tools::interpretRanges, tools/Tools.cpp:559-601): a range runs
+    from a to b inclusive, upwards with a positive stride or downwards with a
+    negative one (108-1:-1); any other stride is an error, with the
+    reference's message.  Returns 0-based absolute indices."""
     out: List[int] = []
     for tok in text.split(","):
         tok = tok.strip()
         if not tok:
             continue
-        m = re.fullmatch(r"(\d+)-(\d+)(?::(\d+))?", tok)
+        m = re.fullmatch(r"(\d+)-(\d+)(?::(-?\d+))?", tok)
         if m:
             a, b, st = int(m.group(1)), int(m.group(2)), int(m.group(3) or 1)
-            out.extend(range(a - 1, b, st))
+            if (st <= 0) if a <= b else (st >= 0):
+                raise ValueError("interpreting ranges %s, stride should be positive" % tok)
+            out.extend(i - 1 for i in range(a, b + (1 if a <= b else -1), st))
         elif re.fullmatch(r"\d+", tok):
             out.append(int(tok) - 1)
         else:

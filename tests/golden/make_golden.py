@@ -19,6 +19,13 @@ so that the tests run where the reference tree is absent.  Sources:
   NLIST against NLISTCELLS (NL_STRIDE=4, NL_CUTOFF=2.0) for RATIONAL D_MAX=1.5,
   COSINUS and GAUSSIAN D_MAX=1.5: check_diff.reference (d - c at %8.4f) and
   ff.reference (forces of SLOPE=0.001 on d - c at %10.5f, all zero)
+* plugins/cudaCoord/regtest/{cudatest,cudatestPair,cudatestWB}/rt-*  the
+  reference's CUDA plugin against COORDINATION on the same input: the
+  COORDINATION line (@mdatoms written as the trajectory's atom range),
+  colvar.reference (gpu - cpu at %8.4f), deriv_delta.reference (at %8.5f),
+  over trajectories/traj-{nopbc,ortho}.xyz.  The two rt-double-bigbox cases
+  are left out: their trajectory is written by `plumed benchmark` when the
+  test runs and is not in the tree.
 * regtest/tools/rt-Neigbourlist         unitTest.reference / testNoNL.reference
   (exact neighbour sets on a simple-cubic lattice)
 * regtest/basic/rt-dhenergy, rt-dhenergy2  DHENERGY between atoms 1-3 and 4-10
@@ -207,6 +214,41 @@ def main(ref):
                "frames": frames, "box": boxes, "variants": variants,
                "fmt": "check_diff %8.4f; forces and virial %10.5f"},
               open(os.path.join(HERE, "rt42_cells.json"), "w"))
+
+    # --- plugins/cudaCoord/regtest -------------------------------------------
+    dcc = os.path.join(ref, "plugins", "cudaCoord", "regtest")
+    trajs = {}
+    for t in ("traj-nopbc.xyz", "traj-ortho.xyz"):
+        fr, bx = read_xyz(os.path.join(dcc, "trajectories", t))
+        trajs[t] = {"frames": fr, "box": bx}
+    cases = {}
+    for suite in ("cudatest", "cudatestPair", "cudatestWB"):
+        for name in sorted(os.listdir(os.path.join(dcc, suite))):
+            dd = os.path.join(dcc, suite, name)
+            if not name.startswith("rt-"):
+                continue
+            traj = re.search(r"--ixyz\s+([^\s\"']+)", open(os.path.join(dd, "config")).read()).group(1)
+            if traj not in trajs:
+                continue
+            lines = [l.split("#", 1)[0].rstrip() for l in open(os.path.join(dd, "plumed.dat"))]
+            k = next(i for i, l in enumerate(lines) if re.match(r"\s*cpu:\s*COORDINATION\b", l))
+            text = lines[k]
+            if text.endswith("..."):  # continued until a line holding only "..."
+                text = text[:-3]
+                k += 1
+                while lines[k].strip() != "...":
+                    text += " " + lines[k]
+                    k += 1
+            line = " ".join(text.split(":", 1)[1].split()[1:])
+            line = line.replace("@mdatoms", "1-%d" % len(trajs[traj]["frames"][0]))
+            cases["%s/%s" % (suite, name)] = {
+                "line": line, "traj": traj, "float": name.startswith("rt-float"),
+                "diff": [r[1] for r in read_table(os.path.join(dd, "colvar.reference"))],
+                "deriv_delta_max": max(abs(r[2]) for r in read_table(os.path.join(dd, "deriv_delta.reference")))}
+    json.dump({"source": "plugins/cudaCoord/regtest (plumed.dat cpu: lines, colvar.reference, "
+                         "deriv_delta.reference, trajectories/)",
+               "trajectories": trajs, "cases": cases, "fmt": "diff %8.4f; derivative deltas %8.5f"},
+              open(os.path.join(HERE, "cudacoord_plugin.json"), "w"))
 
     # --- rt-Neigbourlist ---------------------------------------------------
     dnl = os.path.join(reg, "tools", "rt-Neigbourlist")

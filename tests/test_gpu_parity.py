@@ -8,6 +8,9 @@ Tolerances, stated here once:
               virial: max|dW| / max|W| <= 1e-5
   neighbour lists: the pair set is bit-exact (sorted comparison).
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -194,6 +197,52 @@ def test_rt42_cells_golden(orc, golden, variant):
         fd = np.zeros((n, 3))
         np.add.at(fd, absi, 0.001 * (got_d[1] - got_c[1]))
         assert np.abs(fd).max() <= 5.01e-6 and np.abs(0.001 * (got_d[2] - got_c[2])).max() <= 5.01e-6, step
+
+
+def _oracle_spec(line):
+    """The oracle's switch spec of a COORDINATION line: the SWITCH={...}
+    definition, or the R_0/NN/MM/D_0 keywords (defaults NN=6, MM=0 -> 2NN,
+    D_0=0)."""
+    import re
+    m = re.search(r"SWITCH=\{([^}]*)\}", line)
+    if m:
+        return m.group(1).strip()
+    kw = dict(re.findall(r"\b(R_0|NN|MM|D_0)=(\S+)", line))
+    return "R0SYNTAX %s %s %s %s" % (kw.get("NN", "6"), kw.get("MM", "0"), kw["R_0"], kw.get("D_0", "0.0"))
+
+
+with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cudacoord_plugin.json")) as _f:
+    _CUDACOORD_CASES = sorted(json.load(_f)["cases"])
+
+
+@pytest.mark.parametrize("case", _CUDACOORD_CASES)
+def test_cudacoord_plugin_regtests(orc, golden, case):
+    """plugins/cudaCoord/regtest: each input of the reference's CUDA plugin
+    tests, whose COORDINATION twin printed gpu - cpu = 0 at %8.4f and
+    derivative deltas of 0 at %8.5f, run here through the C ABI over its ten
+    frames and compared with the oracle (the reference's CPU arithmetic):
+    within those print tolerances, and within this file's FP64 or mixed
+    tolerances (the rt-float-* inputs on the mixed path)."""
+    from plumed2_gb300.action import Coordination
+    g = golden("cudacoord_plugin.json")
+    cs = g["cases"][case]
+    tr = g["trajectories"][cs["traj"]]
+    prec = "mixed" if cs["float"] else "fp64"
+    c = Coordination(cs["line"], precision=prec)
+    absi = _abs_index(c)
+    na, nb = len(c.group_a), len(c.group_b)
+    mode = 2 if " PAIR" in " " + cs["line"] else (1 if nb else 0)
+    pairs = orc.all_pairs(mode, na, nb) if mode else orc.all_pairs(0, na)
+    spec = _oracle_spec(cs["line"])
+    assert cs["deriv_delta_max"] == 0.0 and max(map(abs, cs["diff"])) == 0.0
+    for step, (fr, bx) in enumerate(zip(tr["frames"], tr["box"])):
+        pos = np.array(fr)[absi]
+        box = np.array(bx).reshape(3, 3)
+        got = c.calculate(pos, box, step)
+        ref = orc.coordination(spec, pos, box, pairs, abs_index=absi, do_pbc=" NOPBC" not in " " + cs["line"])
+        assert abs(got[0] - ref[0]) <= 5.01e-5, (case, step)
+        assert np.abs(got[1] - ref[1]).max() <= 5.01e-6, (case, step)
+        _check(prec, got, ref, "%s step %d" % (case, step))
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])

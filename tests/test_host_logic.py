@@ -99,3 +99,17 @@ def test_e2e_pair_accounting():
     assert bench.e2e_pairs(100, 110, 5) == 500
     assert bench.e2e_pairs(100, 110, 10) == 9 * 100 + 110
     assert bench.e2e_pairs(100, 110, 12) == 9 * 100 + 3 * 110
+
+
+def test_atom_ranges():
+    """Tools::interpretRanges (tools/Tools.cpp:559-601): a-b:stride runs from a
+    to b inclusive, downwards with a negative stride; a stride of the wrong
+    sign is an error, with the reference's message."""
+    from plumed2_gb300.action import parse_atom_list
+    assert parse_atom_list("1-10:3") == [0, 3, 6, 9]
+    assert parse_atom_list("108-1:-1") == list(range(107, -1, -1))
+    assert parse_atom_list("108-50:-1,1-49") == list(range(107, 48, -1)) + list(range(49))
+    assert parse_atom_list("5-5,3") == [4, 2]
+    for bad in ("10-1", "1-10:-1", "1-10:0", "10-1:2"):
+        with pytest.raises(ValueError, match="interpreting ranges %s, stride should be positive" % bad):
+            parse_atom_list(bad)
