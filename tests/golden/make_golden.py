@@ -220,6 +220,8 @@ def main(ref):
     trajs = {}
     for t in ("traj-nopbc.xyz", "traj-ortho.xyz"):
         fr, bx = read_xyz(os.path.join(dcc, "trajectories", t))
+        # three numbers: an orthorhombic box given by its edges; stored as 3x3
+        bx = [b if len(b) == 9 else [b[0], 0.0, 0.0, 0.0, b[1], 0.0, 0.0, 0.0, b[2]] for b in bx]
         trajs[t] = {"frames": fr, "box": bx}
     cases = {}
     for suite in ("cudatest", "cudatestPair", "cudatestWB"):
