@@ -104,10 +104,27 @@ class Clocks:
         except Exception:
             self.proc = None
 
+    def _one_shot(self):
+        """One query at the end of a timed region too short for the loop's
+        first sample (lines in the loop's format; none if it fails)."""
+        try:
+            r = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+            return r.stdout.splitlines()
+        except Exception:
+            return []
+
     def stop(self):
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         if self.proc is None:
             return out
+        extra = []
+        try:
+            self.f.flush()
+            if not any(len(x.split(",")) >= 9 for x in open(self.path)):
+                extra = self._one_shot()
+        except Exception:
+            extra = []
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -116,7 +133,7 @@ class Clocks:
         self.f.close()
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for line in list(open(self.path)) + extra:
             p = [x.strip() for x in line.split(",")]
             if len(p) < 9:
                 continue
@@ -131,6 +148,8 @@ class Clocks:
         if sm:
             out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                    "samples": len(sm)}
+            if extra:
+                out["one_shot_at_end"] = True
         return out
 
 

@@ -88,3 +88,41 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_silent():
     assert _run_reference({"RANK": "1", "WORLD_SIZE": "2"}, 1, 1) == []
+
+
+def _fake_smi(tmp_path, loop_body):
+    """An nvidia-smi stand-in: with -lms it runs loop_body, else prints one
+    line in the query's format."""
+    f = tmp_path / "nvidia-smi"
+    f.write_text("#!/bin/sh\nfor a in \"$@\"; do case \"$a\" in -lms) %s;; esac; done\n"
+                 "echo '0, 2070, 2070, 500.00, 0x0, Not Active, Not Active, Not Active, Not Active'\n" % loop_body)
+    f.chmod(0o755)
+    return str(tmp_path)
+
+
+def test_clocks_one_shot_when_the_loop_has_no_sample(tmp_path, monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("PATH", _fake_smi(tmp_path, "exec sleep 30") + os.pathsep + os.environ["PATH"])
+    monkeypatch.setenv("COORD_BENCH_CLOCKS_DIR", str(tmp_path))
+    c = bench.Clocks(0)
+    c.start()
+    out = c.stop()
+    assert out["samples"] == 1 and out["sm_mhz"] == 2070.0 and out["one_shot_at_end"] is True
+    assert out["reasons"] == []
+
+
+def test_clocks_loop_samples_and_reasons(tmp_path, monkeypatch):
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    body = ("while true; do echo '0, 1980, 2070, 900.00, 0x4, Not Active, Not Active, Not Active, Active'; "
+            "sleep 0.05; done")
+    monkeypatch.setenv("PATH", _fake_smi(tmp_path, body) + os.pathsep + os.environ["PATH"])
+    monkeypatch.setenv("COORD_BENCH_CLOCKS_DIR", str(tmp_path))
+    c = bench.Clocks(0)
+    c.start()
+    time.sleep(0.5)
+    out = c.stop()
+    assert out["samples"] >= 2 and out["sm_mhz"] == 1980.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"] and "one_shot_at_end" not in out
