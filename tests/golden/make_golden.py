@@ -15,6 +15,13 @@ so that the tests run where the reference tree is absent.  Sources:
 * regtest/basic/rt42, rt42c             108-atom COORDINATION in a triclinic
   box: check_{c,e,g}.reference, colvar.reference, ff.reference
   (forces and virial of a RESTRAINT with SLOPE=1 on c+d)
+* regtest/basic/rt42b                   GROUPA=GROUPB=1-108 R_0=1 over a .gro
+  trajectory with triclinic boxes: colvar.reference (%8.4f), every 9th frame
+* regtest/basic/rt-mpi0                 a two-list whose groups share atom 5,
+  RATIONAL, EXP and GAUSSIAN over regtest/trajectories/trajectory.xyz:
+  COLVAR.reference (%6.3f), deriv.reference (EXP and GAUSSIAN, %8.4f),
+  ff.0.reference (forces and virial diagonal of RESTRAINT KAPPA=5 AT=15 on
+  the RATIONAL one, %f)
 * regtest/basic/rt42-cells{,-cos,-gauss}  108 atoms, GROUPA=GROUPB=1-108,
   NLIST against NLISTCELLS (NL_STRIDE=4, NL_CUTOFF=2.0) for RATIONAL D_MAX=1.5,
   COSINUS and GAUSSIAN D_MAX=1.5: check_diff.reference (d - c at %8.4f) and
@@ -67,8 +74,10 @@ def read_xyz(path):
     return frames, boxes
 
 
-def read_gro(path):
-    lines = open(path).read().split("\n")
+def read_gro(path, lines=None):
+    """The first frame of a .gro file (or of the given lines)."""
+    if lines is None:
+        lines = open(path).read().split("\n")
     n = int(lines[1].split()[0])
     pos = [[float(lines[2 + k][20 + 8 * j:28 + 8 * j]) for j in range(3)] for k in range(n)]
     v = [float(x) for x in lines[2 + n].split()]
@@ -77,6 +86,19 @@ def read_gro(path):
     # v1(x) v2(y) v3(z) v1(y) v1(z) v2(x) v2(z) v3(x) v3(y): rows are lattice vectors
     box = [v[0], v[3], v[4], v[5], v[1], v[6], v[7], v[8], v[2]]
     return pos, box
+
+
+def read_gro_frames(path):
+    """Every frame of a .gro trajectory: title, atom count, atoms, box."""
+    lines = open(path).read().split("\n")
+    frames, boxes, i = [], [], 0
+    while i + 1 < len(lines) and lines[i + 1].strip():
+        n = int(lines[i + 1].split()[0])
+        pos, box = read_gro(None, lines[i:i + n + 3])
+        frames.append(pos)
+        boxes.append(box)
+        i += n + 3
+    return frames, boxes
 
 
 def contactmap_blocks(plumed_dat):
@@ -189,6 +211,40 @@ def main(ref):
                           "g": "EXP R_0=1", "c_single": "R0SYNTAX 6 0 1.0 0.0 single",
                           "forces": "-(dc+dd) - 0.001*(dc - 0.5 dd - 0.5 dfast + de - df + dg - dh)"}},
               open(os.path.join(HERE, "rt42.json"), "w"))
+
+    # --- rt42b ---------------------------------------------------------------
+    frames, boxes = read_gro_frames(os.path.join(reg, "basic", "rt42b", "trajectory.gro"))
+    col = [r[1] for r in read_table(os.path.join(reg, "basic", "rt42b", "colvar.reference"))]
+    keep = list(range(0, len(frames), 9))
+    json.dump({"source": "regtest/basic/rt42b (plumed.dat, trajectory.gro, colvar.reference); every 9th frame",
+               "line": "GROUPA=1-108 GROUPB=1-108 R_0=1", "frames": [frames[k] for k in keep],
+               "box": [boxes[k] for k in keep], "c": [col[k] for k in keep], "fmt": "%8.4f"},
+              open(os.path.join(HERE, "rt42b.json"), "w"))
+
+    # --- rt-mpi0 -------------------------------------------------------------
+    dm = os.path.join(reg, "basic", "rt-mpi0")
+    frames, boxes = read_xyz(os.path.join(reg, "trajectories", "trajectory.xyz"))
+    colvar = read_table(os.path.join(dm, "COLVAR.reference"))
+    der = read_table(os.path.join(dm, "deriv.reference"))
+    nd = len(der) // len(colvar)
+    ffl, fforces, fvir, i = open(os.path.join(dm, "ff.0.reference")).read().split("\n"), [], [], 0
+    while i < len(ffl) and ffl[i].strip():
+        n = int(ffl[i])
+        fvir.append([float(x) for x in ffl[i + 1].split()])
+        fforces.append([[float(x) for x in ffl[i + 2 + k].split()[1:4]] for k in range(n)])
+        i += n + 2
+    json.dump({"source": "regtest/basic/rt-mpi0 (plumed.dat, COLVAR.reference, deriv.reference, ff.0.reference) "
+                         "over regtest/trajectories/trajectory.xyz",
+               "groupa": "1-10", "groupb": "30-40,5,50-100",
+               "switch": {"c": "RATIONAL R_0=1.0", "cexp": "EXP R_0=0.7", "cgaus": "GAUSSIAN R_0=0.2 D_0=0.6"},
+               "restraint": {"arg": "c", "kappa": 5.0, "at": 15.0},
+               "frames": frames[:len(colvar)], "box": boxes[:len(colvar)],
+               "colvar": [{"c": r[1], "cexp": r[2], "cgaus": r[3]} for r in colvar],
+               "deriv_cexp": [[r[2] for r in der[f * nd:(f + 1) * nd]] for f in range(len(colvar))],
+               "deriv_cgaus": [[r[3] for r in der[f * nd:(f + 1) * nd]] for f in range(len(colvar))],
+               "ff_forces": fforces, "ff_virial_diag": fvir,
+               "fmt": "COLVAR %6.3f, deriv %8.4f, forces and virial %f"},
+              open(os.path.join(HERE, "rt_mpi0.json"), "w"))
 
     # --- rt42-cells, rt42-cells-cos, rt42-cells-gauss -------------------------
     variants = {}

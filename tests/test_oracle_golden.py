@@ -83,6 +83,49 @@ def test_rt42_values_forces_virial(orc, golden):
         assert np.abs(V - np.array(g["ff_virial"][fi]).reshape(3, 3)).max() <= 5.01e-6
 
 
+def test_rt42b_gro_triclinic(orc, golden):
+    """regtest/basic/rt42b: GROUPA=GROUPB=1-108 R_0=1 (each pair twice, self
+    pairs skipped) over a .gro trajectory with triclinic boxes, %8.4f."""
+    g = golden("rt42b.json")
+    n = 108
+    absi = np.concatenate([np.arange(n), np.arange(n)])
+    pairs = orc.all_pairs(1, n, n)
+    for fi, (fr, bx) in enumerate(zip(g["frames"], g["box"])):
+        pos = np.array(fr)[absi]
+        s, _, _ = orc.coordination("R0SYNTAX 6 0 1 0.0", pos, np.array(bx).reshape(3, 3), pairs, abs_index=absi)
+        assert abs(s - g["c"][fi]) <= 5.01e-5, fi
+
+
+def test_rt_mpi0_overlapping_groups(orc, golden):
+    """regtest/basic/rt-mpi0: GROUPA=1-10, GROUPB=30-40,5,50-100 (atom 5 in
+    both: its self pair is skipped, and it has a derivative entry in each
+    group).  c, cexp, cgaus (%6.3f); DUMPDERIVATIVES of cexp and cgaus, 3 per
+    requested atom then the box (%8.4f); forces and virial diagonal of
+    RESTRAINT KAPPA=5 AT=15 on c (%f)."""
+    from plumed2_gb300.action import parse_atom_list
+    g = golden("rt_mpi0.json")
+    ga, gb = parse_atom_list(g["groupa"]), parse_atom_list(g["groupb"])
+    absi = np.array(ga + gb)
+    pairs = orc.all_pairs(1, len(ga), len(gb))
+    rs = g["restraint"]
+    for fi, (fr, bx) in enumerate(zip(g["frames"], g["box"])):
+        frame = np.array(fr)
+        pos = frame[absi]
+        box = np.diag(bx) if len(bx) == 3 else np.array(bx).reshape(3, 3)
+        res = {k: orc.coordination(spec, pos, box, pairs, abs_index=absi) for k, spec in g["switch"].items()}
+        for k in ("c", "cexp", "cgaus"):
+            assert abs(res[k][0] - g["colvar"][fi][k]) <= 5.01e-4, (fi, k)
+        for k in ("cexp", "cgaus"):
+            got = np.concatenate([res[k][1].reshape(-1), res[k][2].reshape(-1)])
+            assert np.abs(got - np.array(g["deriv_" + k][fi])).max() <= 5.01e-5, (fi, k)
+        s, d, v = res[rs["arg"]]
+        w = -rs["kappa"] * (s - rs["at"])
+        F = np.zeros_like(frame)
+        np.add.at(F, absi, w * d)
+        assert np.abs(F - np.array(g["ff_forces"][fi])).max() <= 5.01e-7, fi
+        assert np.abs(w * np.diag(v) - np.array(g["ff_virial_diag"][fi])).max() <= 5.01e-7, fi
+
+
 def _rt42_cells_steps(orc, g, spec):
     """The two CVs of an rt42-cells input over its trajectory, lists rebuilt
     on steps that are multiples of NL_STRIDE=4: (s, derivatives per atom,
