@@ -323,3 +323,49 @@ def test_rt_contactmap(orc, golden):
     assert abs(v[0] - r["value"]) <= 5.01e-7
     got = np.concatenate([d.reshape(-1), w.reshape(-1)])
     assert np.abs(got - np.array(r["deriv"])).max() <= 5.01e-9
+
+
+def _box_family(rng, kind):
+    """A random box of one of the families of regtest/basic/rt-make-1
+    (cubic, orthorhombic, hexagonal, bcc, fcc, generic triclinic with some
+    zero entries), rows the lattice vectors."""
+    box = np.where(rng.random((3, 3)) > 0.2, 2.0 * rng.random((3, 3)) - 1.0, 0.0)
+    if kind in (0, 1):
+        box = np.diag(np.diag(box))
+        if kind == 0:
+            box = np.eye(3) * box[0, 0]
+        return box
+    if kind == 5:
+        return box
+    d = 2.0 * rng.random() - 2.0
+    rows = {2: [(2.0 * rng.random() - 2.0, 0, 0), (0, d, 0), (0, 0.5 * d, np.sqrt(3.0) * d * 0.5)],
+            3: [(d, d, d), (d, -d, d), (d, d, -d)],
+            4: [(d, d, 0), (d, 0, d), (0, d, d)]}[kind]
+    perm = int(rng.integers(0, 3))
+    out = np.zeros((3, 3))
+    for k in range(3):
+        out[(perm + k) % 3] = rows[k]
+    return out
+
+
+@pytest.mark.parametrize("kind", range(6))
+def test_pbc_minimum_image_property(orc, kind):
+    """regtest/basic/rt-make-1 restated as a property: for random boxes of
+    each family and random vectors (some components zeroed), the image that
+    Pbc::distance returns is no longer than any image within two lattice
+    shifts of it (the reference's fullSearch check, 1e-15 in squared
+    length; failures 0 in logfile.reference)."""
+    rng = np.random.default_rng(20 + kind)
+    shifts = np.array([(i, j, k) for i in range(-2, 3) for j in range(-2, 3) for k in range(-2, 3)], float)
+    nbox = 0
+    while nbox < 150:
+        box = _box_family(rng, kind)
+        if abs(np.linalg.det(box)) < 1e-3:
+            continue
+        nbox += 1
+        v = (rng.random((40, 3)) - 0.5) * 5.0
+        v[rng.random((40, 3)) > 0.2] = 0.0
+        fast = orc.pbc_distance(box, np.zeros_like(v), v)
+        for f in fast:
+            full = f + shifts @ box
+            assert np.dot(f, f) - (full * full).sum(1).min() <= 1e-15 * max(1.0, np.dot(f, f)), (kind, box, f)
