@@ -103,6 +103,9 @@ class Oracle:
                           _u32p, C.c_int64]
             f.restype = C.c_int64
         L.orc_linkcells_ncells.argtypes = [C.POINTER(_Pbc), C.c_double, C.POINTER(C.c_int * 3)]
+        L.orc_linkcells_required.argtypes = [C.POINTER(_Pbc), C.c_double, C.POINTER(C.c_int * 3), C.c_int,
+                                             C.POINTER(C.c_int * 27)]
+        L.orc_linkcells_required.restype = C.c_int
         L.orc_coordination.argtypes = [C.POINTER(_Switch), C.POINTER(_Pbc), C.c_int, C.c_int64, _i64p, _dp,
                                        _u32p, C.c_int64, C.POINTER(C.c_double), _dp, _dp, C.c_int]
         L.orc_max_threads.restype = C.c_int
@@ -193,6 +196,14 @@ class Oracle:
         p = self.pbc(box)
         self.L.orc_linkcells_ncells(C.byref(p), float(cutoff), C.byref(nc))
         return list(nc)
+
+    def linkcells_required(self, box, cutoff, cell, use_pbc=True):
+        """Sorted indices of the cells searched from the cell with indices cell."""
+        req = (C.c_int * 27)()
+        p = self.pbc(box)
+        n = self.L.orc_linkcells_required(C.byref(p), float(cutoff), C.byref((C.c_int * 3)(*cell)), int(use_pbc),
+                                          C.byref(req))
+        return sorted(req[:n])
 
     # -- the CV ----------------------------------------------------------------
     def coordination(self, spec, pos, box, pairs, abs_index=None, do_pbc=True, nthreads=1):

@@ -1033,6 +1033,16 @@ static int lc_required(const linkcells_t *lc, int cellIndex, int usePbc, int *re
   return nreq;
 }
 
+/* LinkCells::addRequiredCells (LinkCells.cpp:195-240) for the cell with indices
+ * cell[3] of a box (not sorted; no cell twice): returns their number. */
+int orc_linkcells_required(const orc_pbc *pbc, double cutoff, const int cell[3], int use_pbc, int *req) {
+  linkcells_t lc;
+  memset(&lc, 0, sizeof lc);
+  lc_create(&lc, pbc->box, cutoff);
+  const int idx = cell[0] * lc.nstride[0] + cell[1] * lc.nstride[1] + cell[2] * lc.nstride[2];
+  return lc_required(&lc, idx, use_pbc, req);
+}
+
 int64_t orc_nl_linkcells(int mode, int64_t n0, int64_t n1, const double *pos, const orc_pbc *pbc, int do_pbc,
                          double cutoff, uint32_t *pairs, int64_t cap) {
   if (mode == ORC_NL_PAIR) return -1;

@@ -101,6 +101,10 @@ int64_t orc_nl_linkcells(int mode, int64_t n0, int64_t n1, const double *pos,
                          uint32_t *pairs, int64_t cap);
 /* LinkCells::createCells cell counts for a pbc box (LinkCells.cpp:99-122). */
 void orc_linkcells_ncells(const orc_pbc *pbc, double cutoff, int ncells[3]);
+/* LinkCells::addRequiredCells (LinkCells.cpp:195-240): the cells searched
+ * from the cell with indices cell[3], with or without PBC; returns their
+ * number (at most 27) and writes them, unsorted, to req. */
+int orc_linkcells_required(const orc_pbc *pbc, double cutoff, const int cell[3], int use_pbc, int *req);
 
 /* ---- the CV: CoordinationBase::calculate (CoordinationBase.cpp:142-231) -- */
 /* Loops over npairs (first,second) slot pairs, skipping pairs whose absolute

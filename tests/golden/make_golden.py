@@ -33,6 +33,12 @@ so that the tests run where the reference tree is absent.  Sources:
   over trajectories/traj-{nopbc,ortho}.xyz.  The two rt-double-bigbox cases
   are left out: their trajectory is written by `plumed benchmark` when the
   test runs and is not in the tree.
+* regtest/tools/rt-make-CellLists      outputRequiredCells.reference and
+  outputRequiredCellsNotOrtho.reference (cell counts and the cells searched
+  from corner, edge, face and middle cells, with and without PBC),
+  outputIndexes.reference (cell counts of three boxes at cutoff 1.5).  The
+  boxes of the orthorhombic and the index parts are those of main.cpp
+  (testRequiredCells, testIndexes); the other part prints its own.
 * regtest/tools/rt-Neigbourlist         unitTest.reference / testNoNL.reference
   (exact neighbour sets on a simple-cubic lattice)
 * regtest/basic/rt-dhenergy, rt-dhenergy2  DHENERGY between atoms 1-3 and 4-10
@@ -307,6 +313,42 @@ def main(ref):
                          "deriv_delta.reference, trajectories/)",
                "trajectories": trajs, "cases": cases, "fmt": "diff %8.4f; derivative deltas %8.5f"},
               open(os.path.join(HERE, "cudacoord_plugin.json"), "w"))
+
+    # --- rt-make-CellLists ---------------------------------------------------
+    dcl = os.path.join(reg, "tools", "rt-make-CellLists")
+    case_re = re.compile(r'^\[(?:"(?P<title>[^"]+)" )?co=(?P<co>[0-9.]+) -(?P<name>.+?)- \{(?P<cell>[0-9, ]+)\}'
+                         r'(?P<nopbc> noPBC)?\] Cells:(?P<cells>[0-9 ]*)$')
+    counts, req = [], []
+    cube10 = [10.0, 0, 0, 0, 10.0, 0, 0, 0, 10.0]  # main.cpp testRequiredCells
+    for fn in ("outputRequiredCells.reference", "outputRequiredCellsNotOrtho.reference"):
+        boxes_by_title, pending = {}, None
+        for line in open(os.path.join(dcl, fn)).read().split("\n"):
+            m = re.match(r"NUMBER of cells: (\d+) \((\d+) (\d+) (\d+)\)", line)
+            if m:
+                pending = [int(m.group(k)) for k in (2, 3, 4)]
+                continue
+            m = re.match(r"^([^\[#][^:]*): ([-0-9. ]+)$", line)
+            if m and len(m.group(2).split()) == 9:
+                boxes_by_title[m.group(1)] = [float(x) for x in m.group(2).split()]
+                continue
+            m = case_re.match(line)
+            if not m:
+                continue
+            box = boxes_by_title[m.group("title")] if m.group("title") else cube10
+            co = float(m.group("co"))
+            if pending is not None:
+                counts.append({"box": box, "cutoff": co, "ncells": pending})
+                pending = None
+            req.append({"box": box, "cutoff": co, "cell": [int(x) for x in m.group("cell").split(",")],
+                        "pbc": m.group("nopbc") is None, "cells": [int(x) for x in m.group("cells").split()]})
+    idx_boxes = [[10.0, 0, 0, 0, 10.0, 0, 0, 0, 10.0], [10.0, 10.0, 0, 0, 10.0, 0, 0, 0, 10.0],
+                 [10.0, 5.0, 3.0, 5.0, 10.0, 2.0, 3.0, 2.0, 10.0]]  # main.cpp testIndexes, cutoff 1.5
+    nc_idx = [int(l.split(":")[1]) for l in open(os.path.join(dcl, "outputIndexes.reference")) if l.startswith("Ncells")]
+    json.dump({"source": "regtest/tools/rt-make-CellLists (outputRequiredCells.reference, "
+                         "outputRequiredCellsNotOrtho.reference, outputIndexes.reference; boxes of main.cpp)",
+               "counts": counts, "required": req,
+               "index_boxes": [{"box": b, "cutoff": 1.5, "ncells_total": n} for b, n in zip(idx_boxes, nc_idx)]},
+              open(os.path.join(HERE, "rt_celllists.json"), "w"))
 
     # --- rt-Neigbourlist ---------------------------------------------------
     dnl = os.path.join(reg, "tools", "rt-Neigbourlist")

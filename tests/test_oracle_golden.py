@@ -369,3 +369,18 @@ def test_pbc_minimum_image_property(orc, kind):
         for f in fast:
             full = f + shifts @ box
             assert np.dot(f, f) - (full * full).sum(1).min() <= 1e-15 * max(1.0, np.dot(f, f)), (kind, box, f)
+
+
+def test_rt_make_celllists(orc, golden):
+    """regtest/tools/rt-make-CellLists: link-cell counts of orthorhombic,
+    flat and skewed boxes (LinkCells.cpp:99-122), and the cells searched
+    from corner, edge, face and middle cells with and without PBC
+    (LinkCells::addRequiredCells), sorted as the regtest prints them."""
+    g = golden("rt_celllists.json")
+    for r in g["counts"]:
+        assert orc.linkcells_ncells(np.array(r["box"]).reshape(3, 3), r["cutoff"]) == r["ncells"], r
+    for r in g["index_boxes"]:
+        assert int(np.prod(orc.linkcells_ncells(np.array(r["box"]).reshape(3, 3), r["cutoff"]))) == r["ncells_total"]
+    for r in g["required"]:
+        got = orc.linkcells_required(np.array(r["box"]).reshape(3, 3), r["cutoff"], r["cell"], r["pbc"])
+        assert got == r["cells"], r
