@@ -178,6 +178,10 @@ class Oracle:
         while True:
             out = np.empty(2 * cap, np.uint32)
             n = fn(mode, n0, n1, pos.reshape(-1), C.byref(p), int(do_pbc), float(cutoff), out, cap)
+            if n == -2:
+                raise ValueError("Cell lists cannot be built when passing a box with null volume")
+            if n < 0:
+                raise ValueError("this neighbour-list builder does not take PAIR mode")
             if n <= cap:
                 return out[:2 * n].reshape(-1, 2)
             cap = int(n)
@@ -333,6 +337,9 @@ class Reference:
         L.ref_switch_eval.argtypes = [C.c_char_p, C.c_int, _dp, C.c_int, _dp, _dp, C.c_char_p, C.c_int]
         L.ref_switch_params.argtypes = [C.c_char_p, _dp]
         L.ref_pbc.argtypes = [_dp, C.c_int, _dp, _dp, _dp, _dp]
+        L.ref_linkcells_required.argtypes = [_dp, C.c_double, C.POINTER(C.c_uint * 3), C.c_int,
+                                             C.POINTER(C.c_uint * 3), C.POINTER(C.c_uint * 27)]
+        L.ref_linkcells_required.restype = C.c_int
         L.ref_nl.argtypes = [C.c_int, C.c_int64, C.c_int64, _dp, _dp, C.c_int, C.c_double, C.c_int, _u32p,
                              C.c_int64]
         L.ref_nl.restype = C.c_int64
@@ -359,6 +366,17 @@ class Reference:
             raise ValueError(spec)
         return dict(zip(["d0", "dmax", "dmax_2", "invr0", "invr0_2", "stretch", "shift"], out))
 
+    def linkcells_required(self, box, cutoff, cell, use_pbc=True):
+        """(cell limits, sorted cells searched from the cell with indices cell)
+        by the reference's LinkCells."""
+        lim, req = (C.c_uint * 3)(), (C.c_uint * 27)()
+        n = self.L.ref_linkcells_required(np.ascontiguousarray(np.asarray(box, np.float64).reshape(9)),
+                                          float(cutoff), C.byref((C.c_uint * 3)(*cell)), int(use_pbc), C.byref(lim),
+                                          C.byref(req))
+        if n < 0:
+            raise ValueError("Cell lists cannot be built when passing a box with null volume")
+        return list(lim), sorted(req[:n])
+
     def pbc_distance(self, box, v1, v2):
         v1 = np.ascontiguousarray(np.asarray(v1, np.float64).reshape(-1, 3))
         v2 = np.ascontiguousarray(np.asarray(v2, np.float64).reshape(-1, 3))
@@ -375,6 +393,8 @@ class Reference:
         while True:
             out = np.empty(2 * cap, np.uint32)
             n = self.L.ref_nl(mode, n0, n1, pos, box, int(do_pbc), float(cutoff), int(cells), out, cap)
+            if n < 0:
+                raise ValueError("the reference refused the input (an assertion in NeighborList::update)")
             if n <= cap:
                 return out[:2 * n].reshape(-1, 2)
             cap = int(n)

@@ -1047,6 +1047,17 @@ int64_t orc_nl_linkcells(int mode, int64_t n0, int64_t n1, const double *pos, co
                          double cutoff, uint32_t *pairs, int64_t cap) {
   if (mode == ORC_NL_PAIR) return -1;
   int64_t nslots = (mode == ORC_NL_TWO) ? n0 + n1 : n0;
+  {
+    /* LinkCells::setupCells(pbc) (LinkCells.cpp:75-83): a box that is not all
+     * zero must have a volume above DBL_EPSILON */
+    const double *b = pbc->box;
+    int allzero = 1;
+    for (int k = 0; k < 9; k++)
+      if (b[k] != 0.0) allzero = 0;
+    const double det = b[0] * (b[4] * b[8] - b[5] * b[7]) - b[1] * (b[3] * b[8] - b[5] * b[6]) +
+                       b[2] * (b[3] * b[7] - b[4] * b[6]);
+    if (!allzero && !(det > DBL_EPSILON)) return -2;
+  }
   linkcells_t lc;
   lc_setup(&lc, pos, nslots, pbc, cutoff);
   int64_t ncell = (int64_t)lc.ncells[0] * lc.ncells[1] * lc.ncells[2];

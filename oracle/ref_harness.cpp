@@ -4,8 +4,7 @@
 // the reference's tool sources (src/tools/{Pbc,LatticeReduction,
 // SwitchingFunction,LinkCells,NeighborList,...}.cpp and src/lepton/*.cpp, read
 // in place, never copied) into oracle/_ref/libcoord_ref.so.  Tests use it to
-// pin the C restatement in coord_oracle.c bit for bit, and bench.py times its
-// pair loop as the reference CPU baseline where it has been built.
+// pin the C restatement in coord_oracle.c bit for bit.
 //
 // The pair loop below follows CoordinationBase::calculate
 // (src/colvar/CoordinationBase.cpp:142-231) using the reference's Vector,
@@ -13,6 +12,7 @@
 // operation is the reference's own code.
 #include "tools/AtomNumber.h"
 #include "tools/Communicator.h"
+#include "tools/LinkCells.h"
 #include "tools/NeighborList.h"
 #include "tools/Pbc.h"
 #include "tools/SwitchingFunction.h"
@@ -122,6 +122,31 @@ REF_API void ref_pbc(const double *box, int n, const double *v1, const double *v
   }
 }
 
+// LinkCells::setupCells(pbc) at the given cutoff, then addRequiredCells for the
+// cell with indices cell[3]: writes the cell limits and the required cells
+// (unsorted) and returns their number, or -1 when the reference refuses the
+// box.
+REF_API int ref_linkcells_required(const double *box, double cutoff, const unsigned *cell, int use_pbc,
+                                   unsigned *limits, unsigned *req) {
+  Pbc pbc;
+  pbc.setBox(make_box(box));
+  Communicator comm;
+  LinkCells cells(comm);
+  cells.setCutoff(cutoff);
+  try {
+    cells.setupCells(pbc);
+  } catch (const std::exception &) {  // the reference's volume assertion: -1
+    return -1;
+  }
+  const auto &lim = cells.getCellLimits();
+  for (int k = 0; k < 3; k++) limits[k] = lim[k];
+  std::vector<unsigned> r(27);
+  unsigned n = 0;
+  cells.addRequiredCells({cell[0], cell[1], cell[2]}, n, r, use_pbc != 0);
+  for (unsigned i = 0; i < n; i++) req[i] = r[i];
+  return (int)n;
+}
+
 // NeighborList construction + update(); returns nl.size() and writes the
 // pairs (reference order) when cap allows.  cutoff<=0: no NLIST (all pairs).
 REF_API int64_t ref_nl(int mode, int64_t n0, int64_t n1, const double *pos, const double *box, int do_pbc, double cutoff,
@@ -134,7 +159,11 @@ REF_API int64_t ref_nl(int mode, int64_t n0, int64_t n1, const double *pos, cons
   if (cutoff > 0) {
     std::vector<Vector> p(ns);
     for (int64_t i = 0; i < ns; i++) p[i] = Vector(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
-    nl->update(p);
+    try {
+      nl->update(p);
+    } catch (const std::exception &) {  // a reference assertion (e.g. a box without volume): -2
+      return -2;
+    }
   }
   const int64_t n = nl->size();
   for (int64_t i = 0; i < n && i < cap; i++) {

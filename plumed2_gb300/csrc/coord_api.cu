@@ -686,6 +686,23 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
         c->built_frames != n_frames)
       rebuild = true;
   }
+  // LinkCells::setupCells(pbc) (LinkCells.cpp:75-83): a cell list is built on
+  // the given box whenever it is not all zero (NOPBC included), and that box
+  // must have a volume above DBL_EPSILON; checked at each rebuild
+  if (rebuild && c->p.nlist == COORD_NL_CELLS) {
+    for (int f = 0; f < n_frames; f++) {
+      const double *b = boxes + 9 * (size_t)f;
+      if (box_is_zero(b)) continue;
+      const double det = b[0] * (b[4] * b[8] - b[5] * b[7]) - b[1] * (b[3] * b[8] - b[5] * b[6]) +
+                         b[2] * (b[3] * b[7] - b[4] * b[6]);
+      if (!(det > DBL_EPSILON)) {
+        char msg[128];
+        std::snprintf(msg, sizeof msg, "Cell lists cannot be built when passing a box with null volume. Volume is %g",
+                      det);
+        return c->fail(COORD_ERR_BOX, msg);
+      }
+    }
+  }
   // sizes
   if (c->cap == 0 && nl) c->cap = estimate_cap(c, boxes);
   {

@@ -168,6 +168,29 @@ def test_nlistcells_pair_set(orc, mode, pbc):
     _check("fp64", got, ref)
 
 
+@pytest.mark.parametrize("pbc", [True, False])
+def test_nlistcells_refuses_box_without_volume(orc, pbc):
+    """LinkCells::setupCells(pbc) (LinkCells.cpp:75-83): a cell list on a box
+    whose volume is not above DBL_EPSILON (here a left-handed one) is refused
+    at the rebuild with the reference's message, with or without NOPBC (the
+    list gets the box either way).  The context then builds on a proper box."""
+    from plumed2_gb300 import CoordError, _lib
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=0.8"
+    pos = jittered_lattice(1728, 0.31, 0.03, 6)
+    L = 12 * 0.31
+    c = Coordination("GROUPA=1-1728 SWITCH={%s} NLISTCELLS NL_CUTOFF=0.8 NL_STRIDE=2%s" % (spec, "" if pbc else " NOPBC"))
+    left = np.array([[0.0, L, 0.0], [L, 0.0, 0.0], [0.0, 0.0, L]])
+    with pytest.raises(CoordError, match="Cell lists cannot be built when passing a box with null volume") as e:
+        c.calculate(pos, left, 0)
+    assert e.value.status == _lib.ERR_BOX
+    box = np.diag([L] * 3)
+    got = c.calculate(pos, box, 0)
+    ref_pairs = orc.nl_linkcells(0, 1728, 0, pos, box, pbc, 0.8)
+    assert np.array_equal(_sorted(c.pairs()), _sorted(ref_pairs))
+    _check("fp64", got, orc.coordination(spec, pos, box, ref_pairs, do_pbc=pbc))
+
+
 @pytest.mark.parametrize("variant", ["rt42-cells", "rt42-cells-cos", "rt42-cells-gauss"])
 def test_rt42_cells_golden(orc, golden, variant):
     """regtest/basic/rt42-cells{,-cos,-gauss} through the C ABI: the NLIST and

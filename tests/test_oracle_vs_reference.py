@@ -92,3 +92,41 @@ def test_coordination_duplicates_and_self_skip(orc, ref):
     s2, d2, v2 = ref.coordination(spec, 0, len(sel), 0, pos, box, abs_index=sel.astype(np.int64))
     s1, d1, v1 = orc.coordination(spec, pos, box, orc.all_pairs(0, len(sel)), abs_index=sel)
     assert s1 == s2 and np.array_equal(d1, d2) and np.array_equal(v1, v2)
+
+
+def test_linkcells_required_cells(orc, ref):
+    """Link-cell counts and the cells searched from a cell, with and without
+    PBC, against the reference's LinkCells (setupCells(pbc) and
+    addRequiredCells): orthorhombic, flat and skewed boxes, cutoffs from
+    below one cell up to a third of the box, every kind of cell.  Boxes
+    with their rows permuted into a left-handed order have a negative
+    volume, and both refuse them, for the cells and for the list."""
+    rng = np.random.default_rng(12)
+    n = 0
+    for _ in range(300):
+        kind = rng.integers(0, 3)
+        if kind == 0:
+            box = np.diag(rng.uniform(1.0, 10.0, 3))
+        elif kind == 1:
+            box = np.diag([rng.uniform(0.5, 2.0), rng.uniform(4.0, 10.0), rng.uniform(4.0, 10.0)])[rng.permutation(3)]
+        else:
+            box = rng.uniform(-1.0, 1.0, (3, 3)) * 3.0 + np.eye(3) * 6.0
+        cut = rng.uniform(0.15, 0.5) * min(np.abs(np.linalg.det(box)) ** (1 / 3), 6.0)
+        if np.linalg.det(box) <= 0:  # left-handed: both refuse it (LinkCells.cpp:81)
+            with pytest.raises(ValueError, match="null volume"):
+                ref.linkcells_required(box, cut, [0, 0, 0])
+            pos = rng.random((40, 3)) @ box
+            with pytest.raises(ValueError, match="null volume"):
+                orc.nl_linkcells(0, 40, 0, pos, box, True, cut)
+            with pytest.raises(ValueError, match="refused"):
+                ref.nl(0, 40, 0, pos, box, True, cut, cells=True)
+            n += 2
+            continue
+        lim = orc.linkcells_ncells(box, cut)
+        cell = [int(rng.integers(0, lim[k])) for k in range(3)]
+        for use_pbc in (True, False):
+            rlim, rreq = ref.linkcells_required(box, cut, cell, use_pbc)
+            assert lim == rlim, (box, cut)
+            assert orc.linkcells_required(box, cut, cell, use_pbc) == rreq, (box, cut, cell, use_pbc)
+            n += 1
+    assert n == 600
