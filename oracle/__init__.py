@@ -52,6 +52,11 @@ class _Pbc(C.Structure):
                 ("nshift", C.c_int * 8), ("shift", C.c_double * (8 * 32 * 3))]
 
 
+class _Expr(C.Structure):  # orc_expr (orc_expr.h)
+    _fields_ = [("ncode", C.c_int), ("code", C.c_int * 256), ("nconst", C.c_int), ("cst", C.c_double * 64),
+                ("var_x2", C.c_int)]
+
+
 class _Switch(C.Structure):
     _fields_ = [("type", C.c_int), ("d0", C.c_double), ("dmax", C.c_double), ("dmax_2", C.c_double),
                 ("invr0", C.c_double), ("invr0_2", C.c_double), ("stretch", C.c_double),
@@ -59,7 +64,7 @@ class _Switch(C.Structure):
                 ("preDfunc", C.c_double), ("preSecDev", C.c_double), ("nnf", C.c_int), ("mmf", C.c_int),
                 ("preDfuncF", C.c_double), ("preSecDevF", C.c_double), ("a", C.c_int), ("b", C.c_int),
                 ("c", C.c_double), ("d", C.c_double), ("beta", C.c_double), ("lambda_", C.c_double),
-                ("ref", C.c_double)]
+                ("ref", C.c_double), ("expr", _Expr)]
 
 
 class _Pairing(C.Structure):

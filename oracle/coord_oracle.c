@@ -431,9 +431,41 @@ static vd_t nativeq_calculate(const orc_switch *s, double distance) {
   return r;
 }
 
+/* leptonSwitch::calculateSqr (SwitchingFunction.cpp:730-749), FUNC of x2 */
+static vd_t custom_calculate_x2(const orc_switch *s, double distance2) {
+  vd_t r = {0.0, 0.0};
+  if (distance2 <= s->dmax_2) {
+    const double rdist_2 = distance2 * s->invr0_2;
+    orc_expr_eval(&s->expr, rdist_2, &r.f, &r.d);
+    r.d *= 2 * s->invr0_2;
+    r.f = r.f * s->stretch + s->shift;
+    r.d *= s->stretch;
+  }
+  return r;
+}
+
+/* leptonSwitch::calculate (SwitchingFunction.cpp:708-728) */
+static vd_t custom_calculate(const orc_switch *s, double distance) {
+  if (s->expr.var_x2) return custom_calculate_x2(s, distance * distance);
+  vd_t r = {0.0, 0.0};
+  if (distance <= s->dmax) {
+    r.f = 1.0;
+    const double rdist = (distance - s->d0) * s->invr0;
+    if (rdist > 0.0) {
+      orc_expr_eval(&s->expr, rdist, &r.f, &r.d);
+      r.d *= s->invr0;
+      r.d /= distance;
+    }
+    r.f = r.f * s->stretch + s->shift;
+    r.d *= s->stretch;
+  }
+  return r;
+}
+
 /* baseSwitch::calculate (SwitchingFunction.cpp:130-147) with applystretch (:121-127) */
 static vd_t sw_calculate(const orc_switch *s, double distance) {
   if (s->type == ORC_SW_Q) return nativeq_calculate(s, distance);
+  if (s->type == ORC_SW_CUSTOM) return custom_calculate(s, distance);
   vd_t r = {0.0, 0.0};
   const double rdist = (distance - s->d0) * s->invr0;
   if (distance > s->dmax) return r;
@@ -455,6 +487,9 @@ static vd_t sw_calculate(const orc_switch *s, double distance) {
 static vd_t sw_calculate_sqr(const orc_switch *s, double distance2) {
   vd_t r = {0.0, 0.0};
   switch (s->type) {
+  case ORC_SW_CUSTOM:
+    if (s->expr.var_x2) return custom_calculate_x2(s, distance2);
+    return custom_calculate(s, sqrt(distance2));
   case ORC_SW_RATFIX:
     if (distance2 <= s->dmax_2) {
       const double rdist = distance2 * s->invr0_2;
@@ -612,6 +647,17 @@ static int parse_int(words_t *W, const char *key, int *v) {
     }
   return 0;
 }
+/* the text after "KEY=" (removed once read); 1 found, 0 absent */
+static int parse_string(words_t *W, const char *key, char *out, size_t outlen) {
+  size_t kl = strlen(key);
+  for (int i = 0; i < W->n; i++)
+    if (strncmp(W->w[i], key, kl) == 0 && W->w[i][kl] == '=') {
+      snprintf(out, outlen, "%s", W->w[i] + kl + 1);
+      erase_word(W, i);
+      return 1;
+    }
+  return 0;
+}
 static int parse_flag(words_t *W, const char *key) {
   for (int i = 0; i < W->n; i++)
     if (strcmp(W->w[i], key) == 0) {
@@ -689,8 +735,11 @@ int orc_switch_set(orc_switch *s, const char *definition, char *err, int errlen)
       data_init(s, d0, dmax, r0);
       s->type = ORC_SW_COSINUS;
     } else if (strcmp(name, "CUSTOM") == 0 || strcmp(name, "MATHEVAL") == 0) {
-      snprintf(err, errlen, "CUSTOM/MATHEVAL switching functions are not restated in the oracle");
-      return 1;
+      char func[128] = "";
+      parse_string(&W, "FUNC", func, sizeof func);
+      data_init(s, d0, dmax, r0);
+      s->type = ORC_SW_CUSTOM;
+      if (orc_expr_compile(&s->expr, func, err, errlen)) return 1;
     } else {
       snprintf(err, errlen, "cannot understand switching function type '%s'", name);
       return 1;

@@ -17,6 +17,8 @@
 #ifndef COORD_ORACLE_H
 #define COORD_ORACLE_H
 #include <stdint.h>
+
+#include "orc_expr.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -50,7 +52,8 @@ enum {
   ORC_SW_RATIONAL_SIMPLE,      /* rational<standard,simplified> */
   ORC_SW_RATIONAL_SIMPLE_FAST, /* rational<fast,simplified> */
   ORC_SW_EXP, ORC_SW_GAUSSIAN, ORC_SW_FASTGAUSSIAN, ORC_SW_SMAP,
-  ORC_SW_CUBIC, ORC_SW_TANH, ORC_SW_COSINUS, ORC_SW_Q
+  ORC_SW_CUBIC, ORC_SW_TANH, ORC_SW_COSINUS, ORC_SW_Q,
+  ORC_SW_CUSTOM         /* leptonSwitch (SwitchingFunction.cpp:553-760): FUNC of x or x2 */
 };
 
 typedef struct {           /* switchContainers::Data (SwitchingFunction.h:57-95) */
@@ -63,6 +66,7 @@ typedef struct {           /* switchContainers::Data (SwitchingFunction.h:57-95)
   int a, b;
   double c, d;
   double beta, lambda, ref;
+  orc_expr expr;           /* CUSTOM: the compiled FUNC */
 } orc_switch;
 
 /* SwitchingFunction::set(string) (SwitchingFunction.cpp:1055-1159).

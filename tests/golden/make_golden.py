@@ -212,9 +212,11 @@ def main(ref):
                "c": [checks["c"][k] for k in keep], "e": [checks["e"][k] for k in keep],
                "g": [checks["g"][k] for k in keep], "c_single": [colvar_c1[k] for k in keep],
                "ff_forces": [forces[k] for k in keep], "ff_virial": [virials[k] for k in keep],
-               "inputs": {"c": "R0SYNTAX 6 0 1.0 0.0 twolist", "d": "RATIONAL R_0=1 (CUSTOM 1/(1+x^6))",
-                          "e": "R0SYNTAX 7 0 1.0 0.1 twolist", "f": "RATIONAL R_0=1 D_0=0.1 NN=7 MM=14 (CUSTOM)",
-                          "g": "EXP R_0=1", "c_single": "R0SYNTAX 6 0 1.0 0.0 single",
+               "inputs": {"c": "R0SYNTAX 6 0 1.0 0.0 twolist", "d": "CUSTOM FUNC=1/(1+x^6) R_0=1",
+                          "dfast": "CUSTOM FUNC=1/(1+x2^3) R_0=1",
+                          "e": "R0SYNTAX 7 0 1.0 0.1 twolist", "f": "CUSTOM FUNC=1/(1+x^7) R_0=1 D_0=0.1",
+                          "g": "EXP R_0=1", "h": "CUSTOM FUNC=exp(-x) R_0=1",
+                          "c_single": "R0SYNTAX 6 0 1.0 0.0 single",
                           "forces": "-(dc+dd) - 0.001*(dc - 0.5 dd - 0.5 dfast + de - df + dg - dh)"}},
               open(os.path.join(HERE, "rt42.json"), "w"))
 

@@ -51,8 +51,9 @@ def test_rt42_values_forces_virial(orc, golden):
     """regtest/basic/rt42 (+rt42c): 108 atoms in a triclinic box.
 
     c, e, g at %8.4f; forces and full virial of RESTRAINT SLOPE=1 on c+d (plus
-    the SLOPE=0.001 restraint on the CUSTOM cross-check combination) at %10.5f.
-    CUSTOM switches are evaluated as the built-in switch with the same formula.
+    the SLOPE=0.001 restraint on the CUSTOM cross-check combination
+    c - d/2 - dfast/2 + e - f + g - h) at %10.5f, with d, dfast, f and h the
+    regtest's own CUSTOM (lepton) definitions.
     """
     g = golden("rt42.json")
     for fi in range(len(g["frames"])):
@@ -68,17 +69,19 @@ def test_rt42_values_forces_virial(orc, golden):
             return s, d[:n] + d[n:], v
 
         sc, dc, vc = cv("R0SYNTAX 6 0 1.0 0.0")
-        sd, dd, vd = cv("RATIONAL R_0=1")
+        sd, dd, vd = cv("CUSTOM FUNC=1/(1+x^6) R_0=1")
+        _, dq, vq = cv("CUSTOM FUNC=1/(1+x2^3) R_0=1")
         se, de, ve = cv("R0SYNTAX 7 0 1.0 0.1")
-        sf, df, vf = cv("RATIONAL R_0=1 D_0=0.1 NN=7 MM=14")
-        sg, _, _ = cv("EXP R_0=1")
+        sf, df, vf = cv("CUSTOM FUNC=1/(1+x^7) R_0=1 D_0=0.1")
+        sg, dg, vg = cv("EXP R_0=1")
+        _, dh, vh = cv("CUSTOM FUNC=exp(-x) R_0=1")
         s1, _, _ = orc.coordination("R0SYNTAX 6 0 1.0 0.0", pos, box, orc.all_pairs(0, n))
         assert abs(sc - g["c"][fi]) <= 5.01e-5
         assert abs(se - g["e"][fi]) <= 5.01e-5
         assert abs(sg - g["g"][fi]) <= 5.01e-5
         assert abs(s1 - g["c_single"][fi]) <= 5.01e-5
-        F = -(dc + dd) - 0.001 * (dc - dd + de - df)
-        V = -(vc + vd) - 0.001 * (vc - vd + ve - vf)
+        F = -(dc + dd) - 0.001 * (dc - 0.5 * dd - 0.5 * dq + de - df + dg - dh)
+        V = -(vc + vd) - 0.001 * (vc - 0.5 * vd - 0.5 * vq + ve - vf + vg - vh)
         assert np.abs(F - np.array(g["ff_forces"][fi])).max() <= 5.01e-6
         assert np.abs(V - np.array(g["ff_virial"][fi]).reshape(3, 3)).max() <= 5.01e-6
 

@@ -2,7 +2,10 @@
 
 Runs where oracle/_ref (the reference sources compiled by oracle/Makefile)
 exists; skipped elsewhere.  Serial order and -ffp-contract=off on both sides
-make every comparison exact (np.array_equal), not toleranced.
+make every comparison exact (np.array_equal), not toleranced, except for
+CUSTOM switching functions: the reference differentiates the lepton
+expression symbolically and simplifies it, the oracle differentiates it
+forward, so those agree within 1e-13 relative (most results bit for bit).
 """
 import numpy as np
 import pytest
@@ -130,3 +133,64 @@ def test_linkcells_required_cells(orc, ref):
             assert orc.linkcells_required(box, cut, cell, use_pbc) == rreq, (box, cut, cell, use_pbc)
             n += 1
     assert n == 600
+
+
+CUSTOM_FUNCS = [
+    "1/(1+x^6)", "(1+x^3)/(1+x^9)", "exp(-x)", "exp(-0.5*x^2)", "1/(1+x2^3)", "exp(-x2/2)",
+    "step(x)*0.5*(cos(x*pi)+1)+step(-x)*1.0", "1-tanh(x)", "erfc(x)", "1/(1+exp(10*(x-1)))",
+    "select(step(1-x),1-x^2,0)", "max(0,1-x)^2", "min(1,1/x^3)", "abs(x-1.3)*exp(-x)", "sqrt(1+x)^-3",
+    "x^x*exp(-3*x)", "atan2(1,x)/pi", "(cos(pi*x)+1)/2*step(1-x)", "cube(1-x)*step(1-x)", "recip(1+square(x))",
+    "log(1+exp(-x))", "1/cosh(x)^2", "-x^2+1", "2^-x", "ceil(3-x)/3*exp(-x)", "sinh(x)/cosh(x)", "1/(1+x^2.5)",
+    "2*pi*exp(-x)/(2*pi)", "1e-1*x^-2/(1+1e-1*x^-2)", "sec(x/4)-csc(1+x)*sin(1+x)", "cot(1+x)*tan(1+x)*exp(-x)",
+    "asin(1/(1+x))+acos(1/(1+x))-pi_2+exp(-x)"]
+
+
+def _close(a, b, tol):
+    a, b = np.asarray(a), np.asarray(b)
+    same = (a == b) | (np.abs(a - b) <= tol * np.maximum(np.abs(b), 1e-300)) | (np.isnan(a) & np.isnan(b))
+    return bool(np.all(same))
+
+
+@pytest.mark.parametrize("func", CUSTOM_FUNCS)
+def test_custom_switch(orc, ref, func):
+    """CUSTOM (lepton) switching functions of x and x2, with D_0, D_MAX and
+    NOSTRETCH, against the reference's leptonSwitch, both calculate and
+    calculateSqr, across and beyond D_MAX."""
+    x = np.concatenate([np.linspace(0.01, 3.0, 300), [0.1, 0.2, 1.0]])
+    for extra in ("R_0=0.7", "R_0=1.1 D_0=0.2", "R_0=0.9 D_MAX=2.5", "R_0=0.5 D_0=0.1 D_MAX=1.9 NOSTRETCH"):
+        spec = "CUSTOM FUNC=%s %s" % (func, extra)
+        for squared in (True, False):
+            xx = x * x if squared else x
+            f1, d1 = orc.switch_eval(spec, xx, squared)
+            f2, d2 = ref.switch_eval(spec, xx, squared)
+            assert _close(f1, f2, 1e-13) and _close(d1, d2, 1e-13), spec
+
+
+def test_custom_switch_refusals(orc, ref):
+    """Two variables, a name other than x or x2, an unknown function: both
+    refuse, with the reference's messages for the first two kinds."""
+    x = np.array([0.5])
+    for func in ("x*x2", "y+x", "foo(x)"):
+        spec = "CUSTOM FUNC=%s R_0=1" % func
+        with pytest.raises(ValueError):
+            ref.switch_eval(spec, x)
+        with pytest.raises(ValueError) as e:
+            orc.switch_eval(spec, x)
+        want = ("unknown function: foo" if func == "foo(x)" else
+                "Please declare a function with only ONE argument that can only be x or x2")
+        assert want in str(e.value)
+
+
+def test_coordination_custom_switch(orc, ref):
+    """The CV with a CUSTOM switch (regtest/basic/rt42's d) on single, two-list
+    and PAIR groups, with and without a list."""
+    pos = jittered_lattice(1000, 0.30, 0.03, 6)
+    box = np.diag([3.0] * 3)
+    for spec in ("CUSTOM FUNC=1/(1+x^6) R_0=0.3 D_MAX=1.0", "CUSTOM FUNC=exp(-x2/2) R_0=0.25 D_MAX=0.9"):
+        for mode, n0, n1, cut in ((0, 1000, 0, 0.0), (0, 1000, 0, 1.1), (1, 400, 600, 0.0), (2, 500, 500, 0.0)):
+            s2, d2, v2 = ref.coordination(spec, mode, n0, n1, pos, box, nl_cutoff=cut)
+            pairs = orc.all_pairs(mode, n0, n1) if cut == 0 else orc.nl_classic(mode, n0, n1, pos, box, True, cut)
+            s1, d1, v1 = orc.coordination(spec, pos, box, pairs)
+            assert abs(s1 - s2) <= 1e-13 * abs(s2)
+            assert np.abs(d1 - d2).max() <= 1e-12 * np.abs(d2).max()
+            assert np.abs(v1 - v2).max() <= 1e-12 * np.abs(v2).max()
