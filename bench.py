@@ -239,9 +239,11 @@ def run_reference(args):
     nthreads = orc.max_threads()
     # Each timed step is charged its pair loop plus a tenth of the latest list
     # build (NL_STRIDE=10), so the figure does not depend on how many rebuilds
-    # fall inside the timed window.  The build is the reference's serial
-    # cell-list update (NLISTCELLS, NeighborList.cpp:177-231), the faster of its
-    # two builders; its default NLIST build tests all N(N-1)/2 pairs.  The
+    # fall inside the timed window.  The build is the port's classic list
+    # (NLIST: every pair within NL_CUTOFF by the reference's exact test,
+    # NeighborList.cpp:237-308) found through link cells on one thread
+    # (orc_nl_classic_cells), which gives the same pair set as the reference's
+    # loop over all N(N-1)/2 candidates in a small fraction of its time.  The
     # reference's own code (oracle/_ref) builds a list inside every call, so it
     # pins the port in the tests rather than being timed here.
     pairs = None

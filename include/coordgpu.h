@@ -290,7 +290,11 @@ int coord_cmap_forward(coord_cmap *m, const double *pos, const double box[9], do
  * ctx comes from coord_create (which touches no CUDA); do not call
  * coord_set_groups on it.  Groups are host arrays of absolute indices; pos,
  * s, deriv and virial are device pointers on the current device; box is
- * host; stream is a cudaStream_t or NULL.  The call allocates nothing and
+ * host; stream is a cudaStream_t or NULL.  pos and deriv are indexed by
+ * slot, as for coord_forward: (n_a + n_b) rows of 3 doubles, group_a's atoms
+ * then group_b's in the order given, an atom listed twice taking two rows.
+ * They are not the engine's whole position and force arrays indexed by
+ * atom number.  The call allocates nothing and
  * clears the parts of the shared array that must start at zero; calls that
  * overlap on the GPU share the array and race.  The first call on a device
  * looks the array up with cudaGetSymbolAddress: make it before any stream

@@ -25,7 +25,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libcoord_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libcoord_ref.so")
-REFERENCE_TREE = "/root/reference"
+# the reference source tree (read only); PLUMED_REFERENCE_TREE overrides the default
+REFERENCE_TREE = os.environ.get("PLUMED_REFERENCE_TREE", "/root/reference")
 
 MODE_SINGLE, MODE_TWO, MODE_PAIR = 0, 1, 2
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -40,7 +41,7 @@ def build(reference: bool | None = None, quiet: bool = True) -> None:
         reference = os.path.isdir(os.path.join(REFERENCE_TREE, "src", "tools"))
     if reference:
         targets.append("ref")
-    out = subprocess.run(["make", "-s", "-j8", "-C", HERE] + targets,
+    out = subprocess.run(["make", "-s", "-j8", "-C", HERE, "REF=" + REFERENCE_TREE] + targets,
                          capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)

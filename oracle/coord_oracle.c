@@ -594,11 +594,13 @@ int orc_switch_set_rational(orc_switch *s, int nn, int mm, double r0, double d0)
 #define ORC_MAXW 64
 typedef struct {
   int n;
+  int overflow; /* a word longer than the buffer, or more than ORC_MAXW words */
   char w[ORC_MAXW][128];
 } words_t;
 
 static void split_words(const char *def, words_t *W) {
   W->n = 0;
+  W->overflow = 0;
   const char *p = def;
   while (*p) {
     while (*p == ' ' || *p == '\t' || *p == '\n' || *p == '{' || *p == '}') p++;
@@ -609,6 +611,8 @@ static void split_words(const char *def, words_t *W) {
       memcpy(W->w[W->n], p, len);
       W->w[W->n][len] = 0;
       W->n++;
+    } else {
+      W->overflow = 1;
     }
     p += len;
   }
@@ -647,14 +651,15 @@ static int parse_int(words_t *W, const char *key, int *v) {
     }
   return 0;
 }
-/* the text after "KEY=" (removed once read); 1 found, 0 absent */
+/* the text after "KEY=" (removed once read); 1 found, 0 absent, -1 longer
+ * than out */
 static int parse_string(words_t *W, const char *key, char *out, size_t outlen) {
   size_t kl = strlen(key);
   for (int i = 0; i < W->n; i++)
     if (strncmp(W->w[i], key, kl) == 0 && W->w[i][kl] == '=') {
-      snprintf(out, outlen, "%s", W->w[i] + kl + 1);
+      const int n = snprintf(out, outlen, "%s", W->w[i] + kl + 1);
       erase_word(W, i);
-      return 1;
+      return (n < 0 || (size_t)n >= outlen) ? -1 : 1;
     }
   return 0;
 }
@@ -672,6 +677,12 @@ int orc_switch_set(orc_switch *s, const char *definition, char *err, int errlen)
   words_t W;
   split_words(definition, &W);
   memset(s, 0, sizeof *s);
+  if (W.overflow) {
+    /* a word cut short could still parse as a different valid input */
+    snprintf(err, errlen, "switching function input has a word longer than 126 characters or more than %d words "
+             "(the oracle's limits)", ORC_MAXW);
+    return 1;
+  }
   if (W.n < 1) {
     snprintf(err, errlen, "missing all input for switching function");
     return 1;
@@ -736,7 +747,12 @@ int orc_switch_set(orc_switch *s, const char *definition, char *err, int errlen)
       s->type = ORC_SW_COSINUS;
     } else if (strcmp(name, "CUSTOM") == 0 || strcmp(name, "MATHEVAL") == 0) {
       char func[128] = "";
-      parse_string(&W, "FUNC", func, sizeof func);
+      const int got = parse_string(&W, "FUNC", func, sizeof func);
+      if (got <= 0) {
+        snprintf(err, errlen, got < 0 ? "FUNC is longer than the oracle's expression buffer"
+                                      : "CUSTOM switching function without FUNC");
+        return 1;
+      }
       data_init(s, d0, dmax, r0);
       s->type = ORC_SW_CUSTOM;
       if (orc_expr_compile(&s->expr, func, err, errlen)) return 1;

@@ -449,4 +449,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import REFERENCE_TREE
+    main(sys.argv[1] if len(sys.argv) > 1 else REFERENCE_TREE)

@@ -183,7 +183,7 @@ def test_nlistcells_refuses_box_without_volume(orc, pbc):
     left = np.array([[0.0, L, 0.0], [L, 0.0, 0.0], [0.0, 0.0, L]])
     with pytest.raises(CoordError, match="Cell lists cannot be built when passing a box with null volume") as e:
         c.calculate(pos, left, 0)
-    assert e.value.status == _lib.ERR_BOX
+    assert e.value.status == _lib.COORD_ERR_BOX
     box = np.diag([L] * 3)
     got = c.calculate(pos, box, 0)
     ref_pairs = orc.nl_linkcells(0, 1728, 0, pos, box, pbc, 0.8)

@@ -387,3 +387,16 @@ def test_rt_make_celllists(orc, golden):
     for r in g["required"]:
         got = orc.linkcells_required(np.array(r["box"]).reshape(3, 3), r["cutoff"], r["cell"], r["pbc"])
         assert got == r["cells"], r
+
+
+def test_custom_switch_input_the_oracle_cannot_hold_is_refused(orc):
+    """A CUSTOM FUNC longer than the oracle's expression buffer, or one missing,
+    is an error: a silently shortened expression could still compile into a
+    different valid function and pin the checks to the wrong formula."""
+    long_func = "FUNC=" + "+".join(["x"] * 80)
+    with pytest.raises(ValueError, match="longer"):
+        orc.switch("CUSTOM %s R_0=0.3" % long_func)
+    with pytest.raises(ValueError, match="without FUNC"):
+        orc.switch("CUSTOM R_0=0.3")
+    # a short expression still compiles
+    orc.switch("CUSTOM FUNC=1/(1+x^6) R_0=0.3")

@@ -3,12 +3,16 @@ PLUMED source tree is present) and only calls entry points the C ABI declares.""
 import os
 import re
 import subprocess
+import sys
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PLUGIN = os.path.join(ROOT, "plumed2_gb300", "plugin", "CoordinationGPU.cpp")
-PLUMED_SRC = "/root/reference/src"
+sys.path.insert(0, ROOT)
+from oracle import REFERENCE_TREE  # noqa: E402
+
+PLUMED_SRC = os.path.join(REFERENCE_TREE, "src")
 
 
 def test_plugin_uses_declared_abi_only():
