@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="small sizes (for profiling captures)")
+    ap.add_argument("--c2-steps", type=int, default=3,
+                    help="timed graph replays of the batched 256-action workload (0: skip it)")
+    ap.add_argument("--workload", default="c4", choices=["c4", "c2"],
+                    help="c2: only the batched 256-action workload, as its own line")
     return ap.parse_args()
 
 
@@ -199,9 +203,27 @@ def make_walkers(n_walkers, n_atoms, first):
     return out, np.diag([BOX * (n_atoms / N_ATOMS) ** (1 / 3)] * 3)
 
 
-def cpu_baseline(frames, box, budget_s=10.0):
+def accuracy_against(ref, got, pairs_ref=None, pairs_got=None):
+    """Errors of one walker's GPU result against the FP64 oracle's: |dCV|/CV, the norm-wise
+    max_i |dF_i| / max_i |F_i| of the derivatives, max |dvirial| / max |virial|, and whether the
+    neighbour-list pair sets are identical."""
+    s0, d0, v0 = ref
+    s1, d1, v1 = got
+    fn = np.sqrt((d0 ** 2).sum(axis=1)).max()
+    out = {"cv_rel": abs(s1 - s0) / abs(s0),
+           "force_rel_normwise": float(np.sqrt(((d1 - d0) ** 2).sum(axis=1)).max() / fn),
+           "virial_rel": float(np.abs(np.asarray(v1).reshape(9) - np.asarray(v0).reshape(9)).max() /
+                               np.abs(np.asarray(v0)).max())}
+    if pairs_ref is not None and pairs_got is not None:
+        out["nl_bit_exact"] = bool(np.array_equal(pairs_ref, pairs_got))
+    return out
+
+
+def cpu_baseline(frames, box, budget_s=10.0, gpu_check=None):
     """The reference algorithm on this host's cores: classic neighbour list once
-    (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop."""
+    (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop.  The same
+    oracle results check the GPU's (gpu_check: walker -> {"mixed": (s, deriv, virial,
+    sorted pairs), "fp64": (s, deriv, virial)}), untimed."""
     import oracle
     oracle.build()
     orc = oracle.Oracle()
@@ -213,16 +235,123 @@ def cpu_baseline(frames, box, budget_s=10.0):
     kind = "port"
     nthreads = orc.max_threads()
     reps, t_loop = 0, 0.0
+    ref0 = None
     while t_loop < budget_s or reps == 0:
         t0 = time.perf_counter()
-        orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
+        ref0 = orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
         t_loop += time.perf_counter() - t0
         reps += 1
     per_step = t_loop / reps + t_build / 10.0
-    return {"value": len(pairs) / per_step, "unit": "pair-evals/s", "cores": nthreads, "kind": kind,
-            "sample": "1 walker of %d atoms: classic NL build once (%.2f s, serial, amortised /10) + %d pair "
-                      "loops over %d NL pairs (OpenMP, %d threads)" % (n, t_build, reps, len(pairs), nthreads),
-            "ms_per_step": per_step * 1e3}
+    out = {"value": len(pairs) / per_step, "unit": "pair-evals/s", "cores": nthreads, "kind": kind,
+           "sample": "1 walker of %d atoms: classic NL build once (%.2f s, serial, amortised /10) + %d pair "
+                     "loops over %d NL pairs (OpenMP, %d threads)" % (n, t_build, reps, len(pairs), nthreads),
+           "ms_per_step": per_step * 1e3}
+    # one thread, one pair loop (the reference's serial CoordinationBase loop)
+    t0 = time.perf_counter()
+    orc.coordination(SPEC, pos, box, pairs, nthreads=1)
+    t1 = time.perf_counter() - t0
+    out["one_thread"] = {"value": len(pairs) / (t1 + t_build / 10.0), "unit": "pair-evals/s",
+                         "pair_loop_ms": t1 * 1e3, "build_ms_amortised": t_build / 10.0 * 1e3}
+    if gpu_check:
+        acc = {}
+        for w, got in sorted(gpu_check.items()):
+            if w == 0:
+                pw, ref = pairs, ref0
+            else:
+                pw = orc.nl_classic_cells(0, n, 0, frames[w], box, True, 0.8)
+                ref = orc.coordination(SPEC, frames[w], box, pw, nthreads=nthreads)
+            e = {"mixed": accuracy_against(ref, got["mixed"][:3], pw, got["mixed"][3])}
+            if "fp64" in got:
+                e["fp64"] = accuracy_against(ref, got["fp64"])
+            acc["walker_%d" % w] = e
+        out["accuracy"] = acc
+    return out
+
+
+def run_c2(dev, steps=3, warmup=2, frames_per_launch=64, cpu=True):
+    """The batched uneven-actions workload: 256 single-list COORDINATION actions over one
+    100,000-atom system (GROUPA sizes log-uniform in [16, 4096], R_0 ~ U(0.25, 0.45), NN=6 MM=12
+    D_MAX=1.0, no list), mixed precision, 64 frames per launch through one coord_multi batch
+    replayed as a captured CUDA graph.  Returns the measured figures (pair-evals/s over the
+    timed replays, CUDA events on the batch's stream)."""
+    import ctypes as C
+    import torch
+    from plumed2_gb300 import _lib
+    from plumed2_gb300 import frames as FR
+    from plumed2_gb300.action import Coordination
+    L = _lib.load()
+    pos, box = FR.workload_c2_system()
+    sizes, starts, r0 = FR.workload_c2_actions(256)
+    specs = ["RATIONAL R_0=%.6f NN=6 MM=12 D_MAX=1.0" % x for x in r0]
+    acts = [Coordination("GROUPA=%d-%d SWITCH={%s}" % (st + 1, st + sz, sp), precision="mixed")
+            for sz, st, sp in zip(sizes, starts, specs)]
+    for a in acts:
+        a._ensure_groups()
+    arr = (C.c_void_p * len(acts))(*[a._ctx.value for a in acts])
+    m = C.c_void_p()
+    if L.coord_multi_create(arr, len(acts), len(pos), C.byref(m)) != 0:
+        raise RuntimeError(L.coord_multi_last_error(m).decode())
+    per = C.c_int64()
+    o = C.c_int64()
+    L.coord_multi_deriv_offset(m, 0, C.byref(o), C.byref(per))
+    F = frames_per_launch
+    # frame f: the system moved by f Gaussian steps of 0.002 nm
+    rng = np.random.default_rng(77)
+    fr = np.empty((F,) + pos.shape)
+    fr[0] = pos
+    for f in range(1, F):
+        fr[f] = fr[f - 1] + rng.normal(0.0, 0.002, size=pos.shape)
+    tpos = torch.tensor(fr, dtype=torch.float64, device=dev)
+    s = torch.zeros(F, len(acts), dtype=torch.float64, device=dev)
+    der = torch.zeros(F, per.value, dtype=torch.float64, device=dev)
+    vir = torch.zeros(F, len(acts), 9, dtype=torch.float64, device=dev)
+    boxes = np.ascontiguousarray(np.stack([box] * F).reshape(F, 9))
+    stream = torch.cuda.Stream(device=dev)
+    L.coord_multi_use_graph(m, 1)
+    args = (m, F, C.c_void_p(tpos.data_ptr()), boxes.ctypes.data_as(C.POINTER(C.c_double)), 0,
+            C.c_void_p(s.data_ptr()), C.c_void_p(der.data_ptr()), C.c_void_p(vir.data_ptr()),
+            C.c_void_p(stream.cuda_stream))
+    for _ in range(warmup):
+        if L.coord_multi_forward_device(*args) != 0:
+            raise RuntimeError(L.coord_multi_last_error(m).decode())
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = _lib.launch_count()
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(steps):
+            L.coord_multi_forward_device(*args)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    t = ev0.elapsed_time(ev1) * 1e-3 / steps
+    pairs_frame = int(sum(int(n) * (int(n) - 1) // 2 for n in sizes))
+    pairs = pairs_frame * F
+    out = {"workload": "100,000-atom jittered sc lattice (14.5 nm box), 256 single-list actions, GROUPA sizes "
+                       "log-uniform in [16, 4096], R_0 ~ U(0.25, 0.45), NN=6 MM=12 D_MAX=1.0, no list, mixed "
+                       "precision, %d frames per launch, one captured CUDA graph per launch" % F,
+           "value": pairs / t, "unit": "pair-evals/s", "ms_per_launch": t * 1e3, "pairs_per_launch": pairs,
+           "us_per_frame": t / F * 1e6, "launches_per_replay": (_lib.launch_count() - l0) / steps,
+           "fp32": {"achieved_tflops": pairs * ALG_FLOPS_PER_PAIR / t / 1e12}}
+    if cpu:
+        # the reference algorithm on the host cores: every action's pair loop on one frame
+        import oracle
+        oracle.build()
+        orc = oracle.Oracle()
+        nth = orc.max_threads()
+        t0 = time.perf_counter()
+        s_ref = []
+        for sz, st, sp in zip(sizes, starts, specs):
+            sz, st = int(sz), int(st)
+            s_ref.append(orc.coordination(sp, pos[st:st + sz], box, orc.all_pairs(0, sz), nthreads=nth)[0])
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": pairs_frame / tc, "unit": "pair-evals/s", "cores": nth, "kind": "port",
+                               "sample": "one frame of the 256 actions (%d pairs), OpenMP pair loops" % pairs_frame}
+        s0 = s[0].cpu().numpy()
+        out["accuracy"] = {"cv_rel_max_over_actions": float(np.max(np.abs(s0 - np.array(s_ref)) / np.abs(s_ref)))}
+    L.coord_multi_destroy(m)
+    for a in acts:
+        a.close()
+    return out
 
 
 def run_reference(args):
@@ -372,6 +501,22 @@ def run_ours(args):
     ev1.record()
     torch.cuda.synchronize()
     t_plain_step = ev0.elapsed_time(ev1) * 1e-3 / 5
+    # the mixed results of that step for two walkers (checked against the FP64 oracle in the
+    # CPU-baseline leg), and the run-to-run spread of the derivative reduction: the same step
+    # again (its vector atomics add in whatever order the hardware takes)
+    check_w = sorted({0, W - 1})
+    gpu_check = {w: {"mixed": (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy(),
+                               np.asarray(c.pairs(w)))} for w in check_w}
+    for w in check_w:
+        p_ = gpu_check[w]["mixed"][3].reshape(-1, 2)
+        gpu_check[w]["mixed"] = gpu_check[w]["mixed"][:3] + (p_[np.lexsort((p_[:, 1], p_[:, 0]))],)
+    der_a = der.clone()
+    s_a = s.clone()
+    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=base + 4)
+    torch.cuda.synchronize()
+    spread = {"deriv_max_abs_diff_rel": float((der - der_a).abs().max().item() / der_a.abs().max().item()),
+              "cv_max_abs_diff_rel": float(((s - s_a).abs() / s_a.abs()).max().item()),
+              "what": "the same mixed CV+force pass run twice on the same inputs, all walkers"}
 
     # the plain FP64 GPU path on the same workload (the drop-in, for the 5x target)
     c64 = Coordination(line, precision="fp64", device=local)
@@ -384,6 +529,8 @@ def run_ours(args):
     ev1.record()
     torch.cuda.synchronize()
     t64 = ev0.elapsed_time(ev1) * 1e-3 / max(args.fp64_steps, 1)
+    for w in check_w:
+        gpu_check[w]["fp64"] = (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy())
     c64.close()
     del st64
 
@@ -484,7 +631,10 @@ def run_ours(args):
                 x.close()
         cpu = None
         if not args.no_cpu_baseline:
-            cpu = cpu_baseline(frames, box, budget_s=8.0)
+            cpu = cpu_baseline(frames, box, budget_s=8.0, gpu_check=gpu_check)
+        c2 = None
+        if args.c2_steps > 0:
+            c2 = run_c2(dev, steps=args.c2_steps, cpu=not args.no_cpu_baseline)
         line_out = {
             "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -503,6 +653,11 @@ def run_ours(args):
                        "backward": True, "l2": "working set (0.8 GB) larger than the 129 MB L2",
                        "parallelism": "walkers sharded across GPUs, no collective"},
             "roofline": roof, "cpu_baseline": cpu,
+            "accuracy": dict((cpu or {}).get("accuracy", {}), run_to_run=spread,
+                             basis="the CV+force pass of a non-rebuild step against the FP64 oracle "
+                                   "(oracle/, the C restatement pinned to the reference) on the same positions "
+                                   "and the same neighbour list; targets |dCV|/CV <= 1e-6, force <= 1e-5 "
+                                   "(norm-wise), bit-exact list"),
             "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "call": "coord_forward_batch (C ABI, pinned host arrays of all %d walkers by address), steps "
                             "1..%d (lists rebuilt on multiples of 10)" % (W, args.e2e_steps),
@@ -513,6 +668,7 @@ def run_ours(args):
                                                 "per walker, pageable host arrays",
                                         "host_path": host_path}},
             "gpu_launches": launches, "clocks": clk,
+            "other_configs": {"c2_batched_uneven_actions": c2},
         }
         print(json.dumps(line_out), flush=True)
     if ws > 1:
@@ -524,6 +680,13 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c2":
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        out = run_c2(dev, steps=args.steps, warmup=args.warmup, cpu=not args.no_cpu_baseline)
+        print(json.dumps(dict(out, metric=METRIC, n_gpus=1, steps=args.steps, warmup=args.warmup,
+                              higher_is_better=True, dtype="f32", data="synthetic")), flush=True)
     else:
         run_ours(args)
 

@@ -79,6 +79,38 @@ class _Pairing(C.Structure):
 CV_COORDINATION, CV_DHENERGY, CV_GHBFIX = 0, 1, 2
 
 
+# --- biases on a one-dimensional CV (numpy restatements) -------------------
+METAD_DP2CUTOFF = 6.25  # Tools.h:71 (dp2cutoff)
+
+
+def metad_hills(s, centres, sigmas, heights, stretch=True):
+    """Sum of non-multivariate METAD hills at CV values s[f] and its derivative,
+    MetaD::evaluateGaussianAndDerivatives (src/bias/MetaD.cpp:2256-2273):
+    dp = (s - c)/sigma, dp2 = dp^2/2; a hill with dp2 < 6.25 adds
+    h (A exp(-dp2) + B) to V and -A h exp(-dp2) dp/sigma to dV/ds, where A, B
+    are the stretch constants of Tools.h:71-74 (A = 1, B = 0 unstretched).
+    centres, sigmas, heights: [n_frames][n_hills]."""
+    s = np.asarray(s, dtype=float)
+    c, sg, h = (np.asarray(x, dtype=float) for x in (centres, sigmas, heights))
+    e_cut = np.exp(-METAD_DP2CUTOFF)
+    a = 1.0 / (1.0 - e_cut) if stretch else 1.0
+    b = -e_cut / (1.0 - e_cut) if stretch else 0.0
+    dp = (s[:, None] - c) / sg
+    dp2 = 0.5 * dp * dp
+    on = dp2 < METAD_DP2CUTOFF
+    e = np.where(on, h * np.exp(-dp2), 0.0)
+    V = (a * e + np.where(on, h * b, 0.0)).sum(1)
+    dV = (-a * e * dp / sg).sum(1)
+    return V, dV
+
+
+def restraint(s, at, kappa, slope=0.0):
+    """RESTRAINT on one argument, Restraint::calculate (src/bias/Restraint.cpp:
+    125-141): V = kappa/2 (s-at)^2 + slope (s-at), dV/ds = kappa (s-at) + slope."""
+    cv = np.asarray(s, dtype=float) - at
+    return 0.5 * kappa * cv * cv + slope * cv, kappa * cv + slope
+
+
 def _spec_is_r0(spec: str) -> bool:
     return spec.startswith("R0SYNTAX")
 

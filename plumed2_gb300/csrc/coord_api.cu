@@ -104,6 +104,7 @@ struct coord_ctx {
   // device buffers
   DevBuf<int64_t> abs_of_slot;
   DevBuf<FrameConst> fc;
+  DevBuf<int4> qhi;
   DevBuf<int> cell_of_slot, cell_count, cell_start, cell_fill, slot_of_rank, rank_of_slot, scatter_tmp, row_len, slice_w,
       cell_of_rank;
   DevBuf<double4> x64;
@@ -133,6 +134,7 @@ struct coord_ctx {
   int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0, nl_unroll = 4;
   // mixed NL pass, tuned per evaluation mode (EVAL_S / EVAL_DERIV / EVAL_PARAM)
   int nlm_blocks[5] = {0, 0, 0, 0, 0}, nlm_unroll[5] = {4, 4, 4, 4, 4};
+  int nlm_compact[5] = {0, 0, 0, 0, 0};  // 1: the queue-compacted pair kernel won the autotuner
   bool nlm_tuned[5] = {false, false, false, false, false};
   int cells_launch = 0;  // cells per frame known on the host (0: use ncell_cap)
   bool tuned = false;
@@ -219,6 +221,8 @@ int frame_setup(coord_ctx *c, const double *box, FrameConst *fc, bool *need_boun
   // fixed-point frame
   if (usepbc && fc->pbc.type == PBC_ORTHO) {
     fc->fixed_ok = 1;
+    const double minl = std::min(fc->pbc.box[0], std::min(fc->pbc.box[4], fc->pbc.box[8]));
+    fc->shift_ok = (c->sw.dmax_2 < 1e300 && std::sqrt(c->sw.dmax_2) * 1.001 < 0.45 * minl) ? 1 : 0;
     double span = 0;
     for (int k = 0; k < 3; k++) {
       fc->inv_l[k] = fc->pbc.invbox[4 * k];
@@ -257,6 +261,7 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->slice_w, F * std::max(nslices, 1));
   ENS(c->x64, F * ns);
   ENS(c->q, F * ns);
+  if (c->p.precision == COORD_PREC_FP64 && c->p.nlist != COORD_NL_NONE) ENS(c->qhi, F * ns);
   ENS(c->acc64, F * ns * 3);
   if (c->p.precision == COORD_PREC_FP64 && c->peratom_used) ENS(c->accw64, F * ns);
   ENS(c->acc32, F * ns);
@@ -326,6 +331,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.scatter_tmp = c->scatter_tmp.p;
   a.x64 = c->x64.p;
   a.q = c->q.p;
+  a.qhi = c->qhi.p;
   a.ell = c->ell.p;
   a.row_len = c->row_len.p;
   a.slice_w = c->slice_w.p;
@@ -479,7 +485,7 @@ bool launch_evaluation_chunked(coord_ctx *c, const KArgs &a, int mode, const Hos
     ak.pos = dpos;
     cudaStreamWaitEvent(s1, evH[k], 0);
     launch_prep_host(ak, dpos, 1, s1);
-    launch_eval_nl32(ak, c->sw, c->s32, mode, nb, c->nlm_unroll[m], s1);
+    launch_eval_nl32(ak, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->nlm_compact[m], s1);
     launch_band_fix(ak, c->sw, c->s32, mode, s1);
     if (io->deriv) {
       launch_finalize32(ak, 1, s1);
@@ -494,6 +500,18 @@ bool launch_evaluation_chunked(coord_ctx *c, const KArgs &a, int mode, const Hos
   return true;
 }
 
+// Whether the FP64 neighbour-list pass may screen its entries with the
+// fixed-point FP32 distance (k_eval_nl64q): COORDINATION (its switch is zero
+// beyond a finite d_max) on frames with an orthorhombic periodic box, where
+// the fixed-point positions exist.
+bool fp64_prefilter(const coord_ctx *c) {
+  if (c->cv != COORD_CV_COORDINATION || c->p.nopbc || !std::isfinite(c->s32.dmax2_hi) || c->fc_uploaded.empty())
+    return false;
+  for (const FrameConst &fq : c->fc_uploaded)
+    if (fq.pbc.type != PBC_ORTHO || !fq.fixed_ok) return false;
+  return true;
+}
+
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
 // gathered: the list build of this call already left the positions in rank
@@ -502,6 +520,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
   const bool nl = c->p.nlist != COORD_NL_NONE;
   const bool mixed = c->p.precision == COORD_PREC_MIXED;
   const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
+  const bool prefilter64 = !mixed && nl && c->mode != MODE_PAIR && fp64_prefilter(c);
   if (io && io->fused && io->pinned && nl && mixed && c->mode != MODE_PAIR && a.nframes >= 2 && !c->timing &&
       (!io->deriv || a.out_deriv) && launch_evaluation_chunked(c, a, mode, io))
     return;
@@ -511,7 +530,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
   } else if (c->mode == MODE_PAIR || !nl) {
     if (mixed) launch_gather(a, 0, 0, 1, c->stream);
   } else if (!gathered) {
-    launch_gather(a, 1, mixed ? 0 : 1, mixed ? 1 : 0, c->stream);
+    launch_gather(a, 1, mixed ? 0 : 1, (mixed || prefilter64) ? 1 : 0, c->stream);
   }
   // the pair kernel alone, between the timing events
   cudaEvent_t tev1 = nullptr;
@@ -540,10 +559,10 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
     if (mixed) {
       const int m = std::min(std::max(mode, 0), 4);
       const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
-      launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->nlm_compact[m], c->stream);
       launch_band_fix(a, c->sw, c->s32, mode, c->stream);
     } else {
-      launch_eval_nl64(a, c->sw, mode, c->stream);
+      launch_eval_nl64(a, c->sw, mode, prefilter64 ? &c->s32 : nullptr, c->stream);
     }
   }
   if (tev1) cudaEventRecord(tev1, c->stream);
@@ -576,11 +595,20 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   const int bps[7] = {2, 4, 6, 8, 16, 32, 0}, unr[3] = {2, 4, 8};
   const int m = std::min(std::max(mode, 0), 4);
   float best = 1e30f;
-  int bb = c->nl_blocks, bu = c->nl_unroll;
+  int bb = c->nl_blocks, bu = c->nl_unroll, bc = 0;
   const bool timing = c->timing;
   c->timing = false;
+  // the compacted kernel (modes s, derivatives, parameters) with 2 or 4
+  // entries in flight per lane, beside the plain one with 2, 4 or 8
+  const int ncompact = (mode == EVAL_PERATOM || mode == EVAL_VJP) ? 1 : 2;
+  // COORD_AUTOTUNE_LOG=<file>: every candidate's time appended to the file
+  const char *log_path = std::getenv("COORD_AUTOTUNE_LOG");
+  FILE *log = (log_path && log_path[0]) ? std::fopen(log_path, "a") : nullptr;
+  for (int cv = 0; cv < ncompact; cv++)
   for (int b : bps)
     for (int u : unr) {
+      if (cv == 1 && u == 8) continue;
+      c->nlm_compact[m] = cv;
       const int slices_blocks = (int)(((c->ns + 31) / 32 + 7) / 8);  // blocks of one frame at one slice per warp
       c->nlm_blocks[m] = b > 0 ? b * std::max(c->nsm, 1) : a.nframes * slices_blocks;
       c->nlm_unroll[m] = u;
@@ -596,14 +624,19 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
       cudaEventSynchronize(t1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, t0, t1);
+      if (log) std::fprintf(log, "mode=%d blocks=%d unroll=%d compact=%d frames=%d slots=%lld ms=%.4f\n", mode,
+                            c->nlm_blocks[m], u, cv, a.nframes, (long long)c->ns, ms);
       if (ms < best) {
         best = ms;
         bb = c->nlm_blocks[m];
         bu = u;
+        bc = cv;
       }
     }
+  if (log) std::fclose(log);
   c->nlm_blocks[m] = bb;
   c->nlm_unroll[m] = bu;
+  c->nlm_compact[m] = bc;
   c->nlm_tuned[m] = true;
   c->nl_blocks = bb;
   c->nl_unroll = bu;
@@ -996,6 +1029,7 @@ int coord_destroy(coord_ctx *c) {
   c->slice_w.release();
   c->x64.release();
   c->q.release();
+  c->qhi.release();
   c->ell.release();
   c->self_pairs.release();
   c->nl_count.release();
@@ -1520,10 +1554,11 @@ int coord_autotune(coord_ctx *c, char *desc, size_t desclen) {
   if (!c) return COORD_ERR_ARG;
   if (desc && desclen)
     std::snprintf(desc, desclen,
-                  "tuned=%d nl_pass(s/deriv/param)=%d/%d/%d blocks, unroll %d/%d/%d allpairs_tile64=%d "
-                  "allpairs_tile32=%d blocks=%d",
+                  "tuned=%d nl_pass(s/deriv/param)=%d/%d/%d blocks, unroll %d/%d/%d, compacted %d/%d/%d "
+                  "allpairs_tile64=%d allpairs_tile32=%d blocks=%d",
                   (int)c->tuned, c->nlm_blocks[0], c->nlm_blocks[1], c->nlm_blocks[2], c->nlm_unroll[0],
-                  c->nlm_unroll[1], c->nlm_unroll[2], c->tile64, c->tile32, c->ap_blocks);
+                  c->nlm_unroll[1], c->nlm_unroll[2], c->nlm_compact[0], c->nlm_compact[1], c->nlm_compact[2],
+                  c->tile64, c->tile32, c->ap_blocks);
   return COORD_OK;
 }
 

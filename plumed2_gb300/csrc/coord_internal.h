@@ -90,6 +90,10 @@ struct FrameConst {
   double inv_l[3];
   float  scale[3];    // L / 2^32 per axis (FP32)
   int    fixed_ok;    // box is orthorhombic (or none) so fixed point applies
+  // orthorhombic box with d_max below 0.45 of every side: for a pair within
+  // d_max the reference's image shift round(d / L) is the integer difference
+  // of the two atoms' 64-bit fixed-point positions (k_eval_nl64q)
+  int    shift_ok;
   // the same q in one FMA: q = rn(x * fx_s + fx_c) mod 2^32 with
   // fx_s = inv_l * 2^32 and fx_c = -grid.lo * fx_s (fixed_frame_finish)
   double fx_s[3], fx_c[3];

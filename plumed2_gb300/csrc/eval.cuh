@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
         accw += sig;
       }
       part[0] += sig;
-      if (MODE >= EVAL_DERIV) {
+      if (MODE >= EVAL_DERIV && df != 0.0) {  // a pair beyond d_max adds nothing
         const double dd[3] = {df * d[0], df * d[1], df * d[2]};
         double *accp = a.acc64 + (fo + p) * 3;
         // deriv[first] -= dd; deriv[second] += dd  (CoordinationBase.cpp:196-206)
@@ -99,6 +99,177 @@ __global__ void __launch_bounds__(256) k_eval_nl64(KArgs a, SwitchParams sw) {
     }
     if (MODE == EVAL_PERATOM && accw != 0.0) atomicAdd(a.accw64 + fo + r, accw);
   }
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// neighbour list, FP64, COORDINATION on orthorhombic frames: the drop-in's
+// fast form.  One warp per slice.  Each lane screens its row's entries with
+// the FP32 distance of the fixed-point positions; an entry whose FP32 r^2 is
+// above d_max^2 (1 + 2e-6) has an FP64 r^2 above d_max^2 (the FP32 value is
+// within about 4e-7 of it), so the reference gives it sigma = dfunc = 0 and
+// it adds nothing.  The other entries go to a queue in shared memory, and
+// the warp evaluates them 32 at a time with every lane busy, in FP64 with the
+// reference's operations (pair_fp64, as k_eval_nl64).  Both atoms'
+// derivatives go to the FP64 accumulators by atomic adds; s, the virial and
+// the parameter sums stay in the evaluating lane.  The FP64 pipe runs only
+// for queued pairs and never idles lanes on a divergent branch.
+// ---------------------------------------------------------------------------
+// The reference's minimum-image difference v2 - v1 along one orthorhombic
+// axis, d = ((v2 - v1) * invBox + 100 - t) * box with t = int(x + 0.5) of
+// Tools::pbc (Tools.h:557-563), given the image shift n = round((v2 - v1) /
+// L) as an integer: t = 100 + n then, and it is formed exactly in FP64 from
+// the integer by the 1.5 * 2^52 bias (no integer-to-double conversion).  The
+// operations on the values are the reference's, in its order, so the result
+// is bit-identical; only the conversions of Tools::pbc are avoided.
+__device__ __forceinline__ double pbc_axis_shift(double v1, double v2, double invbox, double box, int n) {
+  const double x = (v2 - v1) * invbox + 100.0;
+  const double t = __longlong_as_double(0x4338000000000000LL + (long long)(100 + n)) - 6755399441055744.0;
+  return (x - t) * box;
+}
+
+// round((v_b - v_a) / L) along one axis from the 64-bit fixed-point positions
+// (high word ha/hb, low word qa/qb), exact while |v_b - v_a| < 0.45 L
+__device__ __forceinline__ int image_shift(int ha, uint32_t qa, int hb, uint32_t qb) {
+  const long long low = (long long)qb - (long long)qa;           // in (-2^32, 2^32)
+  const long long carry = (low - (long long)(int)(qb - qa)) >> 32;  // -1, 0 or 1
+  return hb - ha + (int)carry;
+}
+
+// fixedRational<2 NH>::calculateSqr (SwitchingFunction.cpp:203-215) with N
+// known at compile time: the operations of sw_calculate_sqr, in its order.
+template <int NH> __device__ __forceinline__ double ratfix_sqr(const SwitchParams &s, double d2, double &df) {
+  if (!(d2 <= s.dmax_2)) {
+    df = 0.0;
+    return 0.0;
+  }
+  const double rdist = d2 * s.invr0_2;
+  VD<double> r = rational_fixed<double>(NH, rdist);
+  r.d *= 2.0 * s.invr0_2;
+  r.f = r.f * s.stretch + s.shift;
+  r.d *= s.stretch;
+  df = r.d;
+  return r.f;
+}
+
+template <int MODE, int kU, int NH>
+__global__ void __launch_bounds__(256) k_eval_nl64q(KArgs a, SwitchParams sw, SwitchF32 s32) {
+  const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slice = blockIdx.x * 8 + warp;
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  __shared__ uint2 queue[8][64];  // (list entry, row lane); at most 31 + 32 waiting
+  double part[kPartials];
+#pragma unroll
+  for (int k = 0; k < kPartials; k++) part[k] = 0.0;
+  if (slice < a.nslices) {  // warp-uniform
+    const int r = slice * 32 + lane;
+    const bool active = r < a.ns;
+    const int len = active ? a.row_len[fo + r] : 0;
+    const int w = a.slice_w[(size_t)f * a.nslices + slice];
+    const uint4 *__restrict__ q = a.q + fo;
+    const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
+    const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+    const uint32_t *__restrict__ e = a.ell + ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+    uint2 *const qu = queue[warp];
+    const unsigned below = (1u << lane) - 1u;
+    int qn = 0;  // queued entries (warp-uniform)
+    // evaluates qu[0 .. n) one per lane
+    auto evaluate = [&](int n) {
+      if (lane >= n) return;
+      const uint2 it = qu[lane];
+      const int rr = slice * 32 + (int)it.y;
+      const int p = (int)(it.x & kRankMask);
+      const bool rfirst = (it.x & kOrientBit) != 0;
+      const double4 xr4 = a.x64[fo + rr], xp4 = a.x64[fo + p];
+      const double xr[3] = {xr4.x, xr4.y, xr4.z}, xp[3] = {xp4.x, xp4.y, xp4.z};
+      double d[3], df, sig;
+      if (fc.shift_ok && a.qhi) {
+        // the reference's d = pbc(x[second] - x[first]) with the image shifts
+        // taken from the integer fixed-point positions
+        const uint4 qa = q[rr], qb = q[p];
+        const int4 ha = a.qhi[fo + rr], hb = a.qhi[fo + p];
+        const int n0 = image_shift(ha.x, qa.x, hb.x, qb.x), n1 = image_shift(ha.y, qa.y, hb.y, qb.y),
+                  n2 = image_shift(ha.z, qa.z, hb.z, qb.z);
+        const double *v1 = rfirst ? xr : xp, *v2 = rfirst ? xp : xr;
+        const int sg = rfirst ? 1 : -1;
+        d[0] = pbc_axis_shift(v1[0], v2[0], fc.pbc.invbox[0], fc.pbc.box[0], sg * n0);
+        d[1] = pbc_axis_shift(v1[1], v2[1], fc.pbc.invbox[4], fc.pbc.box[4], sg * n1);
+        d[2] = pbc_axis_shift(v1[2], v2[2], fc.pbc.invbox[8], fc.pbc.box[8], sg * n2);
+        if constexpr (NH > 0) {
+          sig = ratfix_sqr<NH>(sw, mod2(d), df);
+        } else {
+          const VD<double> v = sw_calculate_sqr<double>(sw, mod2(d));
+          sig = v.f;
+          df = v.d;
+        }
+      } else {
+        sig = rfirst ? pair_fp64(a, sw, fc, xr, xp, 0, 0, d, df) : pair_fp64(a, sw, fc, xp, xr, 0, 0, d, df);
+      }
+      if (MODE >= EVAL_PERATOM && (mod2(d) < kBondEps || sig < kBondEps)) {
+        sig = 0.0;
+        df = 0.0;
+      }
+      if (MODE == EVAL_VJP) df *= xr4.w + xp4.w;
+      if (MODE == EVAL_PERATOM && sig != 0.0) {
+        atomicAdd(a.accw64 + fo + p, sig);
+        atomicAdd(a.accw64 + fo + rr, sig);
+      }
+      part[0] += sig;
+      if (MODE >= EVAL_DERIV && df != 0.0) {
+        const double dd[3] = {df * d[0], df * d[1], df * d[2]};
+        // deriv[first] -= dd; deriv[second] += dd  (CoordinationBase.cpp:196-206)
+        const double sgn = rfirst ? 1.0 : -1.0;
+        double *accp = a.acc64 + (fo + p) * 3, *accr = a.acc64 + (fo + rr) * 3;
+        for (int k = 0; k < 3; k++) {
+          atomicAdd(accp + k, sgn * dd[k]);
+          atomicAdd(accr + k, -sgn * dd[k]);
+        }
+        // virial -= dd (x) d: dd = dfunc d, so the tensor is symmetric; the
+        // six distinct entries by fused multiply-adds, mirrored at the end
+        part[1] = fma(-dd[0], d[0], part[1]);
+        part[2] = fma(-dd[0], d[1], part[2]);
+        part[3] = fma(-dd[0], d[2], part[3]);
+        part[5] = fma(-dd[1], d[1], part[5]);
+        part[6] = fma(-dd[1], d[2], part[6]);
+        part[9] = fma(-dd[2], d[2], part[9]);
+      }
+      if (MODE == EVAL_PARAM) param_acc64(sw, mod2(d), sig, df, part);
+    };
+    for (int k = 0; k < w; k += kU) {
+      uint32_t en[kU];
+      uint4 qp[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) en[u] = (k + u < len) ? __ldcs(e + (size_t)(k + u) * 32) : 0xffffffffu;
+#pragma unroll
+      for (int u = 0; u < kU; u++) qp[u] = (en[u] != 0xffffffffu) ? __ldg(q + (en[u] & kRankMask)) : qr;
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const float dx = fixed_delta(qr.x, qp[u].x, sx);
+        const float dy = fixed_delta(qr.y, qp[u].y, sy);
+        const float dz = fixed_delta(qr.z, qp[u].z, sz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool cand = en[u] != 0xffffffffu && r2 <= s32.dmax2_hi;
+        const unsigned b = __ballot_sync(0xffffffffu, cand);
+        if (cand) qu[qn + __popc(b & below)] = make_uint2(en[u], (uint32_t)lane);
+        qn += __popc(b);
+        if (qn >= 32) {
+          __syncwarp();
+          evaluate(32);
+          __syncwarp();
+          if (lane < qn - 32) qu[lane] = qu[32 + lane];
+          __syncwarp();
+          qn -= 32;
+        }
+      }
+    }
+    __syncwarp();
+    evaluate(qn);
+  }
+  part[4] = part[2];
+  part[7] = part[3];
+  part[8] = part[6];
   block_partials_finish(a, f, part, gridDim.x);
 }
 
@@ -125,6 +296,12 @@ __device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s,
   }
 }
 
+// Quantities a lane sums per slice in FP32 and totals in FP64: s, the six
+// independent virial components, ds/dR_0, ds/dD_0.
+constexpr int kSliceSums = 9;
+// Slices a lane sums in FP32 before adding the sums to its FP64 totals.
+constexpr int kFlushSlices = 4;
+
 // Per-thread FP32 accumulators of one pair kernel.
 struct Acc32 {
   float cv = 0.f, cvc = 0.f;
@@ -134,10 +311,66 @@ struct Acc32 {
   // row (tens of terms), flushed into an FP64 lane total after every slice
   float cvs = 0.f;
   double cv64 = 0.0;
+  // FP64 totals of the virial and parameter sums, for kernels that flush
+  // their FP32 sums after every tile (flush_tile)
+  double vt[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, pt[2] = {0.0, 0.0};
+  template <int MODE> __device__ __forceinline__ void flush_tile() {
+    if (MODE >= EVAL_DERIV) {
+      vt[0] += (double)vxx;
+      vt[1] += (double)vyy;
+      vt[2] += (double)vzz;
+      vt[3] += (double)vxy;
+      vt[4] += (double)vxz;
+      vt[5] += (double)vyz;
+      vxx = vyy = vzz = vxy = vxz = vyz = 0.f;
+    }
+    if (MODE == EVAL_PARAM) {
+      pt[0] += (double)pr0;
+      pt[1] += (double)pd0;
+      pr0 = pd0 = 0.f;
+    }
+  }
   __device__ __forceinline__ void add_s_slice(float sig) { cvs += sig; }
   __device__ __forceinline__ void flush_s() {
     cv64 += (double)cvs;
     cvs = 0.f;
+  }
+  // The slice's FP32 sums (s in cvs, the virial, the parameter gradients)
+  // added to a lane's FP64 totals tot[32 k] (kSliceSums quantities, stride
+  // 32), then cleared.
+  template <int MODE> __device__ __forceinline__ void flush_slice(double *tot) {
+    tot[0] += (double)cvs;
+    cvs = 0.f;
+    if (MODE >= EVAL_DERIV) {
+      tot[32 * 1] += (double)vxx;
+      tot[32 * 2] += (double)vyy;
+      tot[32 * 3] += (double)vzz;
+      tot[32 * 4] += (double)vxy;
+      tot[32 * 5] += (double)vxz;
+      tot[32 * 6] += (double)vyz;
+      vxx = vyy = vzz = vxy = vxz = vyz = 0.f;
+    }
+    if (MODE == EVAL_PARAM) {
+      tot[32 * 7] += (double)pr0;
+      tot[32 * 8] += (double)pd0;
+      pr0 = pd0 = 0.f;
+    }
+  }
+  template <int MODE> __device__ __forceinline__ static void totals_to_partials(const double *tot,
+                                                                                 double part[kPartials]) {
+    part[0] = tot[0];
+    const double xx = tot[32], yy = tot[64], zz = tot[96], xy = tot[128], xz = tot[160], yz = tot[192];
+    part[1] = xx;
+    part[2] = xy;
+    part[3] = xz;
+    part[4] = xy;
+    part[5] = yy;
+    part[6] = yz;
+    part[7] = xz;
+    part[8] = yz;
+    part[9] = zz;
+    part[10] = tot[224];
+    part[11] = tot[256];
   }
   __device__ __forceinline__ void add_s(float sig) {
     const float yk = sig - cvc;
@@ -160,17 +393,19 @@ struct Acc32 {
   }
   __device__ __forceinline__ void to_partials(double part[kPartials]) const {
     part[0] = ((double)cv - (double)cvc) + (cv64 + (double)cvs);
-    part[1] = vxx;
-    part[2] = vxy;
-    part[3] = vxz;
-    part[4] = vxy;
-    part[5] = vyy;
-    part[6] = vyz;
-    part[7] = vxz;
-    part[8] = vyz;
-    part[9] = vzz;
-    part[10] = pr0;
-    part[11] = pd0;
+    const double xx = vt[0] + vxx, yy = vt[1] + vyy, zz = vt[2] + vzz, xy = vt[3] + vxy, xz = vt[4] + vxz,
+                 yz = vt[5] + vyz;
+    part[1] = xx;
+    part[2] = xy;
+    part[3] = xz;
+    part[4] = xy;
+    part[5] = yy;
+    part[6] = yz;
+    part[7] = xz;
+    part[8] = yz;
+    part[9] = zz;
+    part[10] = pt[0] + pr0;
+    part[11] = pt[1] + pd0;
   }
 };
 
@@ -229,6 +464,16 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
   const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
+  // each lane's FP64 totals of its FP32 sums (s, the six virial components,
+  // the two parameter gradients): a lane sums the pairs of its rows over
+  // kFlushSlices slices (a few tens of pairs) in FP32, then adds those sums
+  // here in FP64, so no FP32 sum runs longer (shared memory rather than
+  // registers: the kernel is held at 64 registers; flushing every slice
+  // measured 8 % slower, the FP64 additions queueing on the FP64 pipe)
+  __shared__ double tot[8][kSliceSums][32];
+  double *const mytot = &tot[threadIdx.x >> 5][0][lane];
+#pragma unroll
+  for (int k = 0; k < kSliceSums; k++) mytot[32 * k] = 0.0;
   const int nw = gridDim.x * wpb;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];
@@ -239,6 +484,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
   const size_t slice_words = (size_t)a.cap * 32;
   const uint32_t *ell_f = a.ell + (size_t)f * a.nslices * slice_words;
   const int *sw_f = a.slice_w + (size_t)f * a.nslices;
+  int pending = 0;  // slices summed in FP32 since the last flush
   {
     // this warp's first slice: its entries (w rows of 32 words) into L2
     const int s0 = blockIdx.x * wpb + (threadIdx.x >> 5);
@@ -318,10 +564,154 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
     }
     if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
-    acc.flush_s();
+    if (++pending == kFlushSlices) {
+      acc.flush_slice<MODE>(mytot);
+      pending = 0;
+    }
   }
+  acc.flush_slice<MODE>(mytot);
   double part[kPartials];
-  acc.to_partials(part);
+  Acc32::totals_to_partials<MODE>(mytot, part);
+  block_partials_finish(a, f, part, gridDim.x);
+}
+
+// The same pass with the evaluation compacted (modes s, derivatives,
+// parameters).  About 40 % of the list entries lie inside d_max; in
+// k_eval_nl32 every entry pays for the switch, the reductions and the virial
+// whenever any lane of the warp needs them.  Here each lane screens its
+// entries (entry -> partner position -> FP32 r^2) and the warp appends the
+// pairs inside d_max to a queue in shared memory (ballot + prefix count);
+// whenever 32 or more are waiting, the warp evaluates them 32 at a time with
+// every lane busy.  A queued pair carries its delta, its partner rank and its
+// row's lane: the partner's derivative goes to the global accumulator by a
+// vector reduction as before, the row's to a per-lane sum in shared memory
+// that the row's own lane adds to its accumulator at the end of the slice.
+// The slice's s, virial and parameter sums stay in the evaluating lane and
+// are flushed per slice as in k_eval_nl32; band pairs are flagged the same
+// way.
+template <int NH, int MODE, int kUnroll>
+__global__ void __launch_bounds__(256) k_eval_nl32c(KArgs a, SwitchParams sw, SwitchF32 s32) {
+  constexpr int kQ = 32 * (kUnroll + 1);  // at most 31 waiting + 32 per unrolled entry
+  const int f = blockIdx.y + a.frame0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int nw = gridDim.x * wpb;
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const uint4 *__restrict__ q = a.q + fo;
+  float4 *__restrict__ acc4 = a.acc32 + fo;
+  __shared__ double tot[8][kSliceSums][32];
+  __shared__ float4 qd[8][kQ];          // queued pairs: delta (x_p - x_r) and the partner rank's bits
+  __shared__ unsigned char ql[8][kQ];   // the row lane of each queued pair
+  __shared__ float4 racc[8][32];        // row-side sums of the slice's evaluated pairs
+  double *const mytot = &tot[warp][0][lane];
+#pragma unroll
+  for (int k = 0; k < kSliceSums; k++) mytot[32 * k] = 0.0;
+  float4 *const qdw = qd[warp];
+  unsigned char *const qlw = ql[warp];
+  float4 *const rac = racc[warp];
+  rac[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const unsigned below = (1u << lane) - 1u;
+  Acc32 acc;
+  int pending = 0;  // slices summed in FP32 since the last flush
+  const size_t slice_words = (size_t)a.cap * 32;
+  const uint32_t *ell_f = a.ell + (size_t)f * a.nslices * slice_words;
+  const int *sw_f = a.slice_w + (size_t)f * a.nslices;
+  {
+    const int s0 = blockIdx.x * wpb + warp;
+    if (lane == 0 && s0 < a.nslices) {
+      const int w0 = sw_f[s0];
+      if (w0 > 0) prefetch_l2_bulk(ell_f + (size_t)s0 * slice_words, (uint32_t)w0 * 128u);
+    }
+  }
+  // evaluates queued pair i (one per lane)
+  auto evaluate = [&](int i) {
+    const float4 it = qdw[i];
+    const int rl = qlw[i];
+    const int p = __float_as_int(it.w);
+    const float r2 = fmaf(it.x, it.x, fmaf(it.y, it.y, it.z * it.z));
+    float sig, df;
+    sw32<NH>(sw, s32, r2, sig, df);
+    acc.add_s_slice(sig);
+    if (MODE >= EVAL_DERIV) {
+      const float ddx = df * it.x, ddy = df * it.y, ddz = df * it.z;
+      red_add_v4(acc4 + p, ddx, ddy, ddz);
+      atomicAdd(&rac[rl].x, -ddx);
+      atomicAdd(&rac[rl].y, -ddy);
+      atomicAdd(&rac[rl].z, -ddz);
+      acc.add_vir(ddx, ddy, ddz, it.x, it.y, it.z);
+    }
+    if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
+  };
+  const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
+  const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
+  for (int slice = blockIdx.x * wpb + warp; slice < a.nslices; slice += nw) {
+    const int r = slice * 32 + lane;
+    const bool active = r < a.ns;
+    const int len = active ? a.row_len[fo + r] : 0;
+    const int w = sw_f[slice];
+    if (lane == 0 && slice + nw < a.nslices) {
+      const int wn = sw_f[slice + nw];
+      if (wn > 0) prefetch_l2_bulk(ell_f + (size_t)(slice + nw) * slice_words, (uint32_t)wn * 128u);
+    }
+    const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t *__restrict__ e = ell_f + (size_t)slice * slice_words + lane;
+    uint32_t band_min = 0xffffffffu;
+    int qn = 0;  // queued pairs (warp-uniform)
+    for (int k = 0; k < w; k += kUnroll) {
+      int p[kUnroll];
+      uint4 qp[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldcs(e + (size_t)(k + u) * 32) & kRankMask) : -1;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) {
+        const float dx = fixed_delta(qr.x, qp[u].x, sx);
+        const float dy = fixed_delta(qr.y, qp[u].y, sy);
+        const float dz = fixed_delta(qr.z, qp[u].z, sz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool in = p[u] >= 0 && r2 <= s32.dmax2_lo;
+        if (!in) band_min = min(band_min, __float_as_uint(r2) - band_lo);
+        const unsigned b = __ballot_sync(0xffffffffu, in);
+        if (in) {
+          const int at = qn + __popc(b & below);
+          qdw[at] = make_float4(dx, dy, dz, __int_as_float(p[u]));
+          qlw[at] = (unsigned char)lane;
+        }
+        qn += __popc(b);
+      }
+      if (qn >= 32) {
+        __syncwarp();
+        int h = 0;
+        for (; h + 32 <= qn; h += 32) evaluate(h + lane);
+        __syncwarp();
+        if (lane < qn - h) {  // the rest to the front (source and destination do not overlap)
+          qdw[lane] = qdw[h + lane];
+          qlw[lane] = qlw[h + lane];
+        }
+        __syncwarp();
+        qn -= h;
+      }
+    }
+    __syncwarp();
+    if (lane < qn) evaluate(lane);
+    __syncwarp();
+    if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
+    if (MODE >= EVAL_DERIV) {
+      const float4 ra = rac[lane];
+      rac[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (len > 0 && (ra.x != 0.f || ra.y != 0.f || ra.z != 0.f)) red_add_v4(acc4 + r, ra.x, ra.y, ra.z);
+    }
+    if (++pending == kFlushSlices) {
+      acc.flush_slice<MODE>(mytot);
+      pending = 0;
+    }
+  }
+  acc.flush_slice<MODE>(mytot);
+  double part[kPartials];
+  Acc32::totals_to_partials<MODE>(mytot, part);
   block_partials_finish(a, f, part, gridDim.x);
 }
 
@@ -621,6 +1011,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
       }
       if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f))
         atomicAdd(a.acc32 + fo + i, make_float4(ax, ay, az, 0.f));
+      acc.flush_tile<MODE>();
     }
     __syncthreads();
     if (MODE >= EVAL_DERIV) {

@@ -93,7 +93,34 @@ void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaSt
   default: CALL(EVAL_DERIV); break; \
   }
 
-void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, cudaStream_t s) {
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const SwitchF32 *prefilter, cudaStream_t s) {
+  if (prefilter) {
+    // one warp per slice: (nslices + 7) / 8 blocks per frame, as many as
+    // grid1(ns, 256) gives below
+    const dim3 g((a.nslices + 7) / 8 > 0 ? (a.nslices + 7) / 8 : 1, a.nframes);
+    // fixedRational<6> (the default NN=6, MM=12 switch) compiled with N fixed
+    if (sw.type == SW_RATFIX && sw.nn == 6) {
+#define CALLQ(M) k_eval_nl64q<M, 4, 3><<<g, 256, 0, s>>>(a, sw, *prefilter)
+      if (mode == EVAL_PERATOM)
+        CALLQ(EVAL_PERATOM);
+      else if (mode == EVAL_VJP)
+        CALLQ(EVAL_VJP);
+      else
+        MODE_DISPATCH(mode, CALLQ)
+#undef CALLQ
+    } else {
+#define CALLQ(M) k_eval_nl64q<M, 4, 0><<<g, 256, 0, s>>>(a, sw, *prefilter)
+      if (mode == EVAL_PERATOM)
+        CALLQ(EVAL_PERATOM);
+      else if (mode == EVAL_VJP)
+        CALLQ(EVAL_VJP);
+      else
+        MODE_DISPATCH(mode, CALLQ)
+#undef CALLQ
+    }
+    g_launches += 1;
+    return;
+  }
 #define CALL(M) k_eval_nl64<M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw)
   if (mode == EVAL_PERATOM)
     CALL(EVAL_PERATOM);

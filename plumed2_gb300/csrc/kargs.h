@@ -38,6 +38,7 @@ struct KArgs {
   int *scatter_tmp;             // [nframes][ns]
   double4 *x64;                 // [nframes][ns] sorted (or slot-order) FP64 positions
   uint4 *q;                     // [nframes][ns] fixed-point positions
+  int4 *qhi;                    // [nframes][ns] their high words (the box image of each coordinate), or null
   uint32_t *ell;                // [nframes][nslices*cap*32]
   int *row_len;                 // [nframes][ns]
   int *slice_w;                 // [nframes][nslices]

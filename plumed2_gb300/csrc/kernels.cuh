@@ -47,26 +47,13 @@ __device__ __forceinline__ int warp_max(int v) {
   return v;
 }
 
-// Block-reduces kPartials doubles (one set per thread), writes the block's
-// record, and lets the last block of the frame (atomic ticket, no waiting)
-// sum all records in block order with Kahan compensation.  The final values
-// land in out_s / out_virial / out_dparam of the frame.
-__device__ void block_partials_finish(const KArgs &a, int frame, double v[kPartials], int nblocks_frame) {
-  __shared__ double red[kPartials][32];
+// The frame's last block (atomic ticket, no waiting) sums every block's record
+// of kPartials doubles in block order with Neumaier compensation; the final
+// values land in out_s / out_virial / out_dparam of the frame.  Called by
+// every thread after the block's record has been written.
+__device__ void block_records_finish(const KArgs &a, int frame, int nblocks_frame) {
   __shared__ bool is_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < kPartials; k++) {
-    double w = warp_sum(v[k]);
-    if (lane == 0) red[k][warp] = w;
-  }
-  __syncthreads();
-  double *rec = a.partials + ((size_t)frame * a.max_blocks + blockIdx.x) * kPartials;
-  if (threadIdx.x < kPartials) {
-    double s = 0.0;
-    for (int w = 0; w < nwarps; w++) s += red[threadIdx.x][w];
-    rec[threadIdx.x] = s;
-  }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -112,6 +99,46 @@ __device__ void block_partials_finish(const KArgs &a, int frame, double v[kParti
   if (threadIdx.x == 0) a.tickets[frame] = 0u;
 }
 
+// Sums 16 doubles per lane over the warp as a reduce-scatter: at each level a
+// lane keeps half of its quantities and adds its partner's copy of them, so
+// 16 FP64 additions per lane (8 + 4 + 2 + 1 + 1) instead of 5 per quantity.
+// Afterwards lanes 2q and 2q+1 hold the warp's sum of quantity q in x[0].
+// (The FP64 pipe is narrow on this part: the additions, not the shuffles,
+// are the cost.)
+__device__ __forceinline__ void warp_reduce_scatter16(double x[16], int lane) {
+#pragma unroll
+  for (int lvl = 0, half = 8, o = 16; lvl < 4; lvl++, half >>= 1, o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      if (i >= half) break;
+      const double mine = up ? x[half + i] : x[i], other = up ? x[i] : x[half + i];
+      x[i] = mine + __shfl_xor_sync(0xffffffffu, other, o);
+    }
+  }
+  x[0] += __shfl_xor_sync(0xffffffffu, x[0], 1);
+}
+
+// Block-reduces kPartials doubles (one set per thread) into the block's
+// record, then block_records_finish.
+__device__ void block_partials_finish(const KArgs &a, int frame, double v[kPartials], int nblocks_frame) {
+  __shared__ double red[kPartials][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
+  double x[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) x[k] = k < kPartials ? v[k] : 0.0;
+  warp_reduce_scatter16(x, lane);
+  if ((lane & 1) == 0 && (lane >> 1) < kPartials) red[lane >> 1][warp] = x[0];
+  __syncthreads();
+  double *rec = a.partials + ((size_t)frame * a.max_blocks + blockIdx.x) * kPartials;
+  if (threadIdx.x < kPartials) {
+    double s = 0.0;
+    for (int w = 0; w < nwarps; w++) s += red[threadIdx.x][w];
+    rec[threadIdx.x] = s;
+  }
+  block_records_finish(a, frame, nblocks_frame);
+}
+
 // ---------------------------------------------------------------------------
 // fixed-point positions (mixed path and the FP32 neighbour-list prefilter)
 // ---------------------------------------------------------------------------
@@ -125,6 +152,15 @@ __device__ __forceinline__ uint32_t to_fixed_fma(double x, double s, double c) {
 __device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x) {
   return make_uint4(to_fixed_fma(x[0], fc.fx_s[0], fc.fx_c[0]), to_fixed_fma(x[1], fc.fx_s[1], fc.fx_c[1]),
                     to_fixed_fma(x[2], fc.fx_s[2], fc.fx_c[2]), 0u);
+}
+// The same fixed-point positions with their high words: the 64-bit value
+// rn(x * 2^32 / L) is (box image) * 2^32 + q.
+__device__ __forceinline__ uint4 fixed_of_hi(const FrameConst &fc, const double *x, int4 &hi) {
+  long long v[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) v[k] = __double2ll_rn(fma(x[k], fc.fx_s[k], fc.fx_c[k]));
+  hi = make_int4((int)(v[0] >> 32), (int)(v[1] >> 32), (int)(v[2] >> 32), 0);
+  return make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], 0u);
 }
 __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float scale) {
   return (float)(int)(b - a) * scale;  // wraps modulo 2^32: minimum image
@@ -486,7 +522,14 @@ __global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wan
   if (want64) a.x64[(size_t)f * a.ns + r] = make_double4(x0, x1, x2, gw);
   if (wantq) {
     const double xx[3] = {x0, x1, x2};
-    uint4 qq = fixed_of(a.fc[f], xx);
+    uint4 qq;
+    if (a.qhi) {
+      int4 hi;
+      qq = fixed_of_hi(a.fc[f], xx, hi);
+      a.qhi[(size_t)f * a.ns + r] = hi;
+    } else {
+      qq = fixed_of(a.fc[f], xx);
+    }
     qq.w = __float_as_uint((float)gw);
     a.q[(size_t)f * a.ns + r] = qq;
   }

@@ -4,9 +4,10 @@
 //
 // Build against an installed PLUMED and load it with LOAD (src/setup/Load.cpp):
 //
-//   g++ -std=c++17 -O2 -fPIC -shared CoordinationGPU.cpp -o CoordinationGPU.so \
-//       -I$PLUMED_PREFIX/include/plumed -I<repo>/include \
+//   g++ -std=c++17 -O2 -fPIC -shared CoordinationGPU.cpp -o CoordinationGPU.so
+//       -I$PLUMED_PREFIX/include/plumed -I<repo>/include
 //       -L<repo>/plumed2_gb300/_build -lcoordgpu -Wl,-rpath,<repo>/plumed2_gb300/_build
+//   (one command line)
 //
 //   LOAD FILE=CoordinationGPU.so
 //   c: COORDINATION GROUPA=1-1000 SWITCH={RATIONAL R_0=0.3 D_MAX=1.0}

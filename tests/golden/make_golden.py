@@ -445,6 +445,25 @@ def main(ref):
                "rt72": {"map": maps72[0], "pos": pos72, "box": box72, "value": col72[0][1],
                         "deriv": [r[2] for r in der72], "fmt": "colvar %f, deriv %12.8f"}},
               open(os.path.join(HERE, "rt_contactmap.json"), "w"))
+    # --- rt-metad-numder: METAD on one distance, the reference's forces -------
+    dmn = os.path.join(reg, "basic", "rt-metad-numder")
+    trm, bxm = read_xyz(os.path.join(reg, "trajectories", "trajectory.xyz"))
+    natm = len(trm[0])
+    rows = read_table(os.path.join(dmn, "forces.reference"))
+    per = 3 * natm + 9
+    nfr = len(rows) // per
+    forces = [[r[1] for r in rows[k * per:(k + 1) * per]] for k in range(nfr)]
+    json.dump({"source": "regtest/basic/rt-metad-numder (plumed.dat: d1: DISTANCE ATOMS=1,10; METAD ARG=d1 "
+                         "SIGMA=0.1 HEIGHT=1.0 PACE=10; config: --trajectory-stride 10, --debug-forces, %8.4f), "
+                         "regtest/trajectories/trajectory.xyz",
+               "atoms": [1, 10], "sigma": 0.1, "height": 1.0, "pace": 10, "trajectory_stride": 10,
+               "frames": [[fr[0], fr[9]] for fr in trm[:nfr]], "box": bxm[:nfr],
+               "forces_atom1": [f[0:3] for f in forces], "forces_atom10": [f[27:30] for f in forces],
+               "virial": [f[3 * natm:3 * natm + 9] for f in forces],
+               "max_abs_other_forces": max(abs(x) for f in forces for i, x in enumerate(f[:3 * natm])
+                                           if not (i < 3 or 27 <= i < 30)),
+               "fmt": "%8.4f (analytical column of --debug-forces)"},
+              open(os.path.join(HERE, "rt_metad_numder.json"), "w"), indent=0)
     print("fixtures written to", HERE)
 
 

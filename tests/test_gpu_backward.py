@@ -211,3 +211,88 @@ def test_saved_forward_matches_recompute(prec):
         if name in ("save", "save+dr0"):
             s_, der, vir, gp = got[:4]
             assert np.abs(gp - g.cpu().numpy()[:, None, None] * der).max() <= 1e-14 * np.abs(gp).max()
+
+
+def test_c3_metad_backward_at_size(orc):
+    """The differentiation workload at its own size: the 32,768-atom two-slab
+    system (GROUPA = the z < L/2 slab, GROUPB = the other, RATIONAL R_0=0.35
+    D_MAX=1.2, NLIST NL_CUTOFF=1.4), s feeding 500 hills (h = 1.2, sigma =
+    0.05 s0, centres uniform in [0.8 s0, 1.2 s0], s0 = frame 0's CV).
+    FP64: dV/dx and dV/dh against the oracle's analytic derivatives times
+    V'(s) (1e-10 of their scale), and against FP64 central differences with
+    h = 1e-6 nm for eight sampled atoms (all three coordinates), four box
+    entries (scaled coordinates fixed), R_0 and D_0 (2e-6 of the gradient's
+    scale).  Mixed: the same gradients within 1e-5 of the FP64 ones."""
+    from plumed2_gb300 import frames as W
+    from plumed2_gb300.autograd import coordination
+    dev = torch.device("cuda:0")
+    frames, box0 = W.workload_c1(n_frames=1)
+    pos0 = frames[0]
+    n, half = len(pos0), len(pos0) // 2
+    pline = ("GROUPA=1-%d GROUPB=%d-%d SWITCH={RATIONAL R_0=%%r NN=6 MM=12 D_MAX=1.2 D_0=%%r} NLIST NL_CUTOFF=1.4 "
+             "NL_STRIDE=20" % (half, half + 1, n))
+    line = pline % (0.35, 0.0)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        act = make(line, prec)
+        pos = torch.tensor(pos0[None], dtype=torch.float64, device=dev, requires_grad=True)
+        box = torch.tensor(box0, dtype=torch.float64, requires_grad=True)
+        r0 = torch.tensor(0.35, dtype=torch.float64, device=dev, requires_grad=True)
+        d0 = torch.tensor(0.0, dtype=torch.float64, device=dev, requires_grad=True)
+        s = coordination(act, pos, box, r0, d0)
+        s0 = float(s.item()) if prec == "fp64" else out["fp64"][0]
+        V = bias(s, s0).sum()
+        V.backward()
+        out[prec] = (s0 if prec == "fp64" else float(s.item()), pos.grad[0].cpu().numpy(), box.grad.numpy(),
+                     r0.grad.item(), d0.grad.item())
+        act.close()
+    s0, gpos, gbox, gr0, gd0 = out["fp64"]
+    # the oracle's analytic derivatives (the reference's layout) times V'(s)
+    pairs = orc.nl_classic_cells(1, half, half, pos0, box0, True, 1.4)
+    so, do, vo = orc.coordination("RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.2", pos0, box0, pairs,
+                                  nthreads=orc.max_threads())
+    assert abs(so - s0) <= 1e-12 * abs(so)
+    _, dV = bias_np(so, s0)
+    assert np.abs(gpos - dV * do).max() <= 1e-10 * np.abs(dV * do).max()
+    ref_box = dV * (-np.linalg.inv(box0).T @ vo)
+    assert np.abs(gbox - ref_box).max() <= 1e-10 * np.abs(ref_box).max()
+
+    def V_of(p, b, r0v=0.35, d0v=0.0):
+        a = make(pline % (r0v, d0v), "fp64")
+        sv, _, _ = a.calculate(p, b, 0, derivatives=False)
+        a.close()
+        return bias_np(sv, s0)[0]
+
+    h = 1e-6
+    rng = np.random.default_rng(5)
+    # sampled atoms: four near the slab interfaces (non-zero forces), four anywhere
+    near = np.flatnonzero(np.linalg.norm(gpos, axis=1) > 0.1 * np.linalg.norm(gpos, axis=1).max())
+    idxs = list(rng.choice(near, 4, replace=False)) + list(rng.choice(n, 4, replace=False))
+    gscale = np.abs(gpos).max()
+    for idx in idxs:
+        for k in range(3):
+            pp = pos0.copy()
+            pm = pos0.copy()
+            pp[idx, k] += h
+            pm[idx, k] -= h
+            fd = (V_of(pp, box0) - V_of(pm, box0)) / (2 * h)
+            assert abs(fd - gpos[idx, k]) <= 2e-6 * gscale + 1e-9, (idx, k, fd, gpos[idx, k])
+    scaled = pos0 @ np.linalg.inv(box0)
+    for (kk, bb) in ((0, 0), (1, 1), (2, 2), (0, 2)):
+        bp = box0.copy()
+        bm = box0.copy()
+        bp[kk, bb] += h
+        bm[kk, bb] -= h
+        fd = (V_of(scaled @ bp, bp) - V_of(scaled @ bm, bm)) / (2 * h)
+        assert abs(fd - gbox[kk, bb]) <= 2e-6 * np.abs(gbox).max() + 1e-9, (kk, bb, fd, gbox[kk, bb])
+    fd_r0 = (V_of(pos0, box0, 0.35 + h) - V_of(pos0, box0, 0.35 - h)) / (2 * h)
+    assert abs(fd_r0 - gr0) <= 2e-6 * abs(fd_r0) + 1e-9, (fd_r0, gr0)
+    fd_d0 = (V_of(pos0, box0, 0.35, h) - V_of(pos0, box0, 0.35, -h)) / (2 * h)
+    assert abs(fd_d0 - gd0) <= 2e-6 * abs(fd_d0) + 1e-9, (fd_d0, gd0)
+    # mixed precision against FP64
+    sm, gpm, gbm, gr0m, gd0m = out["mixed"]
+    assert abs(sm - s0) <= 1e-6 * abs(s0)
+    assert np.sqrt(((gpm - gpos) ** 2).sum(axis=1)).max() <= 1e-5 * np.sqrt((gpos ** 2).sum(axis=1)).max()
+    assert np.abs(gbm - gbox).max() <= 1e-5 * np.abs(gbox).max()
+    assert abs(gr0m - gr0) <= 1e-5 * abs(gr0)
+    assert abs(gd0m - gd0) <= 1e-5 * abs(gd0)

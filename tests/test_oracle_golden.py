@@ -400,3 +400,38 @@ def test_custom_switch_input_the_oracle_cannot_hold_is_refused(orc):
         orc.switch("CUSTOM R_0=0.3")
     # a short expression still compiles
     orc.switch("CUSTOM FUNC=1/(1+x^6) R_0=0.3")
+
+
+def metad_numder_case(orc, g):
+    """rt-metad-numder replayed: d1 = |min-image(x10 - x1)| per frame (DISTANCE);
+    hills deposited after the frames whose step is a multiple of PACE, except
+    the first step (MetaD::update, src/bias/MetaD.cpp:2377-2385: no hill on the
+    first step), each at the frame's d1 with SIGMA and HEIGHT; frame k feels
+    the hills of the frames before it.  Returns d1, the unit vectors and the
+    hill centres each frame sees."""
+    d, u = [], []
+    for fr, bx in zip(g["frames"], g["box"]):
+        v = orc.pbc_distance(np.diag(bx), np.array(fr[0]), np.array(fr[1]))[0]
+        r = float(np.sqrt(v @ v))
+        d.append(r)
+        u.append(v / r)
+    steps = [k * g["trajectory_stride"] for k in range(len(d))]
+    deposit = [k for k, st in enumerate(steps) if st % g["pace"] == 0 and k > 0]
+    seen = [[d[j] for j in deposit if j < k] for k in range(len(d))]
+    return np.array(d), np.array(u), seen
+
+
+def test_rt_metad_numder_forces(orc, golden):
+    """The hill sum's derivative (oracle.metad_hills, stretched Gaussians as
+    METAD's default kernel) times the distance's derivative reproduces the
+    reference's analytical forces on atoms 1 and 10 in every frame (%8.4f)."""
+    from oracle import metad_hills
+    g = golden("rt_metad_numder.json")
+    assert g["max_abs_other_forces"] == 0.0
+    d, u, seen = metad_numder_case(orc, g)
+    for k in range(len(d)):
+        n = len(seen[k])
+        _, dV = metad_hills([d[k]], [seen[k]], [[g["sigma"]] * n], [[g["height"]] * n], stretch=True)
+        f10 = -dV[0] * u[k]  # F = -dV/dd1 * dd1/dx10, dd1/dx10 = u
+        assert np.abs(f10 - np.array(g["forces_atom10"][k])).max() <= 5.01e-5, (k, f10, g["forces_atom10"][k])
+        assert np.abs(-f10 - np.array(g["forces_atom1"][k])).max() <= 5.01e-5, k
