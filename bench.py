@@ -10,7 +10,9 @@ Workload (the 262,144-atom configuration the headline target is quoted on):
   sums).  A step is CV + derivatives + virial for all walkers, followed by the
   backward pass of a 500-hill metadynamics-style bias when it is available.
   Neighbour lists are rebuilt on steps that are multiples of NL_STRIDE, so
-  rebuilds are amortised exactly as in an MD run.
+  rebuilds are amortised exactly as in an MD run; between rebuilds the walkers
+  move by Gaussian steps of 0.002 nm per coordinate (step k uses frame k % 10
+  of a 10-frame trajectory that starts at the lattice frame).
 
   value  = pair-evaluations (neighbour-list entries processed, summed over
            walkers) per second, inputs resident in HBM, CUDA events around the
@@ -48,6 +50,7 @@ N_ATOMS = 262144
 BOX = 19.87
 SPEC = "RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6"
 LINE = "GROUPA=1-%d SWITCH={%s} NLIST NL_CUTOFF=0.8 NL_STRIDE=10"
+MOTION_SIGMA = 0.002  # nm per coordinate per step: the walkers move as in an MD run between rebuilds
 ALG_FLOPS_PER_PAIR = 57  # FMA = 2: delta 3, min-image 9, r^2 5, switch+dfunc 12, chain 4, dd 3, derivs 6, virial 18, s 1
 
 
@@ -65,8 +68,8 @@ def parse():
     ap.add_argument("--quick", action="store_true", help="small sizes (for profiling captures)")
     ap.add_argument("--c2-steps", type=int, default=3,
                     help="timed graph replays of the batched 256-action workload (0: skip it)")
-    ap.add_argument("--workload", default="c4", choices=["c4", "c2"],
-                    help="c2: only the batched 256-action workload, as its own line")
+    ap.add_argument("--workload", default="c4", choices=["c4", "c2", "c1", "c0"],
+                    help="c2 / c1 / c0: only that workload, as its own line")
     return ap.parse_args()
 
 
@@ -192,15 +195,19 @@ def reduce_over_ranks(x, op="max", device=None):
 
 
 def make_walkers(n_walkers, n_atoms, first):
+    """Jittered simple-cubic lattices at the 262,144-atom system's spacing (19.87 / 64 nm) filling a cube
+    of m = n_atoms^(1/3) sites per side (n_atoms a cube: smaller systems for profiling captures)."""
     from plumed2_gb300.frames import sc_sites
     sites = sc_sites(n_atoms)
     m = round(n_atoms ** (1 / 3))
-    a = BOX / m
+    if m ** 3 != n_atoms:
+        raise ValueError("the atom count must be a cube, not %d" % n_atoms)
+    a = BOX / round(N_ATOMS ** (1 / 3))
     out = np.empty((n_walkers, n_atoms, 3))
     for w in range(n_walkers):
         rng = np.random.default_rng([2028, first + w])
         out[w] = sites * a + rng.normal(0.0, 0.03, size=(n_atoms, 3))
-    return out, np.diag([BOX * (n_atoms / N_ATOMS) ** (1 / 3)] * 3)
+    return out, np.diag([a * m] * 3)
 
 
 def accuracy_against(ref, got, pairs_ref=None, pairs_got=None):
@@ -221,9 +228,10 @@ def accuracy_against(ref, got, pairs_ref=None, pairs_got=None):
 
 def cpu_baseline(frames, box, budget_s=10.0, gpu_check=None):
     """The reference algorithm on this host's cores: classic neighbour list once
-    (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop.  The same
-    oracle results check the GPU's (gpu_check: walker -> {"mixed": (s, deriv, virial,
-    sorted pairs), "fp64": (s, deriv, virial)}), untimed."""
+    (amortised over NL_STRIDE=10 steps) + the CoordinationBase pair loop.  The
+    oracle also checks the GPU's results, untimed (gpu_check: walker -> {"mixed":
+    (s, deriv, virial, sorted pairs), "fp64": (s, deriv, virial), "build_pos": the
+    rebuild frame (frames[w]), "pos": the checked step's positions})."""
     import oracle
     oracle.build()
     orc = oracle.Oracle()
@@ -235,10 +243,9 @@ def cpu_baseline(frames, box, budget_s=10.0, gpu_check=None):
     kind = "port"
     nthreads = orc.max_threads()
     reps, t_loop = 0, 0.0
-    ref0 = None
     while t_loop < budget_s or reps == 0:
         t0 = time.perf_counter()
-        ref0 = orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
+        orc.coordination(SPEC, pos, box, pairs, nthreads=nthreads)
         t_loop += time.perf_counter() - t0
         reps += 1
     per_step = t_loop / reps + t_build / 10.0
@@ -255,16 +262,122 @@ def cpu_baseline(frames, box, budget_s=10.0, gpu_check=None):
     if gpu_check:
         acc = {}
         for w, got in sorted(gpu_check.items()):
-            if w == 0:
-                pw, ref = pairs, ref0
-            else:
-                pw = orc.nl_classic_cells(0, n, 0, frames[w], box, True, 0.8)
-                ref = orc.coordination(SPEC, frames[w], box, pw, nthreads=nthreads)
+            # the list of the rebuild frame, evaluated at the checked step's positions
+            pw = pairs if w == 0 else orc.nl_classic_cells(0, n, 0, got["build_pos"], box, True, 0.8)
+            ref = orc.coordination(SPEC, got["pos"], box, pw, nthreads=nthreads)
             e = {"mixed": accuracy_against(ref, got["mixed"][:3], pw, got["mixed"][3])}
             if "fp64" in got:
                 e["fp64"] = accuracy_against(ref, got["fp64"])
             acc["walker_%d" % w] = e
         out["accuracy"] = acc
+    return out
+
+
+def _time_calls(torch, fn, calls):
+    """Device time per call of fn(k) for k in calls (CUDA events on the default stream, which the library's
+    NULL-stream calls are ordered with)."""
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for k in calls:
+        fn(k)
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) * 1e-3 / max(len(calls), 1)
+
+
+def run_c0(dev, frames=10, cpu=True):
+    """The reference's CPU-runnable case: 1,000 atoms (10^3 lattice at 0.30 nm, sigma 0.03, a 3.0 nm box),
+    GROUPA=1-1000, SWITCH={RATIONAL R_0=0.30 D_0=0.0 NN=6 MM=12 D_MAX=1.0}, no list (499,500 pairs), ten
+    frames each re-jittered.  One CV+force call per frame, as a driver makes it, for the FP64 drop-in and
+    the mixed path."""
+    import torch
+    from plumed2_gb300 import _lib
+    from plumed2_gb300 import frames as FR
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.30 D_0=0.0 NN=6 MM=12 D_MAX=1.0"
+    xs = np.stack([FR.workload_c0(frame=f)[0] for f in range(frames)])
+    box = FR.workload_c0()[1]
+    tx = torch.tensor(xs, dtype=torch.float64, device=dev)
+    s = torch.zeros(1, dtype=torch.float64, device=dev)
+    der = torch.zeros(1000, 3, dtype=torch.float64, device=dev)
+    vir = torch.zeros(9, dtype=torch.float64, device=dev)
+    out = {"workload": "1,000 atoms, 10^3 jittered sc lattice at 0.30 nm in a 3.0 nm box, GROUPA=1-1000, %s, "
+                       "no neighbour list, %d frames, one CV+force call per frame" % (spec, frames),
+           "pairs_per_frame": 499500, "unit": "pair-evals/s"}
+    for prec in ("fp64", "mixed"):
+        c = Coordination("GROUPA=1-1000 SWITCH={%s}" % spec, precision=prec, device=dev.index or 0)
+        call = lambda k: c.forward_device(tx[k % frames].data_ptr(), box[None], 1, s.data_ptr(), der.data_ptr(),
+                                          vir.data_ptr(), step=k)
+        for k in range(3):
+            call(k)
+        t = _time_calls(torch, call, list(range(3, 3 + 3 * frames)))
+        out[prec] = {"us_per_frame": t * 1e6, "value": 499500 / t}
+        c.close()
+    if cpu:
+        import oracle
+        oracle.build()
+        orc = oracle.Oracle()
+        pairs = orc.all_pairs(0, 1000)
+        ref = []
+        t0 = time.perf_counter()
+        for f in range(frames):
+            ref.append(orc.coordination(spec, xs[f], box, pairs, nthreads=1))
+        t1 = (time.perf_counter() - t0) / frames
+        out["cpu_baseline"] = {"value": 499500 / t1, "unit": "pair-evals/s", "cores": 1, "kind": "port",
+                               "sample": "the %d frames, serial pair loop" % frames, "us_per_frame": t1 * 1e6}
+    return out
+
+
+def run_c1(dev, steps=100, cpu=True):
+    """The mixed-precision single-CV case: 32,768 atoms (32^3 lattice at 0.31 nm, sigma 0.03, a 9.92 nm box),
+    GROUPA = the z < L/2 slab, GROUPB = the other, RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.2, NLIST
+    NL_CUTOFF=1.4 NL_STRIDE=20, frames that move by Gaussian steps of 0.002 nm.  One CV+force call per
+    frame on the device, mixed and FP64."""
+    import torch
+    from plumed2_gb300 import frames as FR
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.2"
+    line = "GROUPA=1-16384 GROUPB=16385-32768 SWITCH={%s} NLIST NL_CUTOFF=1.4 NL_STRIDE=20" % spec
+    xs, box = FR.workload_c1(n_frames=steps + 20)
+    tx = torch.tensor(xs, dtype=torch.float64, device=dev)
+    s = torch.zeros(1, dtype=torch.float64, device=dev)
+    der = torch.zeros(32768, 3, dtype=torch.float64, device=dev)
+    vir = torch.zeros(9, dtype=torch.float64, device=dev)
+    out = {"workload": "32,768 atoms, 32^3 jittered sc lattice at 0.31 nm in a 9.92 nm box, two z slabs as "
+                       "GROUPA/GROUPB, %s, NLIST NL_CUTOFF=1.4 NL_STRIDE=20, frames moving by 0.002 nm Gaussian "
+                       "steps; one CV+force call per frame, steps 20..%d timed" % (spec, 19 + steps),
+           "unit": "pair-evals/s"}
+    for prec in ("mixed", "fp64"):
+        c = Coordination(line, precision=prec, device=dev.index or 0)
+        call = lambda k: c.forward_device(tx[k].data_ptr(), box[None], 1, s.data_ptr(), der.data_ptr(),
+                                          vir.data_ptr(), step=k)
+        for k in range(20):
+            call(k)
+        t = _time_calls(torch, call, list(range(20, 20 + steps)))
+        # the list sizes of the timed steps (untimed replay: one size per rebuild interval)
+        pairs = 0
+        for k in range(20, 20 + steps):
+            if k % 20 == 0 or k == 20:
+                call(k)
+                size = c.nl_size()
+            pairs += size
+        out[prec] = {"us_per_step": t * 1e6, "value": pairs / steps / t, "pairs_per_step": pairs / steps}
+        c.close()
+    if cpu:
+        import oracle
+        oracle.build()
+        orc = oracle.Oracle()
+        nth = orc.max_threads()
+        t0 = time.perf_counter()
+        nl = orc.nl_classic_cells(1, 16384, 16384, xs[20], box, True, 1.4)
+        tb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for k in range(20, 25):
+            orc.coordination(spec, xs[k], box, nl, nthreads=nth)
+        tl = (time.perf_counter() - t0) / 5
+        out["cpu_baseline"] = {"value": len(nl) / (tl + tb / 20), "unit": "pair-evals/s", "cores": nth,
+                               "kind": "port", "sample": "five steps' pair loops (OpenMP) + 1/20 of the list build"}
     return out
 
 
@@ -421,7 +534,20 @@ def run_ours(args):
     boxes = np.stack([box] * W)
     line = LINE % (n, SPEC)
     c = Coordination(line, precision="mixed", device=local)
-    tpos = torch.from_numpy(frames).to(dev)
+    # a trajectory per walker: the lattice frame, then Gaussian steps of MOTION_SIGMA per coordinate; step k
+    # uses frame k % 10, so every rebuild (NL_STRIDE = 10) starts from the lattice frame and the nine steps
+    # after it move away from it as an MD run does
+    T = 10
+    traj = torch.empty((T, W, n, 3), dtype=torch.float64, device=dev)
+    traj[0] = torch.from_numpy(frames).to(dev)
+    gen_t = torch.Generator(device=dev).manual_seed(11)
+    for k in range(1, T):
+        traj[k] = traj[k - 1] + MOTION_SIGMA * torch.randn((W, n, 3), generator=gen_t, dtype=torch.float64,
+                                                            device=dev)
+
+    def pos_ptr(st):
+        return traj[st % T].data_ptr()
+
     s = torch.zeros(W, dtype=torch.float64, device=dev)
     der = torch.zeros(W, n, 3, dtype=torch.float64, device=dev)
     vir = torch.zeros(W, 9, dtype=torch.float64, device=dev)
@@ -430,7 +556,7 @@ def run_ours(args):
     step = 0
     # a metadynamics bias per walker: 500 METAD hills (truncated, stretched Gaussians, coord_bias_hills),
     # h = 1.2, sigma = 0.05 s0, centres uniform in [0.8 s0, 1.2 s0], s0 = the walker's first CV
-    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), 0, 0, step=0, flags=_lib.FLAG_NO_DERIV)
+    c.forward_device(pos_ptr(0), boxes, W, s.data_ptr(), 0, 0, step=0, flags=_lib.FLAG_NO_DERIV)
     torch.cuda.synchronize()
     s0 = s.clone()
     gen = torch.Generator(device="cpu").manual_seed(7)
@@ -446,11 +572,11 @@ def run_ours(args):
         """CV (derivatives and virial kept for backward) -> METAD hills bias energy and dV/ds on the device ->
         backward kernel: forces and the box gradient (what a metadynamics step needs)."""
         nonlocal step
-        ctx.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), 0, vir.data_ptr(), step=step,
+        ctx.forward_device(pos_ptr(step), boxes, W, s.data_ptr(), 0, vir.data_ptr(), step=step,
                            flags=_lib.FLAG_SAVE)
         _lib.bias_hills(W, s.data_ptr(), 500, centres.data_ptr(), sigmas.data_ptr(), heights.data_ptr(),
                         energy.data_ptr(), g.data_ptr())
-        ctx.backward_device(tpos.data_ptr(), boxes, W, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(), 0)
+        ctx.backward_device(pos_ptr(step), boxes, W, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(), 0)
         step += 1
 
     for _ in range(args.warmup):
@@ -480,39 +606,47 @@ def run_ours(args):
     ktimes = c.kernel_times()
     kern_ms, kern_n = c.kernel_ms()
     c.set_timing(False)
+    # the lists' near parts after the timed steps (what a step reads while the walkers stay within half
+    # the skin of the rebuild), against their full size
+    near = [c.nl_near_size(w) for w in range(W)]
+    near_info = {"near_entries": sum(x[0] for x in near), "list_entries": sum(c.nl_size(w) for w in range(W)),
+                 "skin_nm": near[0][1]}
     t = reduce_over_ranks(t, "max", dev)
     pairs_job = reduce_over_ranks(pairs_per_step, "sum", dev)
     ms_step = t / args.steps * 1e3
     value = pairs_job * args.steps / t
 
-    # cost of one neighbour-list rebuild against a plain CV+force pass (same inputs), and the
-    # CV+force pass alone (s, ds/dx, virial: CoordinationBase::calculate) averaged over 5 calls
+    # cost of one neighbour-list rebuild (at the next multiple of NL_STRIDE, the lattice frame) against a
+    # plain CV+force pass, and the CV+force pass alone (s, ds/dx, virial: CoordinationBase::calculate) over
+    # the five steps after it
     torch.cuda.synchronize()
+    R = (step // T + 1) * T
     ev0.record()
-    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=step,
+    c.forward_device(pos_ptr(R), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R,
                      flags=_lib.FLAG_REBUILD)
     ev1.record()
     torch.cuda.synchronize()
     t_rebuild_step = ev0.elapsed_time(ev1) * 1e-3
-    base = (step // 10 + 1) * 10 + 1  # five steps between rebuilds (NL_STRIDE=10)
     ev0.record()
-    for k in range(5):
-        c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=base + k)
+    for k in range(1, 6):
+        c.forward_device(pos_ptr(R + k), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R + k)
     ev1.record()
     torch.cuda.synchronize()
     t_plain_step = ev0.elapsed_time(ev1) * 1e-3 / 5
-    # the mixed results of that step for two walkers (checked against the FP64 oracle in the
-    # CPU-baseline leg), and the run-to-run spread of the derivative reduction: the same step
-    # again (its vector atomics add in whatever order the hardware takes)
+    # the mixed results of the last of those steps (R + 5: the list of the lattice frame, the walkers five
+    # steps away from it) for two walkers, checked against the FP64 oracle in the CPU-baseline leg; and the
+    # run-to-run spread of the derivative reduction: the same step again (its vector atomics add in
+    # whatever order the hardware takes)
     check_w = sorted({0, W - 1})
-    gpu_check = {w: {"mixed": (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy(),
-                               np.asarray(c.pairs(w)))} for w in check_w}
+    gpu_check = {}
     for w in check_w:
-        p_ = gpu_check[w]["mixed"][3].reshape(-1, 2)
-        gpu_check[w]["mixed"] = gpu_check[w]["mixed"][:3] + (p_[np.lexsort((p_[:, 1], p_[:, 0]))],)
+        p_ = np.asarray(c.pairs(w)).reshape(-1, 2)
+        gpu_check[w] = {"mixed": (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy(),
+                                  p_[np.lexsort((p_[:, 1], p_[:, 0]))]),
+                        "build_pos": traj[0, w].cpu().numpy(), "pos": traj[5, w].cpu().numpy()}
     der_a = der.clone()
     s_a = s.clone()
-    c.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=base + 4)
+    c.forward_device(pos_ptr(R + 5), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R + 5)
     torch.cuda.synchronize()
     spread = {"deriv_max_abs_diff_rel": float((der - der_a).abs().max().item() / der_a.abs().max().item()),
               "cv_max_abs_diff_rel": float(((s - s_a).abs() / s_a.abs()).max().item()),
@@ -520,19 +654,20 @@ def run_ours(args):
 
     # the plain FP64 GPU path on the same workload (the drop-in, for the 5x target)
     c64 = Coordination(line, precision="fp64", device=local)
-    st64 = 0
-    c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=0)
+    c64.forward_device(pos_ptr(R), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R)
     torch.cuda.synchronize()
     ev0.record()
     for k in range(1, 1 + args.fp64_steps):
-        c64.forward_device(tpos.data_ptr(), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=k)
+        c64.forward_device(pos_ptr(R + k), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R + k)
     ev1.record()
     torch.cuda.synchronize()
     t64 = ev0.elapsed_time(ev1) * 1e-3 / max(args.fp64_steps, 1)
+    if args.fp64_steps != 5:  # the checked step, R + 5
+        c64.forward_device(pos_ptr(R + 5), boxes, W, s.data_ptr(), der.data_ptr(), vir.data_ptr(), step=R + 5)
+        torch.cuda.synchronize()
     for w in check_w:
         gpu_check[w]["fp64"] = (s[w].item(), der[w].cpu().numpy(), vir[w].cpu().numpy())
     c64.close()
-    del st64
 
     line_out = None
     if rank == 0:
@@ -594,33 +729,36 @@ def run_ours(args):
             # all walkers in one call, pinned host arrays
             cb = Coordination(line, precision="mixed", device=local)
             pin = lambda *shape: torch.empty(*shape, dtype=torch.float64, pin_memory=True).numpy()
-            hp, hs, hd, hv = pin(W, n, 3), pin(W), pin(W, n, 3), pin(W, 9)
-            hp[:] = frames
+            # the trajectory's frames in page-locked host memory, one per step of the stride
+            hp, hs, hd, hv = pin(T, W, n, 3), pin(W), pin(W, n, 3), pin(W, 9)
+            hp[:] = traj.cpu().numpy()
             hb = np.ascontiguousarray(np.stack([box.reshape(9)] * W))
-            A = (addr(hp), addr(hb), addr(hs), addr(hd), addr(hv))
-            cb.forward_host_batch(W, A[0], A[1], 0, 0, A[2], A[3], A[4])
+            A = (addr(hb), addr(hs), addr(hd), addr(hv))
+            cb.forward_host_batch(W, addr(hp[0]), A[0], 0, 0, A[1], A[2], A[3])
             n_first = sum(cb.nl_size(w) for w in range(W))  # the lists of steps 1..9
             t0 = time.perf_counter()
             for k in range(1, 1 + args.e2e_steps):
-                cb.forward_host_batch(W, A[0], A[1], k, 0, A[2], A[3], A[4])
+                cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
             te_b = time.perf_counter() - t0
             assert np.all(np.isfinite(hs)) and np.all(hs > 0)
             e2e_v = e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), args.e2e_steps) / te_b
             cb.close()
             ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
-            host_pos = [np.ascontiguousarray(frames[w]) for w in range(W)]
+            # pageable host copies of the trajectory: [step % T][walker]
+            host_pos = [[np.array(hp[k, w]) for w in range(W)] for k in range(T)]
             # per walker force and virial arrays reused from step to step, as an MD engine does; the call is the
             # C ABI's coord_forward with the arrays' addresses, as the PLUMED plugin makes it
             outs = [(np.zeros((n, 3)), np.zeros(9), np.zeros(1)) for _ in range(W)]
             hbox = np.ascontiguousarray(box.reshape(9))
-            ptrs = [(addr(host_pos[w]), addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
+            ptrs = [(addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
+            pptr = [[addr(host_pos[k][w]) for w in range(W)] for k in range(T)]
             for w in range(W):
-                ctxs[w].forward_host(ptrs[w][0], addr(hbox), 0, 0, ptrs[w][1], ptrs[w][2], ptrs[w][3])
+                ctxs[w].forward_host(pptr[0][w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
             n_first = sum(ctxs[w].nl_size() for w in range(W))
             t0 = time.perf_counter()
             for k in range(1, 1 + args.e2e_steps):
                 for w in range(W):
-                    ctxs[w].forward_host(ptrs[w][0], addr(hbox), k, 0, ptrs[w][1], ptrs[w][2], ptrs[w][3])
+                    ctxs[w].forward_host(pptr[k % T][w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
             te = time.perf_counter() - t0
             # the results landed in the caller's arrays
             assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
@@ -632,9 +770,11 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(frames, box, budget_s=8.0, gpu_check=gpu_check)
-        c2 = None
+        c2 = c0 = c1 = None
         if args.c2_steps > 0:
             c2 = run_c2(dev, steps=args.c2_steps, cpu=not args.no_cpu_baseline)
+            c0 = run_c0(dev, cpu=not args.no_cpu_baseline)
+            c1 = run_c1(dev, cpu=not args.no_cpu_baseline)
         line_out = {
             "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -651,6 +791,13 @@ def run_ours(args):
                                "backward kernel (forces and box gradient) for all walkers; NL rebuilt every 10th step",
                        "cv_force_pass_ms": t_plain_step * 1e3, "autotune": c.autotune(),
                        "backward": True, "l2": "working set (0.8 GB) larger than the 129 MB L2",
+                       "motion": "each walker moves by Gaussian steps of %g nm per coordinate per step; step k "
+                                 "uses frame k %% 10, so every rebuild starts from the lattice frame" % MOTION_SIGMA,
+                       "near_parts": dict(near_info, what="entries within D_MAX + skin at the last rebuild: a step "
+                                                          "reads only these while every atom has moved less than "
+                                                          "half the skin since it (far entries are then exactly "
+                                                          "zero); value counts every list entry, as the "
+                                                          "reference's loop does"),
                        "parallelism": "walkers sharded across GPUs, no collective"},
             "roofline": roof, "cpu_baseline": cpu,
             "accuracy": dict((cpu or {}).get("accuracy", {}), run_to_run=spread,
@@ -668,7 +815,7 @@ def run_ours(args):
                                                 "per walker, pageable host arrays",
                                         "host_path": host_path}},
             "gpu_launches": launches, "clocks": clk,
-            "other_configs": {"c2_batched_uneven_actions": c2},
+            "other_configs": {"c2_batched_uneven_actions": c2, "c0_cpu_case": c0, "c1_mixed_single_cv": c1},
         }
         print(json.dumps(line_out), flush=True)
     if ws > 1:
@@ -680,11 +827,16 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "c2":
+    elif args.workload in ("c2", "c1", "c0"):
         import torch
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
-        out = run_c2(dev, steps=args.steps, warmup=args.warmup, cpu=not args.no_cpu_baseline)
+        if args.workload == "c2":
+            out = run_c2(dev, steps=args.steps, warmup=args.warmup, cpu=not args.no_cpu_baseline)
+        elif args.workload == "c1":
+            out = run_c1(dev, steps=args.steps, cpu=not args.no_cpu_baseline)
+        else:
+            out = run_c0(dev, cpu=not args.no_cpu_baseline)
         print(json.dumps(dict(out, metric=METRIC, n_gpus=1, steps=args.steps, warmup=args.warmup,
                               higher_is_better=True, dtype="f32", data="synthetic")), flush=True)
     else:

@@ -227,6 +227,14 @@ int coord_apply_forces(coord_ctx *ctx, int n_frames, const double *ff, int64_t n
 /* nl->size() of the last build for frame f (pairs processed per step,
  * CoordinationBase.cpp:163), including pairs skipped as self pairs. */
 int coord_nl_size(coord_ctx *ctx, int frame, int64_t *n);
+/* No reference counterpart.  Of those pairs, how many lie in the rows' near
+ * parts (within D_MAX plus the skin at the last build): the entries a step
+ * reads while every atom has moved less than half the skin since the build.
+ * Equals coord_nl_size's count less the self pairs when the lists are not
+ * split (no finite D_MAX below NL_CUTOFF, no orthorhombic box, or a sibling
+ * CV).  skin (may be NULL) receives the skin in length units, 0 when not
+ * split. */
+int coord_nl_near_size(coord_ctx *ctx, int frame, int64_t *n, double *skin);
 /* The pair set of the last build for frame f as (first, second) slot pairs
  * in the reference's orientation (first<second for a single list, first in
  * GROUPA otherwise), sorted; writes min(n, cap) pairs, returns n. */

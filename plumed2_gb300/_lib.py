@@ -100,6 +100,7 @@ def load() -> C.CDLL:
         L.coord_forward_device.argtypes = [_vp, C.c_int, _vp, _dp, C.c_int64, C.c_uint, _vp, _vp, _vp, _vp, _vp]
         L.coord_backward_device.argtypes = [_vp, C.c_int, _vp, _dp, _vp, _vp, _vp, _vp, _vp]
         L.coord_nl_size.argtypes = [_vp, C.c_int, C.POINTER(C.c_int64)]
+        L.coord_nl_near_size.argtypes = [_vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
         L.coord_get_pairs.argtypes = [_vp, C.c_int, C.POINTER(C.c_uint32), C.c_int64, C.POINTER(C.c_int64)]
         L.coord_multi_create.argtypes = [C.POINTER(_vp), C.c_int, C.c_int64, C.POINTER(_vp)]
         L.coord_multi_destroy.argtypes = [_vp]

@@ -286,6 +286,12 @@ class Coordination:
         check(self._L, self._ctx, self._L.coord_nl_size(self._ctx, frame, C.byref(n)))
         return n.value
 
+    def nl_near_size(self, frame: int = 0):
+        """(entries in the rows' near parts, skin): coord_nl_near_size."""
+        n, sk = C.c_int64(), C.c_double()
+        check(self._L, self._ctx, self._L.coord_nl_near_size(self._ctx, frame, C.byref(n), C.byref(sk)))
+        return n.value, sk.value
+
     def pairs(self, frame: int = 0) -> np.ndarray:
         n = C.c_int64()
         check(self._L, self._ctx, self._L.coord_get_pairs(self._ctx, frame, None, 0, C.byref(n)))

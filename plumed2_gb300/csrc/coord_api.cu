@@ -69,6 +69,9 @@ struct coord_ctx {
   coord_params p{};
   std::string switch_def;
   SwitchParams sw{};
+  // a CUSTOM switch's compiled expression, and its device copy
+  ExprProgram expr{};
+  DevBuf<ExprProgram> d_expr;
   SwitchF32 s32{};
   int mode = MODE_SINGLE;
   int64_t nA = 0, nB = 0, ns = 0;
@@ -99,6 +102,13 @@ struct coord_ctx {
   // neighbour-list state
   bool firsttime = true;
   int built_frames = 0;
+  // near/far rows of the current lists (k_nl_partition): the skin they were
+  // split with, and the boxes of the rebuild (the fixed-point frame the
+  // displacements are measured in)
+  bool skin_valid = false;
+  double skin = 0.0;
+  std::vector<double> skin_boxes;
+  HostBuf<unsigned> h_disp2;
   int cap = 0, self_cap = 64, ncell_cap = 0, max_blocks = 0;
   int nframes_alloc = 0;
   // device buffers
@@ -114,7 +124,10 @@ struct coord_ctx {
   DevBuf<unsigned char> pair_flag;
   DevBuf<double> acc64, partials, accw64;
   DevBuf<float4> acc32;
-  DevBuf<unsigned> tickets, band_tickets;
+  DevBuf<unsigned> tickets, band_tickets, disp2;
+  DevBuf<int> row_near, slice_wn;
+  DevBuf<uint4> q_build;
+  DevBuf<uint32_t> ell_far;
   DevBuf<unsigned char> band_flag;
   DevBuf<double> band_rec;
   // host-API staging
@@ -134,7 +147,6 @@ struct coord_ctx {
   int tile64 = 64, tile32 = 128, ap_blocks = 0, nl_blocks = 0, nl_unroll = 4;
   // mixed NL pass, tuned per evaluation mode (EVAL_S / EVAL_DERIV / EVAL_PARAM)
   int nlm_blocks[5] = {0, 0, 0, 0, 0}, nlm_unroll[5] = {4, 4, 4, 4, 4};
-  int nlm_compact[5] = {0, 0, 0, 0, 0};  // 1: the queue-compacted pair kernel won the autotuner
   bool nlm_tuned[5] = {false, false, false, false, false};
   int cells_launch = 0;  // cells per frame known on the host (0: use ncell_cap)
   bool tuned = false;
@@ -279,10 +291,15 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->partials, F * (size_t)c->max_blocks * kPartials);
   if (c->p.nlist != COORD_NL_NONE && c->mode != MODE_PAIR) {
     ENS(c->ell, F * (size_t)nslices * (size_t)c->cap * 32);
+    ENS(c->row_near, F * ns);
+    ENS(c->slice_wn, F * std::max(nslices, 1));
+    ENS(c->q_build, F * ns);
+    ENS(c->disp2, 2 * F);
   }
 #undef ENS
   if ((e = c->h_fc.ensure(F)) != cudaSuccess) return c->cuda_fail(e, "pinned allocation");
   if ((e = c->h_nl.ensure(F * 4)) != cudaSuccess) return c->cuda_fail(e, "pinned allocation");
+  if ((e = c->h_disp2.ensure(F)) != cudaSuccess) return c->cuda_fail(e, "pinned allocation");
   c->nframes_alloc = std::max(c->nframes_alloc, n_frames);
   return COORD_OK;
 }
@@ -335,6 +352,13 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.ell = c->ell.p;
   a.row_len = c->row_len.p;
   a.slice_w = c->slice_w.p;
+  // near/far rows: off unless forward_impl turns them on for this call
+  a.row_near = nullptr;
+  a.slice_wn = c->slice_wn.p;
+  a.q_build = c->q_build.p;
+  a.disp2 = nullptr;
+  a.near_r2 = -1.f;
+  a.disp_ok2 = -1.f;
   a.nl_count = c->nl_count.p;
   a.self_pairs = c->self_pairs.p;
   a.pair_flag = c->pair_flag.p;
@@ -485,7 +509,7 @@ bool launch_evaluation_chunked(coord_ctx *c, const KArgs &a, int mode, const Hos
     ak.pos = dpos;
     cudaStreamWaitEvent(s1, evH[k], 0);
     launch_prep_host(ak, dpos, 1, s1);
-    launch_eval_nl32(ak, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->nlm_compact[m], s1);
+    launch_eval_nl32(ak, c->sw, c->s32, mode, nb, c->nlm_unroll[m], s1);
     launch_band_fix(ak, c->sw, c->s32, mode, s1);
     if (io->deriv) {
       launch_finalize32(ak, 1, s1);
@@ -510,6 +534,19 @@ bool fp64_prefilter(const coord_ctx *c) {
   for (const FrameConst &fq : c->fc_uploaded)
     if (fq.pbc.type != PBC_ORTHO || !fq.fixed_ok) return false;
   return true;
+}
+
+// Whether a rebuilt list is split into near and far parts (k_nl_partition):
+// COORDINATION lists (every switching function is zero beyond a finite d_max
+// below the cutoff) in orthorhombic periodic frames, on the paths that keep
+// fixed-point positions (mixed, or the screened FP64 pass).
+bool skin_eligible(const coord_ctx *c) {
+  if (c->p.nlist == COORD_NL_NONE || c->mode == MODE_PAIR || c->cv != COORD_CV_COORDINATION || c->p.nopbc)
+    return false;
+  if (!(c->sw.dmax_2 < 1e300) || !(std::sqrt(c->sw.dmax_2) < c->p.nl_cutoff) || c->fc_uploaded.empty()) return false;
+  for (const FrameConst &fq : c->fc_uploaded)
+    if (fq.pbc.type != PBC_ORTHO || !fq.fixed_ok) return false;
+  return c->p.precision == COORD_PREC_MIXED || fp64_prefilter(c);
 }
 
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
@@ -559,7 +596,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
     if (mixed) {
       const int m = std::min(std::max(mode, 0), 4);
       const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
-      launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->nlm_compact[m], c->stream);
+      launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
       launch_band_fix(a, c->sw, c->s32, mode, c->stream);
     } else {
       launch_eval_nl64(a, c->sw, mode, prefilter64 ? &c->s32 : nullptr, c->stream);
@@ -595,20 +632,14 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
   const int bps[7] = {2, 4, 6, 8, 16, 32, 0}, unr[3] = {2, 4, 8};
   const int m = std::min(std::max(mode, 0), 4);
   float best = 1e30f;
-  int bb = c->nl_blocks, bu = c->nl_unroll, bc = 0;
+  int bb = c->nl_blocks, bu = c->nl_unroll;
   const bool timing = c->timing;
   c->timing = false;
-  // the compacted kernel (modes s, derivatives, parameters) with 2 or 4
-  // entries in flight per lane, beside the plain one with 2, 4 or 8
-  const int ncompact = (mode == EVAL_PERATOM || mode == EVAL_VJP) ? 1 : 2;
   // COORD_AUTOTUNE_LOG=<file>: every candidate's time appended to the file
   const char *log_path = std::getenv("COORD_AUTOTUNE_LOG");
   FILE *log = (log_path && log_path[0]) ? std::fopen(log_path, "a") : nullptr;
-  for (int cv = 0; cv < ncompact; cv++)
   for (int b : bps)
     for (int u : unr) {
-      if (cv == 1 && u == 8) continue;
-      c->nlm_compact[m] = cv;
       const int slices_blocks = (int)(((c->ns + 31) / 32 + 7) / 8);  // blocks of one frame at one slice per warp
       c->nlm_blocks[m] = b > 0 ? b * std::max(c->nsm, 1) : a.nframes * slices_blocks;
       c->nlm_unroll[m] = u;
@@ -624,19 +655,17 @@ void autotune_nl(coord_ctx *c, const KArgs &a, int mode) {
       cudaEventSynchronize(t1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, t0, t1);
-      if (log) std::fprintf(log, "mode=%d blocks=%d unroll=%d compact=%d frames=%d slots=%lld ms=%.4f\n", mode,
-                            c->nlm_blocks[m], u, cv, a.nframes, (long long)c->ns, ms);
+      if (log) std::fprintf(log, "mode=%d blocks=%d unroll=%d frames=%d slots=%lld ms=%.4f\n", mode,
+                            c->nlm_blocks[m], u, a.nframes, (long long)c->ns, ms);
       if (ms < best) {
         best = ms;
         bb = c->nlm_blocks[m];
         bu = u;
-        bc = cv;
       }
     }
   if (log) std::fclose(log);
   c->nlm_blocks[m] = bb;
   c->nlm_unroll[m] = bu;
-  c->nlm_compact[m] = bc;
   c->nlm_tuned[m] = true;
   c->nl_blocks = bb;
   c->nl_unroll = bu;
@@ -785,6 +814,19 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
   // fused host steps leave the device copy stale: the pair kernels' rare
   // exact d_max tests read the caller's array itself
   if (hio && hio->fused) a.pos = hio->pos;
+  // near/far rows: the displacements since the last rebuild are measured
+  // (by this step's gather) only against a rebuild in the same boxes
+  const bool skin_on = nl && skin_eligible(c);
+  const bool same_boxes = c->skin_valid && c->skin_boxes.size() == 9 * (size_t)n_frames &&
+                          std::memcmp(c->skin_boxes.data(), boxes, 9 * sizeof(double) * n_frames) == 0;
+  if (skin_on && same_boxes) {
+    a.disp2 = c->disp2.p;
+    cudaMemsetAsync(c->disp2.p, 0, sizeof(unsigned) * n_frames, c->stream);
+    if (!rebuild) {
+      a.row_near = c->row_near.p;
+      a.disp_ok2 = (float)(0.25 * c->skin * c->skin * (1.0 - 1e-5));
+    }
+  }
   cudaError_t e;
   if (rebuild) cudaMemsetAsync(c->nl_count.p, 0, sizeof(unsigned long long) * 4 * n_frames, c->stream);
   if (need_bounds && (mixed || rebuild)) {
@@ -813,6 +855,10 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
         if ((e = cudaMemcpyAsync(c->h_nl.p, c->nl_count.p, sizeof(unsigned long long) * 4 * n_frames,
                                  cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
           return c->cuda_fail(e, "neighbour-list count");
+        // the largest displacement of the interval that this rebuild ends
+        if (a.disp2 && (e = cudaMemcpyAsync(c->h_disp2.p, a.disp2 + n_frames, sizeof(unsigned) * n_frames,
+                                            cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess)
+          return c->cuda_fail(e, "displacement read-back");
         if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return c->cuda_fail(e, "neighbour-list build");
         unsigned long long need = 0, selfn = 0;
         for (int f = 0; f < n_frames; f++) {
@@ -841,6 +887,37 @@ int forward_impl(coord_ctx *c, int n_frames, const double *d_pos, const double *
     }
     c->firsttime = false;
     c->built_frames = n_frames;
+    if (skin_on) {
+      // the skin of the new lists: half the gap between d_max and the cutoff
+      // after a rebuild in new boxes, otherwise 2.5 x the largest
+      // displacement of the interval just ended (the maximum over its steps'
+      // gathers), at least a quarter and at most all of the gap; only the
+      // time taken depends on it, never the results
+      const double dmax = std::sqrt(c->sw.dmax_2), gap = c->p.nl_cutoff - dmax;
+      double skin = 0.5 * gap;
+      if (a.disp2) {
+        float dmax2 = 0.f;
+        for (int f = 0; f < n_frames; f++) {
+          float v;
+          std::memcpy(&v, &c->h_disp2.p[f], sizeof v);
+          dmax2 = std::max(dmax2, v);
+        }
+        skin = std::min(gap, std::max(0.25 * gap, 2.5 * std::sqrt((double)dmax2)));
+      }
+      if ((e = c->ell_far.ensure((size_t)n_frames * a.nslices * (size_t)c->cap * 32)) != cudaSuccess)
+        return c->cuda_fail(e, "allocation of the partition's scratch");
+      a.ell_far = c->ell_far.p;
+      a.row_near = c->row_near.p;
+      a.disp2 = c->disp2.p;
+      a.near_r2 = (float)((dmax + skin) * (dmax + skin) * (1.0 + 1e-5));
+      launch_nl_partition(a, c->stream);
+      a.disp_ok2 = (float)(0.25 * skin * skin * (1.0 - 1e-5));
+      c->skin = skin;
+      c->skin_valid = true;
+      c->skin_boxes.assign(boxes, boxes + 9 * (size_t)n_frames);
+    } else {
+      c->skin_valid = false;
+    }
   }
 
   const int mode = peratom ? EVAL_PERATOM
@@ -914,6 +991,12 @@ int device_init(coord_ctx *c) {
     return c->cuda_fail(e, "stream");
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
+  if (c->sw.type == SW_CUSTOM) {
+    if ((e = c->d_expr.ensure(1)) != cudaSuccess) return c->cuda_fail(e, "allocation of the expression");
+    if ((e = cudaMemcpy(c->d_expr.p, &c->expr, sizeof c->expr, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return c->cuda_fail(e, "expression upload");
+    c->sw.expr_dev = c->d_expr.p;
+  }
   return COORD_OK;
 }
 
@@ -975,7 +1058,7 @@ int coord_create(const coord_params *p, coord_ctx **out) {
     c->switch_def = p->switch_def;
     char err[512];
     err[0] = 0;
-    const int rc = switch_from_string(p->switch_def, &c->sw, err, sizeof err);
+    const int rc = switch_from_string(p->switch_def, &c->sw, err, sizeof err, &c->expr);
     if (rc == 2) return bad(COORD_ERR_UNSUPPORTED, std::string("problem reading SWITCH keyword : ") + err);
     if (rc) return bad(COORD_ERR_ARG, std::string("problem reading SWITCH keyword : ") + err);
   } else {
@@ -1030,6 +1113,11 @@ int coord_destroy(coord_ctx *c) {
   c->x64.release();
   c->q.release();
   c->qhi.release();
+  c->row_near.release();
+  c->slice_wn.release();
+  c->q_build.release();
+  c->disp2.release();
+  c->ell_far.release();
   c->ell.release();
   c->self_pairs.release();
   c->nl_count.release();
@@ -1044,6 +1132,7 @@ int coord_destroy(coord_ctx *c) {
   c->band_flag.release();
   c->band_rec.release();
   c->d_pos.release();
+  c->d_expr.release();
   c->d_s.release();
   c->d_deriv.release();
   c->d_virial.release();
@@ -1059,6 +1148,7 @@ int coord_destroy(coord_ctx *c) {
   c->h_out.release();
   c->h_fc.release();
   c->h_nl.release();
+  c->h_disp2.release();
   for (auto &pr : c->ev_pool) {
     cudaEventDestroy(pr.first);
     cudaEventDestroy(pr.second);
@@ -1106,6 +1196,7 @@ int coord_set_groups(coord_ctx *c, const int64_t *a, int64_t na, const int64_t *
   c->groups_set = true;
   c->sib_dirty = true;
   c->firsttime = true;
+  c->skin_valid = false;
   c->cap = 0;
   c->fc_uploaded.clear();
   return COORD_OK;
@@ -1501,6 +1592,24 @@ int coord_nl_size(coord_ctx *c, int frame, int64_t *n) {
   return COORD_OK;
 }
 
+int coord_nl_near_size(coord_ctx *c, int frame, int64_t *n, double *skin) {
+  if (!c || !n) return COORD_ERR_ARG;
+  if (c->p.nlist == COORD_NL_NONE || c->mode == MODE_PAIR)
+    return c->fail(COORD_ERR_STATE, "no sliced neighbour list in this context");
+  if (frame < 0 || frame >= c->built_frames) return c->fail(COORD_ERR_STATE, "no neighbour list for that frame");
+  cudaSetDevice(c->p.device);
+  std::vector<int> len((size_t)c->ns);
+  const int *src = (c->skin_valid ? c->row_near.p : c->row_len.p) + (size_t)frame * c->ns;
+  cudaError_t e = cudaMemcpyAsync(len.data(), src, sizeof(int) * len.size(), cudaMemcpyDeviceToHost, c->stream);
+  if (!e) e = cudaStreamSynchronize(c->stream);
+  if (e) return c->cuda_fail(e, "near size");
+  int64_t t = 0;
+  for (int v : len) t += v;
+  *n = t;
+  if (skin) *skin = c->skin_valid ? c->skin : 0.0;
+  return COORD_OK;
+}
+
 int coord_get_pairs(coord_ctx *c, int frame, uint32_t *pairs, int64_t cap, int64_t *n) {
   if (!c || !n) return COORD_ERR_ARG;
   if (c->p.nlist == COORD_NL_NONE) return c->fail(COORD_ERR_STATE, "no neighbour list (NLIST not active)");
@@ -1554,11 +1663,10 @@ int coord_autotune(coord_ctx *c, char *desc, size_t desclen) {
   if (!c) return COORD_ERR_ARG;
   if (desc && desclen)
     std::snprintf(desc, desclen,
-                  "tuned=%d nl_pass(s/deriv/param)=%d/%d/%d blocks, unroll %d/%d/%d, compacted %d/%d/%d "
-                  "allpairs_tile64=%d allpairs_tile32=%d blocks=%d",
+                  "tuned=%d nl_pass(s/deriv/param)=%d/%d/%d blocks, unroll %d/%d/%d allpairs_tile64=%d "
+                  "allpairs_tile32=%d blocks=%d",
                   (int)c->tuned, c->nlm_blocks[0], c->nlm_blocks[1], c->nlm_blocks[2], c->nlm_unroll[0],
-                  c->nlm_unroll[1], c->nlm_unroll[2], c->nlm_compact[0], c->nlm_compact[1], c->nlm_compact[2],
-                  c->tile64, c->tile32, c->ap_blocks);
+                  c->nlm_unroll[1], c->nlm_unroll[2], c->tile64, c->tile32, c->ap_blocks);
   return COORD_OK;
 }
 

@@ -24,7 +24,26 @@ enum SwitchType : int {
   SW_CUBIC,
   SW_TANH,
   SW_COSINUS,
-  SW_Q
+  SW_Q,
+  SW_CUSTOM                // leptonSwitch (SwitchingFunction.cpp:553-760): an expression of x or x2
+};
+
+// A CUSTOM switching function's expression (lepton syntax, one variable: x or
+// x2) as a postfix program run on (value, derivative) pairs: host_setup.cpp
+// compiles it (expr_compile), switch_eval.cuh runs it (expr_run).
+enum ExprOp : unsigned char {
+  EX_VAR, EX_CONST, EX_ADD, EX_SUB, EX_MUL, EX_DIV, EX_POW, EX_POWC, EX_NEG,
+  EX_SQRT, EX_EXP, EX_LOG, EX_SIN, EX_COS, EX_SEC, EX_CSC, EX_TAN, EX_COT, EX_ASIN, EX_ACOS, EX_ATAN,
+  EX_SINH, EX_COSH, EX_TANH, EX_ERF, EX_ERFC, EX_STEP, EX_DELTA, EX_SQUARE, EX_CUBE, EX_RECIP, EX_ABS,
+  EX_FLOOR, EX_CEIL, EX_ATAN2, EX_MIN, EX_MAX, EX_SELECT
+};
+constexpr int kExprMaxOps = 160;
+constexpr int kExprMaxStack = 24;
+struct ExprProgram {
+  int n;                      // operations
+  int var_x2;                 // the variable is x2 (else x)
+  unsigned char op[kExprMaxOps];
+  double cst[kExprMaxOps];    // the value of EX_CONST, the exponent of EX_POWC
 };
 
 struct SwitchParams {
@@ -44,11 +63,19 @@ struct SwitchParams {
   // R_0/D_0 do not enter as (r - d0)/r0 (CUBIC, Q).
   double c_r0, c_d0;
   int grad_ok;
+  // SW_CUSTOM: the compiled expression, host and device copies (owned by the
+  // context that parsed the switch)
+  const ExprProgram *expr_host;
+  const ExprProgram *expr_dev;
 };
 
 // Parses SWITCH={...} (SwitchingFunction::set(string), SwitchingFunction.cpp:
-// 1055-1159).  Returns 0 or writes a message into err.
-int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen);
+// 1055-1159).  Returns 0 or writes a message into err (2: valid input the
+// caller cannot take -- a CUSTOM function when prog is null).  A CUSTOM
+// function is compiled into *prog, which sw->expr_host points to.
+int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen, ExprProgram *prog = nullptr);
+// Compiles a lepton expression of x or x2; 0, or 1 with a message.
+int expr_compile(const char *text, ExprProgram *prog, char *err, int errlen);
 // The R_0/NN/MM/D_0 form (SwitchingFunction::set(nn,mm,r0,d0), :1176-1184).
 int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw);
 // Host-side evaluation (same code as the device FP64 evaluator).

@@ -166,8 +166,9 @@ __global__ void __launch_bounds__(256) k_eval_nl64q(KArgs a, SwitchParams sw, Sw
   if (slice < a.nslices) {  // warp-uniform
     const int r = slice * 32 + lane;
     const bool active = r < a.ns;
-    const int len = active ? a.row_len[fo + r] : 0;
-    const int w = a.slice_w[(size_t)f * a.nslices + slice];
+    const bool near_only = near_rows_only(a, f);
+    const int len = active ? (near_only ? a.row_near[fo + r] : a.row_len[fo + r]) : 0;
+    const int w = (near_only ? a.slice_wn : a.slice_w)[(size_t)f * a.nslices + slice];
     const uint4 *__restrict__ q = a.q + fo;
     const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
     const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
@@ -204,6 +205,13 @@ __global__ void __launch_bounds__(256) k_eval_nl64q(KArgs a, SwitchParams sw, Sw
           sig = v.f;
           df = v.d;
         }
+      } else if constexpr (NH > 0) {
+        // fixedRational<2 NH> only: the reference's distance, then the same switch
+        if (rfirst)
+          pbc_distance(fc.pbc, xr, xp, d);
+        else
+          pbc_distance(fc.pbc, xp, xr, d);
+        sig = ratfix_sqr<NH>(sw, mod2(d), df);
       } else {
         sig = rfirst ? pair_fp64(a, sw, fc, xr, xp, 0, 0, d, df) : pair_fp64(a, sw, fc, xp, xr, 0, 0, d, df);
       }
@@ -285,8 +293,14 @@ __device__ __forceinline__ void sw32(const SwitchParams &sw, const SwitchF32 &s,
     float xp = 1.0f;
 #pragma unroll
     for (int i = 0; i < NH - 1; i++) xp *= x;
-    // 1/(1 + x^N): the hardware reciprocal (2 ulp), the argument is >= 1
-    const float s0 = __fdividef(1.0f, fmaf(xp, x, 1.0f));
+    // 1/(1 + x^N): the hardware's approximate reciprocal (the argument is
+    // >= 1), then one Newton-Raphson step r += r (1 - y r), which leaves it
+    // within about half an ulp and without the approximation's bias (the CV
+    // is a sum of millions of these values, so a bias of one ulp shows as a
+    // relative error of 1e-7 in s)
+    const float y = fmaf(xp, x, 1.0f);
+    float s0 = __fdividef(1.0f, y);
+    s0 = fmaf(s0, fmaf(-y, s0, 1.0f), s0);
     sig = fmaf(s0, s.stretch, s.shift);
     df = s.c * xp * s0 * s0;
   } else {
@@ -335,42 +349,23 @@ struct Acc32 {
     cv64 += (double)cvs;
     cvs = 0.f;
   }
-  // The slice's FP32 sums (s in cvs, the virial, the parameter gradients)
-  // added to a lane's FP64 totals tot[32 k] (kSliceSums quantities, stride
-  // 32), then cleared.
-  template <int MODE> __device__ __forceinline__ void flush_slice(double *tot) {
-    tot[0] += (double)cvs;
+  // The warp's FP32 sums of the last slices (s in cvs, the virial, the
+  // parameter gradients): summed over the warp's lanes in FP32 (a fixed
+  // butterfly, so every lane holds the same value), added by lane 0 to the
+  // warp's FP64 totals wt[kSliceSums], then cleared.
+  template <int MODE> __device__ __forceinline__ void flush_warp(double *wt, int lane) {
+    constexpr int nq = (MODE == EVAL_S) ? 1 : (MODE == EVAL_PARAM ? 9 : 7);
+    float v[9] = {cvs, vxx, vyy, vzz, vxy, vxz, vyz, pr0, pd0};
+#pragma unroll
+    for (int k = 0; k < nq; k++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < nq; k++) wt[k] += (double)v[k];
     cvs = 0.f;
-    if (MODE >= EVAL_DERIV) {
-      tot[32 * 1] += (double)vxx;
-      tot[32 * 2] += (double)vyy;
-      tot[32 * 3] += (double)vzz;
-      tot[32 * 4] += (double)vxy;
-      tot[32 * 5] += (double)vxz;
-      tot[32 * 6] += (double)vyz;
-      vxx = vyy = vzz = vxy = vxz = vyz = 0.f;
-    }
-    if (MODE == EVAL_PARAM) {
-      tot[32 * 7] += (double)pr0;
-      tot[32 * 8] += (double)pd0;
-      pr0 = pd0 = 0.f;
-    }
-  }
-  template <int MODE> __device__ __forceinline__ static void totals_to_partials(const double *tot,
-                                                                                 double part[kPartials]) {
-    part[0] = tot[0];
-    const double xx = tot[32], yy = tot[64], zz = tot[96], xy = tot[128], xz = tot[160], yz = tot[192];
-    part[1] = xx;
-    part[2] = xy;
-    part[3] = xz;
-    part[4] = xy;
-    part[5] = yy;
-    part[6] = yz;
-    part[7] = xz;
-    part[8] = yz;
-    part[9] = zz;
-    part[10] = tot[224];
-    part[11] = tot[256];
+    vxx = vyy = vzz = vxy = vxz = vyz = 0.f;
+    pr0 = pd0 = 0.f;
   }
   __device__ __forceinline__ void add_s(float sig) {
     const float yk = sig - cvc;
@@ -459,21 +454,23 @@ __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)
 // positions, gathered many times, stay resident in L2.  (A grid that visits
 // the frames in order, for L2 locality, measured 2x slower: the per-frame
 // block barrier costs more than the locality gains.)
+// (four resident blocks of 256 threads per SM: a 64-register budget, which
+// the latency of the partner gathers needs more than registers)
 template <int NH, int MODE, int kUnroll>
-__global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
+__global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  // each lane's FP64 totals of its FP32 sums (s, the six virial components,
+  // each warp's FP64 totals of its FP32 sums (s, the six virial components,
   // the two parameter gradients): a lane sums the pairs of its rows over
-  // kFlushSlices slices (a few tens of pairs) in FP32, then adds those sums
-  // here in FP64, so no FP32 sum runs longer (shared memory rather than
-  // registers: the kernel is held at 64 registers; flushing every slice
-  // measured 8 % slower, the FP64 additions queueing on the FP64 pipe)
-  __shared__ double tot[8][kSliceSums][32];
-  double *const mytot = &tot[threadIdx.x >> 5][0][lane];
-#pragma unroll
-  for (int k = 0; k < kSliceSums; k++) mytot[32 * k] = 0.0;
+  // kFlushSlices slices (about 150 pairs) in FP32, the warp sums its lanes
+  // in FP32, and lane 0 adds the result here in FP64, so no FP32 sum runs
+  // longer.  (Per-lane FP64 totals in shared memory measured 4 % slower:
+  // their 21 KB per block came out of L1, which holds the partners.)
+  __shared__ double wtot[8][kSliceSums];
+  double *const mytot = wtot[threadIdx.x >> 5];
+  if (lane < kSliceSums) mytot[lane] = 0.0;
+  __syncwarp();
   const int nw = gridDim.x * wpb;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];
@@ -483,7 +480,11 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
   Acc32 acc;
   const size_t slice_words = (size_t)a.cap * 32;
   const uint32_t *ell_f = a.ell + (size_t)f * a.nslices * slice_words;
-  const int *sw_f = a.slice_w + (size_t)f * a.nslices;
+  // rows read to their near parts while the atoms have moved less than half
+  // the skin since the rebuild (near_rows_only), else in full
+  const bool near_only = near_rows_only(a, f);
+  const int *sw_f = (near_only ? a.slice_wn : a.slice_w) + (size_t)f * a.nslices;
+  const int *rl_f = (near_only ? a.row_near : a.row_len) + fo;
   int pending = 0;  // slices summed in FP32 since the last flush
   {
     // this warp's first slice: its entries (w rows of 32 words) into L2
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
   for (int slice = blockIdx.x * wpb + (threadIdx.x >> 5); slice < a.nslices; slice += nw) {
     const int r = slice * 32 + lane;
     const bool active = r < a.ns;
-    const int len = active ? a.row_len[fo + r] : 0;
+    const int len = active ? rl_f[r] : 0;
     const int w = sw_f[slice];
     if (lane == 0 && slice + nw < a.nslices) {
       // the next slice's entries stream into L2 while this one is evaluated
@@ -565,154 +566,23 @@ __global__ void __launch_bounds__(256) k_eval_nl32(KArgs a, SwitchParams sw, Swi
     if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
     if (++pending == kFlushSlices) {
-      acc.flush_slice<MODE>(mytot);
+      acc.flush_warp<MODE>(mytot, lane);
       pending = 0;
     }
   }
-  acc.flush_slice<MODE>(mytot);
-  double part[kPartials];
-  Acc32::totals_to_partials<MODE>(mytot, part);
-  block_partials_finish(a, f, part, gridDim.x);
-}
-
-// The same pass with the evaluation compacted (modes s, derivatives,
-// parameters).  About 40 % of the list entries lie inside d_max; in
-// k_eval_nl32 every entry pays for the switch, the reductions and the virial
-// whenever any lane of the warp needs them.  Here each lane screens its
-// entries (entry -> partner position -> FP32 r^2) and the warp appends the
-// pairs inside d_max to a queue in shared memory (ballot + prefix count);
-// whenever 32 or more are waiting, the warp evaluates them 32 at a time with
-// every lane busy.  A queued pair carries its delta, its partner rank and its
-// row's lane: the partner's derivative goes to the global accumulator by a
-// vector reduction as before, the row's to a per-lane sum in shared memory
-// that the row's own lane adds to its accumulator at the end of the slice.
-// The slice's s, virial and parameter sums stay in the evaluating lane and
-// are flushed per slice as in k_eval_nl32; band pairs are flagged the same
-// way.
-template <int NH, int MODE, int kUnroll>
-__global__ void __launch_bounds__(256) k_eval_nl32c(KArgs a, SwitchParams sw, SwitchF32 s32) {
-  constexpr int kQ = 32 * (kUnroll + 1);  // at most 31 waiting + 32 per unrolled entry
-  const int f = blockIdx.y + a.frame0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  const int nw = gridDim.x * wpb;
-  const size_t fo = (size_t)f * a.ns;
-  const FrameConst &fc = a.fc[f];
-  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
-  const uint4 *__restrict__ q = a.q + fo;
-  float4 *__restrict__ acc4 = a.acc32 + fo;
-  __shared__ double tot[8][kSliceSums][32];
-  __shared__ float4 qd[8][kQ];          // queued pairs: delta (x_p - x_r) and the partner rank's bits
-  __shared__ unsigned char ql[8][kQ];   // the row lane of each queued pair
-  __shared__ float4 racc[8][32];        // row-side sums of the slice's evaluated pairs
-  double *const mytot = &tot[warp][0][lane];
-#pragma unroll
-  for (int k = 0; k < kSliceSums; k++) mytot[32 * k] = 0.0;
-  float4 *const qdw = qd[warp];
-  unsigned char *const qlw = ql[warp];
-  float4 *const rac = racc[warp];
-  rac[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const unsigned below = (1u << lane) - 1u;
-  Acc32 acc;
-  int pending = 0;  // slices summed in FP32 since the last flush
-  const size_t slice_words = (size_t)a.cap * 32;
-  const uint32_t *ell_f = a.ell + (size_t)f * a.nslices * slice_words;
-  const int *sw_f = a.slice_w + (size_t)f * a.nslices;
-  {
-    const int s0 = blockIdx.x * wpb + warp;
-    if (lane == 0 && s0 < a.nslices) {
-      const int w0 = sw_f[s0];
-      if (w0 > 0) prefetch_l2_bulk(ell_f + (size_t)s0 * slice_words, (uint32_t)w0 * 128u);
-    }
+  acc.flush_warp<MODE>(mytot, lane);
+  // the block's record: the warps' totals summed in warp order
+  __syncthreads();
+  if (threadIdx.x < kPartials) {
+    // record layout (s, virial row-major, ds/dR_0, ds/dD_0) from the totals
+    // (s, xx, yy, zz, xy, xz, yz, ds/dR_0, ds/dD_0): total index of record
+    // entry k is nibble k of 0x873656245410
+    const int src = (int)((0x873656245410ull >> (4 * threadIdx.x)) & 15ull);
+    double v = 0.0;
+    for (int w2 = 0; w2 < wpb; w2++) v += wtot[w2][src];
+    a.partials[((size_t)f * a.max_blocks + blockIdx.x) * kPartials + threadIdx.x] = v;
   }
-  // evaluates queued pair i (one per lane)
-  auto evaluate = [&](int i) {
-    const float4 it = qdw[i];
-    const int rl = qlw[i];
-    const int p = __float_as_int(it.w);
-    const float r2 = fmaf(it.x, it.x, fmaf(it.y, it.y, it.z * it.z));
-    float sig, df;
-    sw32<NH>(sw, s32, r2, sig, df);
-    acc.add_s_slice(sig);
-    if (MODE >= EVAL_DERIV) {
-      const float ddx = df * it.x, ddy = df * it.y, ddz = df * it.z;
-      red_add_v4(acc4 + p, ddx, ddy, ddz);
-      atomicAdd(&rac[rl].x, -ddx);
-      atomicAdd(&rac[rl].y, -ddy);
-      atomicAdd(&rac[rl].z, -ddz);
-      acc.add_vir(ddx, ddy, ddz, it.x, it.y, it.z);
-    }
-    if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
-  };
-  const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
-  const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
-  for (int slice = blockIdx.x * wpb + warp; slice < a.nslices; slice += nw) {
-    const int r = slice * 32 + lane;
-    const bool active = r < a.ns;
-    const int len = active ? a.row_len[fo + r] : 0;
-    const int w = sw_f[slice];
-    if (lane == 0 && slice + nw < a.nslices) {
-      const int wn = sw_f[slice + nw];
-      if (wn > 0) prefetch_l2_bulk(ell_f + (size_t)(slice + nw) * slice_words, (uint32_t)wn * 128u);
-    }
-    const uint4 qr = active ? q[r] : make_uint4(0u, 0u, 0u, 0u);
-    const uint32_t *__restrict__ e = ell_f + (size_t)slice * slice_words + lane;
-    uint32_t band_min = 0xffffffffu;
-    int qn = 0;  // queued pairs (warp-uniform)
-    for (int k = 0; k < w; k += kUnroll) {
-      int p[kUnroll];
-      uint4 qp[kUnroll];
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldcs(e + (size_t)(k + u) * 32) & kRankMask) : -1;
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) {
-        const float dx = fixed_delta(qr.x, qp[u].x, sx);
-        const float dy = fixed_delta(qr.y, qp[u].y, sy);
-        const float dz = fixed_delta(qr.z, qp[u].z, sz);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool in = p[u] >= 0 && r2 <= s32.dmax2_lo;
-        if (!in) band_min = min(band_min, __float_as_uint(r2) - band_lo);
-        const unsigned b = __ballot_sync(0xffffffffu, in);
-        if (in) {
-          const int at = qn + __popc(b & below);
-          qdw[at] = make_float4(dx, dy, dz, __int_as_float(p[u]));
-          qlw[at] = (unsigned char)lane;
-        }
-        qn += __popc(b);
-      }
-      if (qn >= 32) {
-        __syncwarp();
-        int h = 0;
-        for (; h + 32 <= qn; h += 32) evaluate(h + lane);
-        __syncwarp();
-        if (lane < qn - h) {  // the rest to the front (source and destination do not overlap)
-          qdw[lane] = qdw[h + lane];
-          qlw[lane] = qlw[h + lane];
-        }
-        __syncwarp();
-        qn -= h;
-      }
-    }
-    __syncwarp();
-    if (lane < qn) evaluate(lane);
-    __syncwarp();
-    if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
-    if (MODE >= EVAL_DERIV) {
-      const float4 ra = rac[lane];
-      rac[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (len > 0 && (ra.x != 0.f || ra.y != 0.f || ra.z != 0.f)) red_add_v4(acc4 + r, ra.x, ra.y, ra.z);
-    }
-    if (++pending == kFlushSlices) {
-      acc.flush_slice<MODE>(mytot);
-      pending = 0;
-    }
-  }
-  acc.flush_slice<MODE>(mytot);
-  double part[kPartials];
-  Acc32::totals_to_partials<MODE>(mytot, part);
-  block_partials_finish(a, f, part, gridDim.x);
+  block_records_finish(a, f, gridDim.x);
 }
 
 // FP64 fix-up of the mixed NL pass: the slices flagged by k_eval_nl32 scan

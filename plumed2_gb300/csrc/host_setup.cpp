@@ -130,6 +130,17 @@ struct Words {
       }
     return 0;
   }
+  // KEY=text; true when found
+  bool get_string(const char *key, std::string *v) {
+    const std::string k = std::string(key) + "=";
+    for (size_t i = 0; i < w.size(); i++)
+      if (w[i].compare(0, k.size(), k) == 0) {
+        *v = w[i].substr(k.size());
+        w.erase(w.begin() + i);
+        return true;
+      }
+    return false;
+  }
   bool flag(const char *key) {
     for (size_t i = 0; i < w.size(); i++)
       if (w[i] == key) {
@@ -140,16 +151,23 @@ struct Words {
   }
 };
 
+// Tools::getWords (Tools.cpp:201-270) with its defaults: blanks separate
+// words outside braces; a brace that opens or closes the outermost level is
+// dropped, inner ones are kept (so FUNC={1 / (1 + x^6)} is one word).
 Words split(const char *def) {
   Words W;
   std::string cur;
+  int level = 0;
   for (const char *p = def; *p; ++p) {
     const char c = *p;
-    if (c == ' ' || c == '\t' || c == '\n' || c == '{' || c == '}') {
-      if (!cur.empty()) W.w.push_back(cur);
+    if (c == '}') level = std::max(0, level - 1);
+    const bool blank = c == ' ' || c == '\t' || c == '\n';
+    const bool brace = c == '{' || c == '}';
+    if (!(level == 0 && (blank || brace))) cur.push_back(c);
+    if (c == '{') level++;
+    if (level == 0 && blank && !cur.empty()) {
+      W.w.push_back(cur);
       cur.clear();
-    } else {
-      cur.push_back(c);
     }
   }
   if (!cur.empty()) W.w.push_back(cur);
@@ -164,7 +182,7 @@ Words split(const char *def) {
 void setup_param_grad(SwitchParams *s) {
   s->c_r0 = 0.0;
   s->c_d0 = 0.0;
-  s->grad_ok = !(s->type == SW_CUBIC || s->type == SW_Q);
+  s->grad_ok = !(s->type == SW_CUBIC || s->type == SW_Q || s->type == SW_CUSTOM);
   if (!s->grad_ok || !s->stretched || s->r0_syntax) return;
   const double xd = (s->dmax - s->d0) * s->invr0;
   if (!(xd > 0.0)) return;
@@ -174,6 +192,265 @@ void setup_param_grad(SwitchParams *s) {
 }
 
 } // namespace
+
+// ---------------------------------------------------------------------------
+// CUSTOM expressions: lepton's grammar (src/lepton/Parser.cpp) parsed into a
+// tree, constant subtrees folded to numbers (as ParsedExpression::optimize
+// precalculates them; a constant exponent becomes a constant power), then
+// emitted as the postfix program that expr_run executes.
+// ---------------------------------------------------------------------------
+namespace {
+struct ExprNode {
+  int op;                  // ExprOp
+  double c = 0.0;          // EX_CONST value, EX_POWC exponent
+  int kid[3] = {-1, -1, -1};
+  bool var = false;        // depends on the variable
+};
+
+struct ExprParser {
+  const std::string src;
+  size_t at = 0;
+  std::vector<ExprNode> nodes;
+  std::string err;
+  bool saw_x = false, saw_x2 = false, saw_other = false;
+
+  int add(int op, int a = -1, int b = -1, int c = -1) {
+    ExprNode n;
+    n.op = op;
+    n.kid[0] = a;
+    n.kid[1] = b;
+    n.kid[2] = c;
+    for (int k : n.kid)
+      if (k >= 0 && nodes[k].var) n.var = true;
+    nodes.push_back(n);
+    return (int)nodes.size() - 1;
+  }
+  int constant(double v) {
+    ExprNode n;
+    n.op = EX_CONST;
+    n.c = v;
+    nodes.push_back(n);
+    return (int)nodes.size() - 1;
+  }
+  char peek() {
+    while (at < src.size() && (src[at] == ' ' || src[at] == '\t')) at++;
+    return at < src.size() ? src[at] : '\0';
+  }
+  void fail(const std::string &m) {
+    if (err.empty()) err = m + " in expression \"" + src + "\"";
+  }
+  static int function_op(const std::string &name, int *nargs) {
+    static const struct {
+      const char *name;
+      int op, nargs;
+    } table[] = {{"sqrt", EX_SQRT, 1},  {"exp", EX_EXP, 1},     {"log", EX_LOG, 1},     {"sin", EX_SIN, 1},
+                 {"cos", EX_COS, 1},    {"sec", EX_SEC, 1},     {"csc", EX_CSC, 1},     {"tan", EX_TAN, 1},
+                 {"cot", EX_COT, 1},    {"asin", EX_ASIN, 1},   {"acos", EX_ACOS, 1},   {"atan", EX_ATAN, 1},
+                 {"atan2", EX_ATAN2, 2}, {"sinh", EX_SINH, 1},  {"cosh", EX_COSH, 1},   {"tanh", EX_TANH, 1},
+                 {"erf", EX_ERF, 1},    {"erfc", EX_ERFC, 1},   {"step", EX_STEP, 1},   {"delta", EX_DELTA, 1},
+                 {"square", EX_SQUARE, 1}, {"cube", EX_CUBE, 1}, {"recip", EX_RECIP, 1}, {"min", EX_MIN, 2},
+                 {"max", EX_MAX, 2},    {"abs", EX_ABS, 1},     {"floor", EX_FLOOR, 1}, {"ceil", EX_CEIL, 1},
+                 {"select", EX_SELECT, 3}};
+    for (const auto &t : table)
+      if (name == t.name) {
+        *nargs = t.nargs;
+        return t.op;
+      }
+    return -1;
+  }
+  // lepton::Constants()
+  static bool named(const std::string &n, double *v) {
+    const double pi = 3.14159265358979323846;
+    if (n == "e") *v = std::exp(1.0);
+    else if (n == "log2e") *v = 1.0 / std::log(2.0);
+    else if (n == "log10e") *v = 1.0 / std::log(10.0);
+    else if (n == "ln2") *v = std::log(2.0);
+    else if (n == "ln10") *v = std::log(10.0);
+    else if (n == "pi") *v = pi;
+    else if (n == "pi_2") *v = pi * 0.5;
+    else if (n == "pi_4") *v = pi * 0.25;
+    else if (n == "sqrt2") *v = std::sqrt(2.0);
+    else if (n == "sqrt1_2") *v = std::sqrt(0.5);
+    else return false;
+    return true;
+  }
+  int operand() {
+    const char ch = peek();
+    if (ch == '(') {
+      at++;
+      const int e = binary(0);
+      if (peek() != ')') fail("unbalanced parentheses");
+      else at++;
+      return e;
+    }
+    if (ch == '-') {  // unary minus binds at precedence 2
+      at++;
+      return add(EX_NEG, binary(2));
+    }
+    if (std::isdigit((unsigned char)ch) || ch == '.') {
+      const size_t start = at;
+      bool exp_seen = false;
+      while (at < src.size()) {
+        const char d = src[at];
+        if (std::isdigit((unsigned char)d) || d == '.') {
+          at++;
+        } else if ((d == 'e' || d == 'E') && !exp_seen) {
+          exp_seen = true;
+          at++;
+          if (at < src.size() && (src[at] == '+' || src[at] == '-')) at++;
+        } else {
+          break;
+        }
+      }
+      const std::string num = src.substr(start, at - start);
+      char *end = nullptr;
+      const double v = std::strtod(num.c_str(), &end);
+      if (end == num.c_str() || *end) fail("could not parse the number " + num);
+      return constant(v);
+    }
+    if (std::isalpha((unsigned char)ch) || ch == '_') {
+      const size_t start = at;
+      while (at < src.size() && (std::isalnum((unsigned char)src[at]) || src[at] == '_')) at++;
+      const std::string name = src.substr(start, at - start);
+      if (peek() == '(') {
+        at++;
+        int nargs = 0;
+        const int op = function_op(name, &nargs);
+        if (op < 0) {
+          fail("unknown function: " + name);
+          return constant(0.0);
+        }
+        int args[3] = {-1, -1, -1};
+        for (int k = 0; k < nargs && err.empty(); k++) {
+          if (k > 0) {
+            if (peek() != ',') {
+              fail("wrong number of arguments to " + name);
+              break;
+            }
+            at++;
+          }
+          args[k] = binary(0);
+        }
+        if (peek() != ')') fail("wrong number of arguments to " + name);
+        else at++;
+        return add(op, args[0], args[1], args[2]);
+      }
+      double v;
+      if (name == "x" || name == "x2") {
+        (name == "x" ? saw_x : saw_x2) = true;
+      } else if (named(name, &v)) {
+        return constant(v);
+      } else {
+        saw_other = true;  // lepton takes it for a variable; the switch refuses it
+      }
+      ExprNode n;
+      n.op = EX_VAR;
+      n.var = true;
+      nodes.push_back(n);
+      return (int)nodes.size() - 1;
+    }
+    fail(std::string("unexpected character '") + ch + "'");
+    at = src.size();
+    return constant(0.0);
+  }
+  // + - * / ^ at precedences 0 0 1 1 3; ^ groups to the right
+  int binary(int prec) {
+    int lhs = operand();
+    while (err.empty()) {
+      const char ch = peek();
+      const int op = ch == '+' ? EX_ADD : ch == '-' ? EX_SUB : ch == '*' ? EX_MUL : ch == '/' ? EX_DIV
+                                                               : ch == '^' ? EX_POW : -1;
+      if (op < 0) break;
+      const int p = (op == EX_ADD || op == EX_SUB) ? 0 : (op == EX_POW ? 3 : 1);
+      if (p < prec) break;
+      at++;
+      const int rhs = binary(op == EX_POW ? p : p + 1);
+      lhs = add(op, lhs, rhs);
+    }
+    return lhs;
+  }
+};
+
+// Postfix code of the subtree at i into prog (folding constant subtrees).
+struct ExprEmitter {
+  std::vector<ExprNode> &nodes;
+  ExprProgram *prog;
+  std::string err;
+  void put(int op, double c = 0.0) {
+    if (prog->n >= kExprMaxOps) {
+      err = "expression too long";
+      return;
+    }
+    prog->op[prog->n] = (unsigned char)op;
+    prog->cst[prog->n] = c;
+    prog->n++;
+  }
+  // the value of a subtree that does not depend on the variable
+  double value_of(int i) {
+    ExprProgram tmp{};
+    ExprEmitter sub{nodes, &tmp, ""};
+    sub.emit(i, false);
+    if (!sub.err.empty()) err = sub.err;
+    return expr_run(tmp, 0.0).f;
+  }
+  void emit(int i, bool fold) {
+    ExprNode &n = nodes[i];
+    if (fold && !n.var && n.op != EX_CONST) {
+      put(EX_CONST, value_of(i));
+      return;
+    }
+    if (n.op == EX_POW && fold && !nodes[n.kid[1]].var) {
+      emit(n.kid[0], fold);
+      put(EX_POWC, value_of(n.kid[1]));
+      return;
+    }
+    for (int k : n.kid)
+      if (k >= 0) emit(k, fold);
+    put(n.op, n.c);
+  }
+};
+}  // namespace
+
+int expr_compile(const char *text, ExprProgram *prog, char *err, int errlen) {
+  std::memset(prog, 0, sizeof *prog);
+  ExprParser ps{text ? text : ""};
+  int root = -1;
+  if (ps.src.find_first_not_of(" \t") == std::string::npos) ps.fail("empty expression");
+  else root = ps.binary(0);
+  if (ps.err.empty() && ps.peek() != '\0') ps.fail("unexpected characters at the end");
+  if (!ps.err.empty()) {
+    std::snprintf(err, errlen, "Parse error: %s", ps.err.c_str());
+    return 1;
+  }
+  // leptonSwitch::funcAndDeriv (SwitchingFunction.cpp:566-585)
+  if (ps.saw_other || (ps.saw_x && ps.saw_x2)) {
+    std::snprintf(err, errlen,
+                  "Please declare a function with only ONE argument that can only be x or x2. Your function is: %s",
+                  text);
+    return 1;
+  }
+  ExprEmitter em{ps.nodes, prog, ""};
+  em.emit(root, true);
+  if (!em.err.empty()) {
+    std::snprintf(err, errlen, "%s", em.err.c_str());
+    return 1;
+  }
+  // stack depth within what expr_run holds
+  int depth = 0, deepest = 0;
+  for (int i = 0; i < prog->n; i++) {
+    const int op = prog->op[i];
+    if (op == EX_VAR || op == EX_CONST) depth++;
+    else if (op == EX_SELECT) depth -= 2;
+    else if ((op >= EX_ADD && op <= EX_POW) || op >= EX_ATAN2) depth--;
+    deepest = std::max(deepest, depth);
+  }
+  if (deepest > kExprMaxStack) {
+    std::snprintf(err, errlen, "expression too deeply nested for the device evaluator");
+    return 1;
+  }
+  prog->var_x2 = ps.saw_x2 ? 1 : 0;
+  return 0;
+}
 
 int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw) {
   if (mm == 0) mm = 2 * nn;
@@ -186,7 +463,7 @@ int switch_from_rational(int nn, int mm, double r0, double d0, SwitchParams *sw)
   return 0;
 }
 
-int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen) {
+int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen, ExprProgram *prog) {
   Words W = split(def);
   std::string e;
   if (W.w.empty()) {
@@ -251,9 +528,21 @@ int switch_from_string(const char *def, SwitchParams *sw, char *err, int errlen)
       data_init(sw, d0, dmax, r0);
       sw->type = SW_COSINUS;
     } else if (name == "CUSTOM" || name == "MATHEVAL") {
-      std::snprintf(err, errlen, "switching function type '%s' (a lepton expression) is not available on the GPU",
-                    name.c_str());
-      return 2;
+      // leptonSwitch (SwitchingFunction.cpp:1138-1141)
+      if (!prog) {
+        std::snprintf(err, errlen, "switching function type '%s' is not available here", name.c_str());
+        return 2;
+      }
+      std::string func;
+      W.get_string("FUNC", &func);
+      char msg[512];
+      if (expr_compile(func.c_str(), prog, msg, sizeof msg)) {
+        std::snprintf(err, errlen, "%s", msg);
+        return 1;
+      }
+      data_init(sw, d0, dmax, r0);
+      sw->type = SW_CUSTOM;
+      sw->expr_host = prog;
     } else {
       std::snprintf(err, errlen, "cannot understand switching function type '%s'", name.c_str());
       return 1;

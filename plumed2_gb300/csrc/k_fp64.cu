@@ -76,6 +76,11 @@ void launch_apply_forces(const KArgs &a, bool mixed, int rank_order, const doubl
   }
 }
 
+void launch_nl_partition(const KArgs &a, cudaStream_t s) {
+  k_nl_partition<4><<<dim3((a.nslices + 7) / 8 > 0 ? (a.nslices + 7) / 8 : 1, a.nframes), 256, 0, s>>>(a);
+  g_launches += 1;
+}
+
 void launch_pair_flags(const KArgs &a, cudaStream_t s) {
   k_pair_flags<<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a);
   g_launches += 1;

@@ -60,24 +60,11 @@ static int nh_compiled(const SwitchParams &sw) {
 }
 
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
-                      int unroll, int compact, cudaStream_t s) {
+                      int unroll, cudaStream_t s) {
   // persistent: nblocks blocks over all frames, at least one per frame, at
   // most one per 8 slices of a frame (8 warps per block)
   const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
   const dim3 g(per_frame, a.nframes);
-  if (compact && mode != EVAL_PERATOM && mode != EVAL_VJP) {
-    if (unroll >= 4) {
-#define CALL(N, M) k_eval_nl32c<N, M, 4><<<g, 256, 0, s>>>(a, sw, s32)
-      NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
-#undef CALL
-    } else {
-#define CALL(N, M) k_eval_nl32c<N, M, 2><<<g, 256, 0, s>>>(a, sw, s32)
-      NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
-#undef CALL
-    }
-    g_launches += 1;
-    return;
-  }
   if (unroll >= 8) {
 #define CALL(N, M) k_eval_nl32<N, M, 8><<<g, 256, 0, s>>>(a, sw, s32)
     NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);

@@ -42,6 +42,17 @@ struct KArgs {
   uint32_t *ell;                // [nframes][nslices*cap*32]
   int *row_len;                 // [nframes][ns]
   int *slice_w;                 // [nframes][nslices]
+  // near/far rows (k_nl_partition): entries [0, row_near) of a row were
+  // within d_max + skin of the row atom at the rebuild, the rest beyond it
+  int *row_near;                // [nframes][ns] or null
+  int *slice_wn;                // [nframes][nslices] the slice's longest near part
+  uint32_t *ell_far;            // like ell: the partition's scratch for far entries
+  uint4 *q_build;               // [nframes][ns] fixed-point positions at the rebuild (rank order)
+  unsigned *disp2;              // [2][nframes] the largest squared displacement since the rebuild (FP32
+                                // bits, max over atoms) of this step, and of every step since the
+                                // rebuild; measured by the gather; or null
+  float near_r2;                // the partition's threshold: (d_max + skin)^2 (1 + 1e-5)
+  float disp_ok2;               // near parts suffice while disp2 <= (skin/2)^2 (1 - 1e-5); < 0: off
   unsigned long long *nl_count; // [nframes][4]: pairs, self pairs, max row length, geometry error
   uint32_t *self_pairs;         // [nframes][self_cap][2]
   unsigned char *pair_flag;     // [nframes][nA] PAIR-mode neighbour flags

@@ -165,6 +165,30 @@ __device__ __forceinline__ uint4 fixed_of_hi(const FrameConst &fc, const double 
 __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float scale) {
   return (float)(int)(b - a) * scale;  // wraps modulo 2^32: minimum image
 }
+// The largest d2 of the block's threads (valid ones) into *step and
+// *interval: warp maxima, a shared maximum, then one atomic pair per block
+// (unsigned bits of a non-negative float order like the floats).  Every
+// thread of the block calls it.  (Atomics per warp on the frame's one
+// address measured 50 % slower for the gather.)
+__device__ __forceinline__ void disp_max_block(unsigned *step, unsigned *interval, float d2, bool valid) {
+  __shared__ unsigned bmax;
+  if (threadIdx.x == 0) bmax = 0u;
+  __syncthreads();
+  const unsigned v = __reduce_max_sync(0xffffffffu, valid ? __float_as_uint(d2) : 0u);
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(&bmax, v);
+  __syncthreads();
+  if (threadIdx.x == 0 && bmax) {
+    atomicMax(step, bmax);
+    atomicMax(interval, bmax);
+  }
+}
+// Squared displacement since the rebuild of a rank whose new fixed-point
+// position is qq (wrapped: the minimum image in a periodic box).
+__device__ __forceinline__ float disp2_of(const FrameConst &fc, uint4 qb, uint4 qq) {
+  const float dx = fixed_delta(qb.x, qq.x, fc.scale[0]), dy = fixed_delta(qb.y, qq.y, fc.scale[1]),
+              dz = fixed_delta(qb.z, qq.z, fc.scale[2]);
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
 
 // ---------------------------------------------------------------------------
 // cells: binning, scan, scatter, per-cell ordering
@@ -439,11 +463,16 @@ __global__ void __launch_bounds__(kSlotBlock) k_prep_host(KArgs a, const double 
   stage_in3(sx, hpos + (fo + s0) * 3, nb);
   __syncthreads();
   const int t = threadIdx.x;
-  if (t >= nb) return;
-  const int s = s0 + t;
-  const double xx[3] = {sx[3 * t], sx[3 * t + 1], sx[3 * t + 2]};
-  const int r = rank_order ? a.rank_of_slot[fo + s] : s;
-  a.q[fo + r] = fixed_of(a.fc[f], xx);
+  float d2 = 0.f;
+  if (t < nb) {
+    const int s = s0 + t;
+    const double xx[3] = {sx[3 * t], sx[3 * t + 1], sx[3 * t + 2]};
+    const int r = rank_order ? a.rank_of_slot[fo + s] : s;
+    const uint4 qq = fixed_of(a.fc[f], xx);
+    a.q[fo + r] = qq;
+    if (a.disp2) d2 = disp2_of(a.fc[f], a.q_build[fo + r], qq);
+  }
+  if (a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.nframes + f, d2, t < nb);
 }
 __global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
   const int f = blockIdx.y + a.frame0;
@@ -509,10 +538,10 @@ __global__ void k_apply_box_forces(int nframes, const double *__restrict__ ff, c
 
 // FP64 positions in rank order (and the fixed-point copy for the NL prefilter
 // and the mixed kernels).  rank_order==0: slot order.
-__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
-  const int f = blockIdx.y;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.ns) return;
+// k_gather's work for rank r of frame f; returns the squared displacement
+// since the rebuild when it is measured (0 otherwise).
+__device__ __forceinline__ float gather_one(const KArgs &a, int f, int r, int rank_order, int want64, int wantq,
+                                            int wantcell) {
   const int s = rank_order ? a.slot_of_rank[(size_t)f * a.ns + r] : r;
   if (wantcell) a.cell_of_rank[(size_t)f * a.ns + r] = a.cell_of_slot[(size_t)f * a.ns + s];
   const double *x = a.pos + ((size_t)f * a.ns + s) * 3;
@@ -532,7 +561,89 @@ __global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wan
     }
     qq.w = __float_as_uint((float)gw);
     a.q[(size_t)f * a.ns + r] = qq;
+    if (a.disp2) return disp2_of(a.fc[f], a.q_build[(size_t)f * a.ns + r], qq);
   }
+  return 0.f;
+}
+
+__global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wantcell) {
+  const int f = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  float d2 = 0.f;
+  if (r < a.ns) d2 = gather_one(a, f, r, rank_order, want64, wantq, wantcell);
+  if (wantq && a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.nframes + f, d2, r < a.ns);
+}
+
+// Orders each row of a rebuilt list near part first: entries whose FP32
+// distance at the rebuild is within a.near_r2 (d_max + skin, squared, with a
+// margin), then the rest.  A warp streams its slice's rows in lock step, kU
+// entries and partner positions in flight per lane as in the pair pass: near
+// entries are written back compacted to the front of the row (never ahead of
+// what has been read), far ones to the row's column of a scratch list, and
+// the far entries then follow the near ones.  Records the near counts, the
+// slices' longest near parts, the rebuild positions, and zero displacements
+// (this step's and the interval's).  One warp per slice, one lane per row.
+template <int kU>
+__global__ void __launch_bounds__(256) k_nl_partition(KArgs a) {
+  const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31;
+  const int slice = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (slice >= a.nslices) return;  // warp-uniform
+  const size_t fo = (size_t)f * a.ns;
+  const FrameConst &fc = a.fc[f];
+  const int r = slice * 32 + lane;
+  const bool active = r < a.ns;
+  const size_t base = ((size_t)f * a.nslices + slice) * (size_t)a.cap * 32 + lane;
+  uint32_t *row = a.ell + base, *far = a.ell_far + base;
+  const int len = active ? a.row_len[fo + r] : 0;
+  const int w = a.slice_w[(size_t)f * a.nslices + slice];
+  const uint4 qr = active ? a.q[fo + r] : make_uint4(0u, 0u, 0u, 0u);
+  if (active) a.q_build[fo + r] = qr;
+  int nn = 0, nf = 0;
+  for (int k = 0; k < w; k += kU) {
+    uint32_t e[kU];
+    uint4 qp[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) e[u] = (k + u < len) ? row[(size_t)(k + u) * 32] : 0xffffffffu;
+#pragma unroll
+    for (int u = 0; u < kU; u++) qp[u] = (e[u] != 0xffffffffu) ? a.q[fo + (e[u] & kRankMask)] : qr;
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (e[u] == 0xffffffffu) continue;
+      const float dx = fixed_delta(qr.x, qp[u].x, fc.scale[0]), dy = fixed_delta(qr.y, qp[u].y, fc.scale[1]),
+                  dz = fixed_delta(qr.z, qp[u].z, fc.scale[2]);
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= a.near_r2)
+        row[(size_t)(nn++) * 32] = e[u];
+      else
+        far[(size_t)(nf++) * 32] = e[u];
+    }
+  }
+  // the far entries after the near ones, four loads in flight
+  for (int i = 0; i < nf; i += 4) {
+    uint32_t t[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) t[u] = (i + u < nf) ? far[(size_t)(i + u) * 32] : 0u;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (i + u < nf) row[(size_t)(nn + i + u) * 32] = t[u];
+  }
+  if (active) a.row_near[fo + r] = nn;
+  const int wmax = warp_max(nn);
+  if (lane == 0) {
+    a.slice_wn[(size_t)f * a.nslices + slice] = wmax;
+    if (slice == 0) {
+      a.disp2[f] = 0u;
+      a.disp2[a.nframes + f] = 0u;
+    }
+  }
+}
+
+// Whether frame f's rows may be read up to their near parts: the skin is on
+// and every atom has moved less than half of it since the rebuild, so an
+// entry of a far part (beyond d_max + skin then) lies beyond d_max now,
+// where every switching function is exactly zero.
+__device__ __forceinline__ bool near_rows_only(const KArgs &a, int f) {
+  return a.row_near != nullptr && a.disp_ok2 >= 0.f && __uint_as_float(a.disp2[f]) <= a.disp_ok2;
 }
 
 // ---------------------------------------------------------------------------

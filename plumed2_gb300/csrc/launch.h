@@ -26,6 +26,8 @@ void launch_apply_forces(const KArgs &a, bool mixed, int rank_order, const doubl
 void launch_prep_host(const KArgs &a, const double *hpos, int rank_order, cudaStream_t s);
 void launch_finalize_host32(const KArgs &a, double *hderiv, int rank_order, cudaStream_t s);
 void launch_nl_build(const KArgs &a, bool classic, cudaStream_t s);
+// near part first in every row of a rebuilt list (k_nl_partition)
+void launch_nl_partition(const KArgs &a, cudaStream_t s);
 void launch_pair_flags(const KArgs &a, cudaStream_t s);
 void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s);
 // prefilter: the FP32 parameters of the switch, for the fixed-point screen of
@@ -41,10 +43,8 @@ void launch_grad_post(const KArgs &a, const double *vir, const double *dpar, dou
 // FP64 decision of d_max for the pairs the mixed NL pass left in the band
 // around d_max^2 (after launch_eval_nl32, before the finalize kernel)
 void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s);
-// compact: the queue-compacted kernel (k_eval_nl32c) for the modes s,
-// derivatives and parameters; otherwise k_eval_nl32
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
-                      int unroll, int compact, cudaStream_t s);
+                      int unroll, cudaStream_t s);
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s);
 void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,

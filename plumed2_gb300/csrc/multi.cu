@@ -461,7 +461,7 @@ int coord_multi_create(coord_ctx *const *ctxs, int n_actions, int64_t n_atoms, c
   for (int k = 0; k < n_actions; k++) {
     const MultiView &v = m->views[k];
     const bool fuse = v.p->nlist == COORD_NL_NONE && v.p->precision == COORD_PREC_MIXED && v.mode != MODE_PAIR &&
-                      !v.p->nopbc && v.ns > 0;
+                      !v.p->nopbc && v.ns > 0 && v.sw->type != SW_CUSTOM;
     if (!fuse) {
       m->others.push_back(k);
       continue;

@@ -20,8 +20,12 @@
 
 #ifdef __CUDACC__
 #define SW_HD __host__ __device__ __forceinline__
+// called, not inlined: the expression interpreter would otherwise be copied
+// into every kernel that can meet a CUSTOM switch (compile time, registers)
+#define SW_HD_CALL static __host__ __device__ __noinline__
 #else
 #define SW_HD inline
+#define SW_HD_CALL static
 #endif
 
 namespace coordgpu {
@@ -169,6 +173,142 @@ template <typename T> SW_HD VD<T> sw_function(const SwitchParams &s, T rdist) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// CUSTOM: the compiled expression run forward on (value, derivative) pairs,
+// with lepton's operations and their derivatives (src/lepton/Operation.h and
+// Operation.cpp: step differentiates to delta without the chain factor, abs
+// to 2 step - 1, min and max through step(a - b), select through its
+// branches; a constant integer power by repeated squaring as
+// PowerConstant::evaluate).  FP64 in every path.
+// ---------------------------------------------------------------------------
+SW_HD double expr_powc(double a, double c) {
+  const int ic = (int)c;
+  if ((double)ic != c) return pow(a, c);
+  int n = ic < 0 ? -ic : ic;
+  double base = ic < 0 ? 1.0 / a : a, r = 1.0;
+  for (; n != 0; n >>= 1) {
+    if (n & 1) r *= base;
+    base *= base;
+  }
+  return r;
+}
+
+SW_HD_CALL VD<double> expr_run(const ExprProgram &p, double var) {
+  double v[kExprMaxStack], d[kExprMaxStack];
+  int sp = 0;
+  const double two_over_sqrtpi = 1.1283791670955126;  // 2/sqrt(pi)
+  for (int i = 0; i < p.n; i++) {
+    const int op = p.op[i];
+    if (op == EX_VAR || op == EX_CONST) {
+      v[sp] = op == EX_VAR ? var : p.cst[i];
+      d[sp] = op == EX_VAR ? 1.0 : 0.0;
+      sp++;
+      continue;
+    }
+    if (op == EX_SELECT) {  // select(c, a, b)
+      const bool t = v[sp - 3] != 0.0;
+      v[sp - 3] = t ? v[sp - 2] : v[sp - 1];
+      d[sp - 3] = t ? d[sp - 2] : d[sp - 1];
+      sp -= 2;
+      continue;
+    }
+    if (op >= EX_ADD && op <= EX_POW || op >= EX_ATAN2) {  // two arguments
+      const double x = v[sp - 2], dx = d[sp - 2], y = v[sp - 1], dy = d[sp - 1];
+      double r, dr;
+      switch (op) {
+      case EX_ADD: r = x + y; dr = dx + dy; break;
+      case EX_SUB: r = x - y; dr = dx - dy; break;
+      case EX_MUL: r = x * y; dr = dx * y + x * dy; break;
+      case EX_DIV: r = x / y; dr = dx / y - x * dy / (y * y); break;
+      case EX_POW: r = pow(x, y); dr = y * pow(x, y - 1.0) * dx + log(x) * r * dy; break;
+      case EX_ATAN2: r = atan2(x, y); dr = (y * dx - x * dy) / (x * x + y * y); break;
+      case EX_MIN: r = (y < x) ? y : x; dr = (x - y >= 0.0) ? dy : dx; break;
+      default: r = (x < y) ? y : x; dr = (x - y >= 0.0) ? dx : dy; break;  // EX_MAX
+      }
+      sp--;
+      v[sp - 1] = r;
+      d[sp - 1] = dr;
+      continue;
+    }
+    const double x = v[sp - 1], dx = d[sp - 1];
+    double r = 0.0, dr = 0.0;
+    switch (op) {
+    case EX_POWC: r = expr_powc(x, p.cst[i]); dr = p.cst[i] * expr_powc(x, p.cst[i] - 1.0) * dx; break;
+    case EX_NEG: r = -x; dr = -dx; break;
+    case EX_SQRT: r = sqrt(x); dr = 0.5 * (1.0 / r) * dx; break;
+    case EX_EXP: r = exp(x); dr = r * dx; break;
+    case EX_LOG: r = log(x); dr = (1.0 / x) * dx; break;
+    case EX_SIN: r = sin(x); dr = cos(x) * dx; break;
+    case EX_COS: r = cos(x); dr = -sin(x) * dx; break;
+    case EX_SEC: r = 1.0 / cos(x); dr = r * tan(x) * dx; break;
+    case EX_CSC: r = 1.0 / sin(x); dr = -r * (1.0 / tan(x)) * dx; break;
+    case EX_TAN: { const double sc = 1.0 / cos(x); r = tan(x); dr = sc * sc * dx; break; }
+    case EX_COT: { const double sc = 1.0 / sin(x); r = 1.0 / tan(x); dr = -sc * sc * dx; break; }
+    case EX_ASIN: r = asin(x); dr = 1.0 / sqrt(1.0 - x * x) * dx; break;
+    case EX_ACOS: r = acos(x); dr = -1.0 / sqrt(1.0 - x * x) * dx; break;
+    case EX_ATAN: r = atan(x); dr = 1.0 / (1.0 + x * x) * dx; break;
+    case EX_SINH: r = sinh(x); dr = cosh(x) * dx; break;
+    case EX_COSH: r = cosh(x); dr = sinh(x) * dx; break;
+    case EX_TANH: r = tanh(x); dr = (1.0 - r * r) * dx; break;
+    case EX_ERF: r = erf(x); dr = two_over_sqrtpi * exp(-x * x) * dx; break;
+    case EX_ERFC: r = erfc(x); dr = -two_over_sqrtpi * exp(-x * x) * dx; break;
+    case EX_STEP: r = (x >= 0.0) ? 1.0 : 0.0; dr = (x == 0.0) ? INFINITY : 0.0; break;
+    case EX_DELTA: r = (x == 0.0) ? INFINITY : 0.0; dr = (x == 0.0) ? NAN : 0.0; break;
+    case EX_SQUARE: r = x * x; dr = 2.0 * x * dx; break;
+    case EX_CUBE: r = x * x * x; dr = 3.0 * (x * x) * dx; break;
+    case EX_RECIP: r = 1.0 / x; dr = -(1.0 / (x * x)) * dx; break;
+    case EX_ABS: r = fabs(x); dr = (dx == 0.0) ? 0.0 : dx * (2.0 * ((x >= 0.0) ? 1.0 : 0.0) - 1.0); break;
+    case EX_FLOOR: r = floor(x); break;
+    case EX_CEIL: r = ceil(x); break;
+    default: break;
+    }
+    v[sp - 1] = r;
+    d[sp - 1] = dr;
+  }
+  return sp ? VD<double>{v[sp - 1], d[sp - 1]} : VD<double>{0.0, 0.0};
+}
+
+SW_HD const ExprProgram &expr_of(const SwitchParams &s) {
+#ifdef __CUDA_ARCH__
+  return *s.expr_dev;
+#else
+  return *s.expr_host;
+#endif
+}
+
+// leptonSwitch::calculate and calculateSqr (SwitchingFunction.cpp:709-751)
+// for a distance r or its square r2 (from_sqr).  With x2 the expression takes
+// r^2 / r0^2 (D_0 does not enter); with x it takes (r - d0) / r0 and is 1
+// (stretched) for x <= 0.
+SW_HD_CALL VD<double> custom_eval(const SwitchParams &s, double r, double r2, bool from_sqr) {
+  const ExprProgram &p = expr_of(s);
+  VD<double> out{0.0, 0.0};
+  if (p.var_x2) {
+    const double distance2 = from_sqr ? r2 : r * r;
+    if (distance2 <= s.dmax_2) {
+      const double rdist_2 = distance2 * s.invr0_2;
+      out = expr_run(p, rdist_2);
+      out.d *= 2 * s.invr0_2;
+      out.f = out.f * s.stretch + s.shift;
+      out.d *= s.stretch;
+    }
+    return out;
+  }
+  const double distance = from_sqr ? sqrt(r2) : r;
+  if (distance <= s.dmax) {
+    out.f = 1.0;
+    const double rdist = (distance - s.d0) * s.invr0;
+    if (rdist > 0.0) {
+      out = expr_run(p, rdist);
+      out.d *= s.invr0;
+      out.d /= distance;
+    }
+    out.f = out.f * s.stretch + s.shift;
+    out.d *= s.stretch;
+  }
+  return out;
+}
+
 // nativeqSwitch::calculate (:527-555)
 template <typename T> SW_HD VD<T> nativeq_calculate(const SwitchParams &s, T distance) {
   T res = T(0.0), dfunc = T(0.0);
@@ -189,6 +329,10 @@ template <typename T> SW_HD VD<T> nativeq_calculate(const SwitchParams &s, T dis
 // baseSwitch::calculate + applystretch
 template <typename T> SW_HD VD<T> sw_calculate(const SwitchParams &s, T distance) {
   if (s.type == SW_Q) return nativeq_calculate<T>(s, distance);
+  if (s.type == SW_CUSTOM) {
+    const VD<double> r = custom_eval(s, (double)distance, 0.0, false);
+    return VD<T>{T(r.f), T(r.d)};
+  }
   const T rdist = (distance - T(s.d0)) * T(s.invr0);
   if (distance > T(s.dmax)) return VD<T>{T(0.0), T(0.0)};
   if (rdist > T(0.0)) {
@@ -206,6 +350,10 @@ template <typename T> SW_HD VD<T> sw_calculate(const SwitchParams &s, T distance
 template <typename T> SW_HD VD<T> sw_calculate_sqr(const SwitchParams &s, T distance2) {
   VD<T> r{T(0.0), T(0.0)};
   switch (s.type) {
+  case SW_CUSTOM: {
+    const VD<double> c = custom_eval(s, 0.0, (double)distance2, true);
+    return VD<T>{T(c.f), T(c.d)};
+  }
   case SW_RATFIX:
     if (distance2 <= T(s.dmax_2)) {
       const T rdist = distance2 * T(s.invr0_2);

@@ -60,11 +60,17 @@ def test_keyword_errors(line, msg):
         Coordination(line)
 
 
-def test_custom_switch_is_reported_unsupported():
-    from plumed2_gb300 import CoordError
+def test_custom_switch_errors():
+    """CUSTOM (lepton) expressions the reference refuses are refused with its
+    messages (leptonSwitch::funcAndDeriv, SwitchingFunction.cpp:566-585);
+    lepton's parse errors are reported as such."""
     from plumed2_gb300.action import Coordination
-    with pytest.raises(CoordError, match="lepton"):
-        Coordination("GROUPA=1-10 SWITCH={CUSTOM FUNC=1/(1+x^6) R_0=1}")
+    Coordination("GROUPA=1-10 SWITCH={CUSTOM FUNC=1/(1+x^6) R_0=1}").close()
+    Coordination("GROUPA=1-10 SWITCH={CUSTOM FUNC={1 / (1 + x2^3)} R_0=1}").close()
+    for func, msg in (("x*x2", "only ONE argument"), ("y+x", "only ONE argument"), ("foo(x)", "unknown function"),
+                      ("(1+x", "unbalanced"), ("1/(1+x^6))", "unexpected")):
+        with pytest.raises(ValueError, match=re.escape(msg)):
+            Coordination("GROUPA=1-10 SWITCH={CUSTOM FUNC=%s R_0=1}" % func)
 
 
 def test_atom_list_parsing():

@@ -148,6 +148,46 @@ def test_nlist_pairs_crossing_dmax_between_rebuilds(orc, prec, mode, pbc):
         pos = pos + rng.normal(0, 0.04, pos.shape)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["NLIST", "NLISTCELLS"])
+@pytest.mark.parametrize("mode", ["single", "two"])
+def test_near_and_far_rows_over_a_trajectory(orc, prec, kind, mode):
+    """Lists of orthorhombic periodic frames are split at each rebuild into a
+    near part (within D_MAX + skin) and a far part; while every atom has
+    moved less than half the skin since the rebuild only the near parts are
+    read.  A trajectory of small steps (0.002 nm per coordinate) over three
+    NL_STRIDE=10 intervals, with one kick of 0.08 nm at step 14 that moves
+    atoms past half the skin (the far parts are read again until the next
+    rebuild), and a box that changes at step 23 (no near parts until the
+    next rebuild).  Every step follows the oracle on the last rebuild's
+    list."""
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.6"
+    n, a0 = 4096, 0.31
+    L = 16 * a0
+    if mode == "single":
+        line, m, n0, n1 = "GROUPA=1-4096", 0, n, 0
+    else:
+        line, m, n0, n1 = "GROUPA=1-2048 GROUPB=2049-4096", 1, 2048, 2048
+    c = Coordination("%s SWITCH={%s} %s NL_CUTOFF=0.8 NL_STRIDE=10" % (line, spec, kind), precision=prec)
+    rng = np.random.default_rng(21)
+    pos = jittered_lattice(n, a0, 0.03, 9)
+    nl_ref = None
+    for step in range(30):
+        box = np.diag([L] * 3) if step < 23 else np.diag([L * 1.001] * 3)
+        if step % 10 == 0:
+            if kind == "NLIST":
+                nl_ref = orc.nl_classic_cells(m, n0, n1, pos, box, True, 0.8)
+            else:
+                nl_ref = orc.nl_linkcells(m, n0, n1, pos, box, True, 0.8)
+        got = c.calculate(pos, box, step)
+        if step % 10 == 0:
+            assert np.array_equal(_sorted(c.pairs()), _sorted(nl_ref)), step
+        ref = orc.coordination(spec, pos, box, nl_ref)
+        _check(prec, got, ref, "step %d" % step)
+        pos = pos + rng.normal(0, 0.08 if step == 14 else 0.002, pos.shape)
+
+
 @pytest.mark.parametrize("mode", ["single", "two"])
 @pytest.mark.parametrize("pbc", [True, False])
 def test_nlistcells_pair_set(orc, mode, pbc):

@@ -194,3 +194,24 @@ def test_coordination_custom_switch(orc, ref):
             assert abs(s1 - s2) <= 1e-13 * abs(s2)
             assert np.abs(d1 - d2).max() <= 1e-12 * np.abs(d2).max()
             assert np.abs(v1 - v2).max() <= 1e-12 * np.abs(v2).max()
+
+
+@pytest.mark.parametrize("func", CUSTOM_FUNCS)
+def test_library_custom_switch_host_values(orc, ref, func):
+    """The library's own CUSTOM compiler and evaluator (host side, the code the
+    kernels run) against the reference's leptonSwitch and the oracle, both
+    calculate and calculateSqr, across and beyond D_MAX: within 1e-12
+    relative (the reference differentiates symbolically and simplifies)."""
+    from plumed2_gb300.action import Coordination
+    x = np.concatenate([np.linspace(0.01, 3.0, 300), [0.1, 0.2, 1.0]])
+    for extra in ("R_0=0.7", "R_0=1.1 D_0=0.2", "R_0=0.9 D_MAX=2.5", "R_0=0.5 D_0=0.1 D_MAX=1.9 NOSTRETCH"):
+        spec = "CUSTOM FUNC=%s %s" % (func, extra)
+        c = Coordination("GROUPA=1-2 SWITCH={%s}" % spec)
+        for squared in (True, False):
+            xx = x * x if squared else x
+            f, d = c.switch(xx, squared)
+            fr, dr = ref.switch_eval(spec, xx, squared)
+            fo, do = orc.switch_eval(spec, xx, squared)
+            assert _close(f, fr, 1e-12) and _close(d, dr, 1e-12), (spec, squared)
+            assert _close(f, fo, 1e-12) and _close(d, do, 1e-12), (spec, squared)
+        c.close()
