@@ -25,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "k_fp64.cu": ["-fmad=false"],
     "k_mixed.cu": [],
+    "k_mixed_tric.cu": [],
     "coord_api.cu": [],
     "multi.cu": [],
     "peaks.cu": [],

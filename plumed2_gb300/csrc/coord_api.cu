@@ -109,6 +109,9 @@ struct coord_ctx {
   double skin = 0.0;
   std::vector<double> skin_boxes;
   HostBuf<unsigned> h_disp2;
+  // the D_MAX band of the last frames uploaded when they have generic boxes
+  // on the mixed path (tric_band_of), else 0
+  double tric_band = 0.0;
   int cap = 0, self_cap = 64, ncell_cap = 0, max_blocks = 0;
   int nframes_alloc = 0;
   // device buffers
@@ -250,9 +253,44 @@ int frame_setup(coord_ctx *c, const double *box, FrameConst *fc, bool *need_boun
     fc->cut2_lo = -1.0f;  // finished on the device (span known there)
     fc->cut2_hi = -1.0f;
   } else {
-    fc->fixed_ok = 0;  // generic box
+    fc->fixed_ok = 0;  // generic box: the exact search, no fixed-point prefilter
+    if (c->p.precision == COORD_PREC_MIXED) {
+      fc->tric = 1;
+      for (int k = 0; k < 9; k++) {
+        fc->fx_m[k] = fc->pbc.invreduced[k] * 4294967296.0;
+        fc->red32[k] = (float)(fc->pbc.reduced[k] / 4294967296.0);
+      }
+    }
   }
   return COORD_OK;
+}
+
+// Relative half-width of the band around d_max^2 inside which the FP32 r^2
+// of a generic-box frame cannot decide the reference's test (Geo32<true>).
+// With s = d invReduced and A_i = sum_j |s_j| |R_ji| <= kappa |d|
+// (kappa = max_i sum_j |R_ji| |column j of invReduced|): the wrapped
+// integer differences as floats and the three FMAs per component are each
+// within 2^-24 of A_i, and one fixed-point unit of either position adds
+// 2^-32 sum_j |R_ji|; r^2 = |d|^2 then errs by at most
+// (10 sqrt(3) kappa + 3) 2^-24 r^2 plus twice the unit term over d_max.
+// Doubled, and never below the orthorhombic band (2e-6).
+double tric_band_of(const PbcParams &pbc, double dmax) {
+  double kappa = 0.0, unit = 0.0;
+  for (int i = 0; i < 3; i++) {
+    double ki = 0.0, ui = 0.0;
+    for (int j = 0; j < 3; j++) {
+      const double cj = std::sqrt(pbc.invreduced[0 * 3 + j] * pbc.invreduced[0 * 3 + j] +
+                                  pbc.invreduced[1 * 3 + j] * pbc.invreduced[1 * 3 + j] +
+                                  pbc.invreduced[2 * 3 + j] * pbc.invreduced[2 * 3 + j]);
+      ki += std::fabs(pbc.reduced[j * 3 + i]) * cj;
+      ui += std::fabs(pbc.reduced[j * 3 + i]);
+    }
+    kappa = std::max(kappa, ki);
+    unit = std::max(unit, ui);
+  }
+  const double rel = (10.0 * std::sqrt(3.0) * kappa + 3.0) / 16777216.0 +
+                     (std::isfinite(dmax) && dmax > 0 ? 2.0 * std::sqrt(3.0) * unit / 4294967296.0 / dmax : 0.0);
+  return std::max(2e-6, 2.0 * rel);
 }
 
 int ensure_buffers(coord_ctx *c, int n_frames) {
@@ -320,6 +358,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.flags = (int)flags;
   a.has_dup = c->has_dup ? 1 : 0;
   a.fc = c->fc.p;
+  a.tric_band = (float)c->tric_band;
   a.abs_of_slot = c->abs_of_slot.p;
   a.pos = d_pos;
   a.accw64 = c->accw64.p;
@@ -419,6 +458,12 @@ int set_tuning_defaults(coord_ctx *c) {
 
 int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bounds_any) {
   *need_bounds_any = false;
+  double tric_band = 0.0;
+  struct SetBand {  // on every return: the band of the frames set up so far
+    coord_ctx *c;
+    double &b;
+    ~SetBand() { c->tric_band = b; }
+  } set_band{c, tric_band};
   bool changed = (int)c->fc_uploaded.size() != n_frames;
   c->fc_uploaded.resize(n_frames);
   for (int f = 0; f < n_frames; f++) {
@@ -428,9 +473,7 @@ int upload_frames(coord_ctx *c, int n_frames, const double *boxes, bool *need_bo
     *need_bounds_any = *need_bounds_any || nb;
     if (std::memcmp(&fcs, &c->fc_uploaded[f], sizeof fcs) != 0) changed = true;
     c->fc_uploaded[f] = fcs;
-    if (fcs.pbc.type == PBC_GENERIC && !c->p.nopbc && c->p.precision == COORD_PREC_MIXED)
-      return c->fail(COORD_ERR_UNSUPPORTED, "the mixed-precision path needs an orthorhombic box (or NOPBC); "
-                                            "use the FP64 path for triclinic boxes");
+    if (fcs.tric) tric_band = std::max(tric_band, tric_band_of(fcs.pbc, std::sqrt(c->sw.dmax_2)));
     if (fcs.grid.ncells > c->ncell_cap) return COORD_ERR_STATE;  // caller grows ncell_cap
   }
   if (changed || *need_bounds_any) {

@@ -124,6 +124,15 @@ struct FrameConst {
   // the same q in one FMA: q = rn(x * fx_s + fx_c) mod 2^32 with
   // fx_s = inv_l * 2^32 and fx_c = -grid.lo * fx_s (fixed_frame_finish)
   double fx_s[3], fx_c[3];
+  // generic (triclinic) periodic box on the mixed path: q holds the
+  // fractional coordinates in the reduced lattice, component i =
+  // frac(sum_j x_j invReduced(j,i)) * 2^32 (fx_m = invReduced * 2^32), so
+  // the wrapped difference of two q is Pbc::distance's Tools::pbc of the
+  // scaled distance; red32 = reduced / 2^32 takes it back to Cartesian in
+  // FP32 (Pbc.cpp:383-415)
+  int    tric;
+  double fx_m[9];
+  float  red32[9];
 };
 
 #ifdef __CUDACC__

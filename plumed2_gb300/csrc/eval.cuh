@@ -410,11 +410,45 @@ struct Acc32 {
 // (a stretched switch is zero at d_max but its derivative is not, so the
 // decision must match).  x1 is the reference's first atom; every operation is
 // an explicitly rounded intrinsic, so no contraction changes the result.
-// Orthorhombic box or none (the mixed path's frames).
+// Generic boxes: Pbc::distance's reduced-lattice branch (Pbc.cpp:392-413),
+// each matmul summed j = 0, 1, 2 from zero as Vector.h's matmul does.
+__device__ __noinline__ void pbc_generic_rn(const PbcParams *pbc, double d[3]) {
+  double sc[3];
+  for (int i = 0; i < 3; i++) {
+    double acc = 0.0;
+    for (int j = 0; j < 3; j++) acc = __dadd_rn(acc, __dmul_rn(d[j], pbc->invreduced[j * 3 + i]));
+    const double x = __dadd_rn(acc, 100.0);  // Tools::pbc (Tools.h:557-563)
+    const double t = (x >= 0) ? (double)__double2int_rz(__dadd_rn(x, 0.5)) : (double)__double2int_rz(__dsub_rn(x, 0.5));
+    sc[i] = __dsub_rn(x, t);
+  }
+  for (int i = 0; i < 3; i++) {
+    double acc = 0.0;
+    for (int j = 0; j < 3; j++) acc = __dadd_rn(acc, __dmul_rn(sc[j], pbc->reduced[j * 3 + i]));
+    d[i] = acc;
+  }
+  if (__dadd_rn(__dadd_rn(fabs(sc[0]), fabs(sc[1])), fabs(sc[2])) > 0.5) {
+    const int o = 4 * (sc[0] > 0 ? 1 : 0) + 2 * (sc[1] > 0 ? 1 : 0) + (sc[2] > 0 ? 1 : 0);
+    double best[3] = {d[0], d[1], d[2]};
+    double lbest = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+    for (int i = 0; i < pbc->nshift[o]; i++) {
+      double t[3];
+      for (int k = 0; k < 3; k++) t[k] = __dadd_rn(d[k], pbc->shift[o][i][k]);
+      const double l = __dadd_rn(__dadd_rn(__dmul_rn(t[0], t[0]), __dmul_rn(t[1], t[1])), __dmul_rn(t[2], t[2]));
+      if (l < lbest) {
+        lbest = l;
+        best[0] = t[0];
+        best[1] = t[1];
+        best[2] = t[2];
+      }
+    }
+    for (int k = 0; k < 3; k++) d[k] = best[k];
+  }
+}
 __device__ __forceinline__ bool dmax_exact(const double *x1, const double *x2, const PbcParams *pbc, int do_pbc,
                                         double dmax_2) {
   double d[3];
   for (int k = 0; k < 3; k++) d[k] = __dsub_rn(x2[k], x1[k]);
+  if (do_pbc && pbc->type == PBC_GENERIC) pbc_generic_rn(pbc, d);
   if (do_pbc && pbc->type == PBC_ORTHO) {
     for (int k = 0; k < 3; k++) {
       // Tools::pbc (Tools.h:557-563) of d * invBox(k,k), times box(k,k)
@@ -427,6 +461,65 @@ __device__ __forceinline__ bool dmax_exact(const double *x1, const double *x2, c
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
   return r2 <= dmax_2;
 }
+
+// FP32 displacement x_b - x_a of two fixed-point positions under the frame's
+// periodic boundary conditions (the mixed path's pair geometry).
+// Orthorhombic (or no) box: the wrapped difference per axis times L / 2^32.
+// Generic box: the wrapped differences are the reduced scaled distance after
+// Tools::pbc; Pbc::distance takes it back through the reduced cell and, when
+// |s0| + |s1| + |s2| > 0.5, tries the shifts of the octant for a shorter
+// image (Pbc.cpp:392-413), here in FP32 (the shift test compares the
+// fixed-point sum with 2^31).
+__device__ __noinline__ void tric_shift32(const FrameConst *fc, float t0, float t1, float t2, float *d) {
+  const int o = 4 * (t0 > 0.f ? 1 : 0) + 2 * (t1 > 0.f ? 1 : 0) + (t2 > 0.f ? 1 : 0);
+  float b0 = d[0], b1 = d[1], b2 = d[2];
+  float lb = fmaf(b0, b0, fmaf(b1, b1, b2 * b2));
+  for (int i = 0; i < fc->pbc.nshift[o]; i++) {
+    const float x = d[0] + (float)fc->pbc.shift[o][i][0], y = d[1] + (float)fc->pbc.shift[o][i][1],
+                z = d[2] + (float)fc->pbc.shift[o][i][2];
+    const float l = fmaf(x, x, fmaf(y, y, z * z));
+    if (l < lb) {
+      lb = l;
+      b0 = x;
+      b1 = y;
+      b2 = z;
+    }
+  }
+  d[0] = b0;
+  d[1] = b1;
+  d[2] = b2;
+}
+template <bool TRIC> struct Geo32 {
+  float sx, sy, sz;
+  __device__ __forceinline__ explicit Geo32(const FrameConst &fc)
+      : sx(fc.scale[0]), sy(fc.scale[1]), sz(fc.scale[2]) {}
+  __device__ __forceinline__ void delta(const uint4 &a, const uint4 &b, float &dx, float &dy, float &dz) const {
+    dx = fixed_delta(a.x, b.x, sx);
+    dy = fixed_delta(a.y, b.y, sy);
+    dz = fixed_delta(a.z, b.z, sz);
+  }
+};
+template <> struct Geo32<true> {
+  const FrameConst *fc;
+  float m[9];
+  __device__ __forceinline__ explicit Geo32(const FrameConst &f) : fc(&f) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) m[k] = f.red32[k];
+  }
+  __device__ __forceinline__ void delta(const uint4 &a, const uint4 &b, float &dx, float &dy, float &dz) const {
+    const float t0 = (float)(int)(b.x - a.x), t1 = (float)(int)(b.y - a.y), t2 = (float)(int)(b.z - a.z);
+    dx = fmaf(t0, m[0], fmaf(t1, m[3], t2 * m[6]));
+    dy = fmaf(t0, m[1], fmaf(t1, m[4], t2 * m[7]));
+    dz = fmaf(t0, m[2], fmaf(t1, m[5], t2 * m[8]));
+    if (fabsf(t0) + fabsf(t1) + fabsf(t2) > 2147483648.0f) {
+      float d[3] = {dx, dy, dz};
+      tric_shift32(fc, t0, t1, t2, d);
+      dx = d[0];
+      dy = d[1];
+      dz = d[2];
+    }
+  }
+};
 
 // Asks the TMA engine to bring [p, p + bytes) into L2 (no registers, no
 // completion to wait for); p 16-byte aligned, bytes a multiple of 16.
@@ -456,7 +549,7 @@ __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)
 // block barrier costs more than the locality gains.)
 // (four resident blocks of 256 threads per SM: a 64-register budget, which
 // the latency of the partner gathers needs more than registers)
-template <int NH, int MODE, int kUnroll>
+template <int NH, int MODE, int kUnroll, bool TRIC = false>
 __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31;
@@ -473,8 +566,7 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
   __syncwarp();
   const int nw = gridDim.x * wpb;
   const size_t fo = (size_t)f * a.ns;
-  const FrameConst &fc = a.fc[f];
-  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const Geo32<TRIC> geo(a.fc[f]);
   const uint4 *__restrict__ q = a.q + fo;
   float4 *__restrict__ acc4 = a.acc32 + fo;
   Acc32 acc;
@@ -553,9 +645,8 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
       for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
 #pragma unroll
       for (int u = 0; u < kUnroll; u++) {
-        const float dx = fixed_delta(qr.x, qp[u].x, sx);
-        const float dy = fixed_delta(qr.y, qp[u].y, sy);
-        const float dz = fixed_delta(qr.z, qp[u].z, sz);
+        float dx, dy, dz;
+        geo.delta(qr, qp[u], dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         if (p[u] >= 0 && r2 <= s32.dmax2_lo)
           pair(p[u], dx, dy, dz, r2, qp[u].w);
@@ -595,13 +686,13 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
 // slice order to the frame's results and clears the flags, so the outcome
 // does not depend on timing.  With no flagged slice this is a scan of one
 // byte per slice.
-template <int NH, int MODE>
+template <int NH, int MODE, bool TRIC = false>
 __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];
-  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const Geo32<TRIC> geo(fc);
   const uint4 *__restrict__ q = a.q + fo;
   float4 *__restrict__ acc4 = a.acc32 + fo;
   unsigned char *flag = a.band_flag + (size_t)f * band_stride(a);
@@ -631,8 +722,8 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
       for (int u = 0; u < kU; u++) qq[u] = (en[u] != 0xffffffffu) ? q[en[u] & kRankMask] : qr;
 #pragma unroll
       for (int u = 0; u < kU; u++) {
-        const float dx = fixed_delta(qr.x, qq[u].x, sx), dy = fixed_delta(qr.y, qq[u].y, sy),
-                    dz = fixed_delta(qr.z, qq[u].z, sz);
+        float dx, dy, dz;
+        geo.delta(qr, qq[u], dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         if ((__float_as_uint(r2) - band_lo) >= band_w) continue;  // dead entries: r2 = 0, never in the band
         const int p = (int)(en[u] & kRankMask);
@@ -818,7 +909,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs64(KArgs a, SwitchParams sw, i
   block_partials_finish(a, f, part, gridDim.x);
 }
 
-template <int TILE, int NH, int MODE>
+template <int TILE, int NH, int MODE, bool TRIC = false>
 __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int nTi, int nTj,
                                                      int ntp) {
   const int f = blockIdx.z;
@@ -826,7 +917,7 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
   const int iend = tri ? a.ns : a.nA, jbase0 = tri ? 0 : a.nA, jend = a.ns;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];
-  const float sx = fc.scale[0], sy = fc.scale[1], sz = fc.scale[2];
+  const Geo32<TRIC> geo(fc);
   __shared__ uint4 qj[TILE];
   __shared__ float accj[TILE][3];
   __shared__ long long absj[TILE];
@@ -856,8 +947,8 @@ __global__ void __launch_bounds__(TILE) k_allpairs32(KArgs a, SwitchParams sw, S
         const int j = jb + jl;
         if (j >= jend || (diag && jl <= (int)threadIdx.x) || absj[jl] == absi) continue;
         const uint4 qp = qj[jl];
-        const float dx = fixed_delta(qi.x, qp.x, sx), dy = fixed_delta(qi.y, qp.y, sy),
-                    dz = fixed_delta(qi.z, qp.z, sz);
+        float dx, dy, dz;
+        geo.delta(qi, qp, dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         bool in = r2 <= s32.dmax2_lo;
         if (!in && r2 <= s32.dmax2_hi)  // band: slot i is the reference's first atom
@@ -925,7 +1016,8 @@ template <int MODE> __global__ void k_pairs64(KArgs a, SwitchParams sw, int use_
   block_partials_finish(a, f, part, gridDim.x);
 }
 
-template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int use_flags) {
+template <int NH, int MODE, bool TRIC = false>
+__global__ void k_pairs32(KArgs a, SwitchParams sw, SwitchF32 s32, int use_flags) {
   const int f = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const size_t fo = (size_t)f * a.ns;
@@ -933,8 +1025,8 @@ template <int NH, int MODE> __global__ void k_pairs32(KArgs a, SwitchParams sw, 
   if (i < a.nA && (!use_flags || a.pair_flag[(size_t)f * a.nA + i]) && a.abs_of_slot[i] != a.abs_of_slot[i + a.nA]) {
     const FrameConst &fc = a.fc[f];
     const uint4 q0 = a.q[fo + i], q1 = a.q[fo + i + a.nA];
-    const float dx = fixed_delta(q0.x, q1.x, fc.scale[0]), dy = fixed_delta(q0.y, q1.y, fc.scale[1]),
-                dz = fixed_delta(q0.z, q1.z, fc.scale[2]);
+    float dx, dy, dz;
+    Geo32<TRIC>(fc).delta(q0, q1, dx, dy, dz);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     bool in = r2 <= s32.dmax2_lo;
     if (!in && r2 <= s32.dmax2_hi)  // band: pair i is (slot i, slot i+nA) in the reference's orientation

@@ -61,6 +61,7 @@ static int nh_compiled(const SwitchParams &sw) {
 
 void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
                       int unroll, cudaStream_t s) {
+  if (a.tric_band > 0.f) return launch_eval_nl32_tric(a, sw, s32, mode, nblocks, s);
   // persistent: nblocks blocks over all frames, at least one per frame, at
   // most one per 8 slices of a frame (8 warps per block)
   const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
@@ -83,6 +84,7 @@ void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s
 
 void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s) {
   if (!(s32.dmax2_lo < s32.dmax2_hi)) return;  // no d_max: nothing to decide
+  if (a.tric_band > 0.f) return launch_band_fix_tric(a, sw, s32, mode, s);
   const int chunks = (a.nslices + 31) / 32;  // one warp per 32 slices
   const dim3 g(std::max(1, std::min((chunks + 7) / 8, 64)), a.nframes);
 #define CALL(N, M) k_band_fix<N, M><<<g, 256, 0, s>>>(a, sw, s32)
@@ -93,6 +95,7 @@ void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s3
 
 void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile, int nblocks,
                        cudaStream_t s) {
+  if (a.tric_band > 0.f) return launch_allpairs32_tric(a, sw, s32, mode, tile, nblocks, s);
   const bool tri = a.mode == MODE_SINGLE;
   const int ni = tri ? a.ns : a.nA, nj = tri ? a.ns : a.ns - a.nA;
   const int nTi = (ni + tile - 1) / tile, nTj = (nj + tile - 1) / tile;
@@ -113,6 +116,7 @@ void launch_allpairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &
 
 void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,
                     cudaStream_t s) {
+  if (a.tric_band > 0.f) return launch_pairs32_tric(a, sw, s32, mode, use_flags, s);
 #define CALL(N, M) k_pairs32<N, M><<<grid1(a.nA, 256, a.nframes), 256, 0, s>>>(a, sw, s32, use_flags)
   NH_MODE_DISPATCH(nh_compiled(sw), mode, CALL);
 #undef CALL

@@ -18,6 +18,9 @@ struct KArgs {
   int do_pbc;     // !NOPBC
   int nl_kind;    // COORD_NL_* (1 classic, 2 cells)
   int cap;        // neighbour-list row capacity (entries per row)
+  // > 0: the frames have generic (triclinic) boxes on the mixed path; the
+  // relative half-width of the FP32 band around d_max^2 (Geo32<true>)
+  float tric_band;
   int ncell_cap;  // cells per frame (allocation)
   int self_cap;   // self-pair list capacity per frame
   int nslices;    // ceil(ns/32)

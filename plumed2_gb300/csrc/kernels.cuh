@@ -150,6 +150,14 @@ __device__ __forceinline__ uint32_t to_fixed_fma(double x, double s, double c) {
   return (uint32_t)(unsigned long long)__double2ll_rn(fma(x, s, c));
 }
 __device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x) {
+  if (fc.tric) {  // reduced fractional coordinates: three FMAs per component
+    uint32_t v[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      v[i] = (uint32_t)(unsigned long long)__double2ll_rn(
+          fma(x[0], fc.fx_m[i], fma(x[1], fc.fx_m[3 + i], x[2] * fc.fx_m[6 + i])));
+    return make_uint4(v[0], v[1], v[2], 0u);
+  }
   return make_uint4(to_fixed_fma(x[0], fc.fx_s[0], fc.fx_c[0]), to_fixed_fma(x[1], fc.fx_s[1], fc.fx_c[1]),
                     to_fixed_fma(x[2], fc.fx_s[2], fc.fx_c[2]), 0u);
 }

@@ -51,6 +51,17 @@ void launch_pairs32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32
                     cudaStream_t s);
 void launch_finalize32(const KArgs &a, int rank_order, cudaStream_t s);
 
+// k_mixed_tric.cu: the same pair kernels for generic (triclinic) boxes
+// (a.tric_band > 0), called by the launchers above; fixedRational<6> and the
+// generic evaluator, one unroll, the D_MAX band widened to a.tric_band
+void launch_eval_nl32_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
+                           cudaStream_t s);
+void launch_band_fix_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s);
+void launch_allpairs32_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int tile,
+                            int nblocks, cudaStream_t s);
+void launch_pairs32_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int use_flags,
+                         cudaStream_t s);
+
 // number of 32-lane switch specialisations compiled for the mixed path
 int mixed_nh(const SwitchParams &sw);  // N/2 of fixedRational<N>, or 0 for the generic evaluator
 

@@ -334,7 +334,10 @@ SWITCHES = ["RATIONAL R_0=0.3 NN=5 MM=11 D_MAX=0.9", "RATIONAL R_0=0.3 NN=5 D_MA
             "RATIONAL R_0=0.3 NN=6 MM=10 D_MAX=0.9", "RATIONAL R_0=0.3 NN=8 MM=16 D_MAX=0.9",
             "RATIONAL R_0=0.3 NN=6 MM=12", "EXP R_0=0.2 D_0=0.1 D_MAX=0.9", "GAUSSIAN R_0=1.0 D_0=0.0 D_MAX=0.9",
             "GAUSSIAN R_0=0.3 D_0=0.1 D_MAX=0.9", "TANH R_0=0.3 D_MAX=0.9", "SMAP R_0=0.3 A=3 B=2 D_MAX=0.9",
-            "CUBIC D_MAX=0.9 D_0=0.1", "COSINUS R_0=0.9", "Q R_0=0.3 D_0=0.1 BETA=5.0 LAMBDA=1.0 REF=0.4 D_MAX=0.9"]
+            "CUBIC D_MAX=0.9 D_0=0.1", "COSINUS R_0=0.9", "Q R_0=0.3 D_0=0.1 BETA=5.0 LAMBDA=1.0 REF=0.4 D_MAX=0.9",
+            "CUSTOM FUNC=1/(1+x^6) R_0=0.3 D_MAX=0.9", "CUSTOM FUNC=1/(1+x2^3) R_0=0.3 D_MAX=0.9",
+            "CUSTOM FUNC=exp(-x^2)*cos(x) R_0=0.3 D_0=0.05 D_MAX=0.9",
+            "CUSTOM FUNC=step(1-x)*(1-x)^2+0.1*tanh(1-x) R_0=0.4 D_MAX=0.9"]
 
 
 @pytest.mark.parametrize("spec", SWITCHES)
@@ -354,30 +357,130 @@ def test_switch_types(orc, spec, prec):
     _check(prec_t, got, ref)
 
 
-def test_triclinic_box_rt42_golden(orc, golden):
-    """regtest/basic/rt42 through the GPU FP64 path: a triclinic box, GROUPA and
-    GROUPB the same 108 atoms; values at %8.4f, forces/virial at %10.5f."""
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_custom_switch_nlist_steps(orc, prec):
+    """CUSTOM switches through the neighbour-list path, lists rebuilt every
+    second step while the atoms move, against the oracle on the same list."""
+    from plumed2_gb300.action import Coordination
+    rng = np.random.default_rng(11)
+    pos = jittered_lattice(1000, 0.3, 0.03, 10)
+    box = np.diag([3.0] * 3)
+    spec = "CUSTOM FUNC=exp(-x^2)*cos(x) R_0=0.3 D_0=0.05 D_MAX=0.8"
+    c = Coordination("GROUPA=1-1000 SWITCH={%s} NLIST NL_CUTOFF=1.0 NL_STRIDE=2" % spec, precision=prec)
+    tol = "fp64_libm" if prec == "fp64" else prec
+    TOL["fp64_libm"] = (1e-11, 1e-10)
+    for step in range(4):
+        if step % 2 == 0:
+            pairs = orc.nl_classic(0, 1000, 0, pos, box, True, 1.0)
+        got = c.calculate(pos, box, step)
+        if step % 2 == 0:
+            assert np.array_equal(_sorted(c.pairs()), _sorted(pairs)), step
+        _check(tol, got, orc.coordination(spec, pos, box, pairs), step)
+        pos = pos + rng.normal(0.0, 0.01, pos.shape)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_triclinic_box_rt42_golden(orc, golden, prec):
+    """regtest/basic/rt42 through the GPU: a triclinic box that the reference
+    reduces, GROUPA and GROUPB the same 108 atoms; values at %8.4f,
+    forces/virial at %10.5f (the regtest's own precision; for the mixed path
+    that plus its relative bounds: the values are about 1.2e4 and the
+    virial about 620 on the diagonal), with d,
+    dfast, f and h the regtest's own CUSTOM (lepton) switching functions."""
     from plumed2_gb300.action import Coordination
     g = golden("rt42.json")
-    pos = np.array(g["frames"][0])
-    box = np.array(g["box"][0]).reshape(3, 3)
+    cs = {k: Coordination("GROUPA=1-108 GROUPB=1-108 " + v, precision=prec) for k, v in [
+        ("c", "R_0=1"), ("d", "SWITCH={CUSTOM FUNC=1/(1+x^6) R_0=1}"),
+        ("dfast", "SWITCH={CUSTOM FUNC=1/(1+x2^3) R_0=1}"), ("e", "R_0=1 NN=7 D_0=0.1"),
+        ("f", "SWITCH={CUSTOM FUNC=1/(1+x^7) R_0=1 D_0=0.1}"), ("g", "SWITCH={EXP R_0=1}"),
+        ("h", "SWITCH={CUSTOM FUNC=exp(-x) R_0=1}")]}
+    c1 = Coordination("GROUPA=1-108 R_0=1", precision=prec)
+    for fi in range(len(g["frames"])):
+        pos = np.array(g["frames"][fi])
+        box = np.array(g["box"][fi]).reshape(3, 3)
+        n = len(pos)
+        o = {}
+        for k, c in cs.items():
+            s, d, v = c.calculate(np.concatenate([pos, pos]), box)
+            o[k] = (s, d[:n] + d[n:], v)
+        for k in "ceg":
+            # mixed: the printed precision plus the path's relative bound
+            tol = 5.01e-5 + (TOL[prec][0] * abs(g[k][fi]) if prec == "mixed" else 0.0)
+            assert abs(o[k][0] - g[k][fi]) <= tol, (fi, k)
+        for i in (1, 2):
+            X = -(o["c"][i] + o["d"][i]) - 0.001 * (o["c"][i] - 0.5 * o["d"][i] - 0.5 * o["dfast"][i]
+                                                    + o["e"][i] - o["f"][i] + o["g"][i] - o["h"][i])
+            ref = np.array(g["ff_forces" if i == 1 else "ff_virial"][fi]).reshape(X.shape)
+            # mixed: the printed precision plus the path's relative bound (the
+            # virial's diagonal is about 620)
+            tol = 5.01e-6 + (TOL[prec][1] * np.abs(ref).max() if prec == "mixed" else 0.0)
+            assert np.abs(X - ref).max() <= tol, (fi, i, np.abs(X - ref).max())
+        tol = 5.01e-5 + (TOL[prec][0] * abs(g["c_single"][fi]) if prec == "mixed" else 0.0)
+        assert abs(c1.calculate(pos, box)[0] - g["c_single"][fi]) <= tol
+
+
+TRIC_BOX = np.array([[3.0, 0.0, 0.0], [0.9, 2.8, 0.0], [-0.6, 0.7, 2.9]])
+
+
+def _tric_frame(m, box, sigma, seed):
+    """m^3 atoms on a jittered lattice in scaled coordinates, through the box rows."""
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*(np.arange(m),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    return ((g + 0.5) / m + rng.normal(0.0, sigma, g.shape)) @ box
+
+
+@pytest.mark.parametrize("kind", ["none", "NLIST", "NLISTCELLS", "PAIR", "PAIR+NLIST"])
+@pytest.mark.parametrize("groups", ["single", "two"])
+def test_mixed_triclinic_box(orc, kind, groups):
+    """The mixed path on a triclinic box: FP32 pair geometry through the
+    reduced cell (and its octant shifts), the D_MAX band decided in FP64;
+    pair sets bit-exact, values within the mixed tolerance of the oracle."""
+    from plumed2_gb300.action import Coordination
+    if groups == "single" and kind.startswith("PAIR"):
+        pytest.skip("PAIR needs two groups")
+    spec = "RATIONAL R_0=0.3 NN=6 MM=12 D_MAX=0.9"
+    pos = _tric_frame(10, TRIC_BOX, 0.01, 3)
     n = len(pos)
-    cs = {k: Coordination("GROUPA=1-108 GROUPB=1-108 " + v) for k, v in [
-        ("c", "R_0=1"), ("d", "SWITCH={RATIONAL R_0=1}"), ("e", "R_0=1 NN=7 D_0=0.1"),
-        ("f", "SWITCH={RATIONAL R_0=1 D_0=0.1 NN=7 MM=14}"), ("g", "SWITCH={EXP R_0=1}")]}
-    out = {}
-    for k, c in cs.items():
-        s, d, v = c.calculate(np.concatenate([pos, pos]), box)
-        out[k] = (s, d[:n] + d[n:], v)
-    assert abs(out["c"][0] - g["c"][0]) <= 5.01e-5
-    assert abs(out["e"][0] - g["e"][0]) <= 5.01e-5
-    assert abs(out["g"][0] - g["g"][0]) <= 5.01e-5
-    F = -(out["c"][1] + out["d"][1]) - 0.001 * (out["c"][1] - out["d"][1] + out["e"][1] - out["f"][1])
-    V = -(out["c"][2] + out["d"][2]) - 0.001 * (out["c"][2] - out["d"][2] + out["e"][2] - out["f"][2])
-    assert np.abs(F - np.array(g["ff_forces"][0])).max() <= 5.01e-6
-    assert np.abs(V - np.array(g["ff_virial"][0]).reshape(3, 3)).max() <= 5.01e-6
-    c1 = Coordination("GROUPA=1-108 R_0=1")
-    assert abs(c1.calculate(pos, box)[0] - g["c_single"][0]) <= 5.01e-5
+    if groups == "single":
+        line, m, n0, n1 = "GROUPA=1-1000", 0, n, 0
+    else:
+        line, m, n0, n1 = "GROUPA=1-500 GROUPB=501-1000", 1, 500, 500
+    if kind.startswith("PAIR"):
+        line += " PAIR"
+        m = 2
+        pos = np.concatenate([pos[:500], pos[100:600]])  # pair i: lattice neighbours along the first row
+    nl = {"NLIST": " NLIST NL_CUTOFF=1.1 NL_STRIDE=2", "NLISTCELLS": " NLISTCELLS NL_CUTOFF=1.1 NL_STRIDE=2",
+          "PAIR+NLIST": " NLIST NL_CUTOFF=1.1 NL_STRIDE=1"}.get(kind, "")
+    c = Coordination("%s SWITCH={%s}%s" % (line, spec, nl), precision="mixed")
+    rng = np.random.default_rng(9)
+    for step in range(3):
+        got = c.calculate(pos, TRIC_BOX, step)
+        if kind == "NLISTCELLS":
+            if step % 2 == 0:
+                pairs = orc.nl_linkcells(m, n0, n1, pos, TRIC_BOX, True, 1.1)
+        elif nl:
+            if step % 2 == 0 or kind == "PAIR+NLIST":
+                pairs = orc.nl_classic(m, n0, n1, pos, TRIC_BOX, True, 1.1)
+        else:
+            pairs = orc.all_pairs(m, n0, n1)
+        if nl and (step % 2 == 0 or kind == "PAIR+NLIST"):
+            assert np.array_equal(_sorted(c.pairs()), _sorted(pairs)), step
+        _check("mixed", got, orc.coordination(spec, pos, TRIC_BOX, pairs), "%s step %d" % (kind, step))
+        pos = pos + rng.normal(0.0, 0.01, pos.shape)
+    c.close()
+
+
+@pytest.mark.parametrize("spec", ["RATIONAL R_0=0.3 NN=6 MM=12", "EXP R_0=0.2 D_0=0.1",
+                                  "CUSTOM FUNC=1/(1+x^6) R_0=0.3 D_MAX=0.7"])
+def test_mixed_triclinic_small_box_shifts(orc, spec):
+    """A 1.5 nm triclinic box and no (or a long) D_MAX: distant pairs take the
+    octant shifts of Pbc::distance."""
+    from plumed2_gb300.action import Coordination
+    box = TRIC_BOX / 2.0
+    pos = _tric_frame(5, box, 0.02, 4)
+    c = Coordination("GROUPA=1-125 SWITCH={%s}" % spec, precision="mixed")
+    got = c.calculate(pos, box)
+    _check("mixed", got, orc.coordination(spec, pos, box, orc.all_pairs(0, 125)), spec)
 
 
 def test_rt20_switch_goldens(golden):
