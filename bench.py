@@ -744,22 +744,27 @@ def run_ours(args):
             e2e_v = e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), args.e2e_steps) / te_b
             cb.close()
             ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
-            # pageable host copies of the trajectory: [step % T][walker]
-            host_pos = [[np.array(hp[k, w]) for w in range(W)] for k in range(T)]
-            # per walker force and virial arrays reused from step to step, as an MD engine does; the call is the
-            # C ABI's coord_forward with the arrays' addresses, as the PLUMED plugin makes it
+            # one pageable position array per walker, which the MD engine rewrites in place every step (outside
+            # the timed calls, as the integrator's update is not PLUMED's); force and virial arrays reused from
+            # step to step.  The call is the C ABI's coord_forward with the arrays' addresses, as the PLUMED
+            # plugin makes it.  (A fresh array per step, never an MD engine's pattern, runs about 1.5x slower on
+            # the direct host path: each first GPU touch of host pages costs address translations.)
+            host_pos = [np.array(hp[0, w]) for w in range(W)]
             outs = [(np.zeros((n, 3)), np.zeros(9), np.zeros(1)) for _ in range(W)]
             hbox = np.ascontiguousarray(box.reshape(9))
             ptrs = [(addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
-            pptr = [[addr(host_pos[k][w]) for w in range(W)] for k in range(T)]
+            pptr = [addr(host_pos[w]) for w in range(W)]
             for w in range(W):
-                ctxs[w].forward_host(pptr[0][w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+                ctxs[w].forward_host(pptr[w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
             n_first = sum(ctxs[w].nl_size() for w in range(W))
-            t0 = time.perf_counter()
+            te = 0.0
             for k in range(1, 1 + args.e2e_steps):
                 for w in range(W):
-                    ctxs[w].forward_host(pptr[k % T][w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-            te = time.perf_counter() - t0
+                    np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
+                t0 = time.perf_counter()
+                for w in range(W):
+                    ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+                te += time.perf_counter() - t0
             # the results landed in the caller's arrays
             assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
             e2e_walker = e2e_pairs(n_first, sum(ctxs[w].nl_size() for w in range(W)), args.e2e_steps) / te
@@ -812,7 +817,8 @@ def run_ours(args):
                                  "by cudaMemcpyAsync on two copy streams beside the kernels of the other chunks",
                     "per_walker_call": {"value": e2e_walker, "unit": "pair-evals/s",
                                         "call": "coord_forward per walker and step (the plugin's call), one context "
-                                                "per walker, pageable host arrays",
+                                                "per walker, pageable host arrays: one position array per walker "
+                                                "rewritten in place between steps (untimed), as an MD engine does",
                                         "host_path": host_path}},
             "gpu_launches": launches, "clocks": clk,
             "other_configs": {"c2_batched_uneven_actions": c2, "c0_cpu_case": c0, "c1_mixed_single_cv": c1},

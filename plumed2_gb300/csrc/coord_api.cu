@@ -133,6 +133,9 @@ struct coord_ctx {
   DevBuf<uint32_t> ell_far;
   DevBuf<unsigned char> band_flag;
   DevBuf<double> band_rec;
+  DevBuf<uint4> band_q;
+  DevBuf<unsigned> band_qn;
+  DevBuf<double> band_qrec;
   // host-API staging
   DevBuf<double> d_pos, d_s, d_deriv, d_virial, d_dparam, d_bvir, d_bpar;
   // saved forward (COORD_FLAG_SAVE)
@@ -321,6 +324,9 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->band_tickets, F);
   ENS(c->band_flag, F * (size_t)((nslices + 31) & ~31) + 32);
   ENS(c->band_rec, F * std::max(nslices, 1) * kPartials);
+  ENS(c->band_q, (size_t)kBandQueueCap);
+  ENS(c->band_qn, 2);
+  ENS(c->band_qrec, (size_t)kBandQueueCap * kPartials);
   ENS(c->cell_count, F * (size_t)c->ncell_cap);
   ENS(c->cell_fill, F * (size_t)c->ncell_cap);
   ENS(c->cell_start, F * ((size_t)c->ncell_cap + 1));
@@ -410,6 +416,10 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
   a.band_flag = c->band_flag.p;
   a.band_rec = c->band_rec.p;
   a.band_tickets = c->band_tickets.p;
+  a.band_q = c->band_q.p;
+  a.band_qn = c->band_qn.p;
+  a.band_qrec = c->band_qrec.p;
+  a.band_qcap = kBandQueueCap;
   a.out_s = s;
   a.out_deriv = deriv;
   a.out_virial = virial;
@@ -640,6 +650,8 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
       const int m = std::min(std::max(mode, 0), 4);
       const int nb = c->nlm_blocks[m] > 0 ? c->nlm_blocks[m] : c->nl_blocks;
       launch_eval_nl32(a, c->sw, c->s32, mode, nb, c->nlm_unroll[m], c->stream);
+      if (tev1) cudaEventRecord(tev1, c->stream);
+      tev1 = nullptr;
       launch_band_fix(a, c->sw, c->s32, mode, c->stream);
     } else {
       launch_eval_nl64(a, c->sw, mode, prefilter64 ? &c->s32 : nullptr, c->stream);
@@ -1174,6 +1186,9 @@ int coord_destroy(coord_ctx *c) {
   c->band_tickets.release();
   c->band_flag.release();
   c->band_rec.release();
+  c->band_q.release();
+  c->band_qn.release();
+  c->band_qrec.release();
   c->d_pos.release();
   c->d_expr.release();
   c->d_s.release();

@@ -549,6 +549,14 @@ __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)
 // block barrier costs more than the locality gains.)
 // (four resident blocks of 256 threads per SM: a 64-register budget, which
 // the latency of the partner gathers needs more than registers)
+// Queues one band pair for k_band_fix and flags its slice (out of line: the
+// pair kernel's loop keeps its registers for the partner gathers).
+__device__ __noinline__ void band_push(unsigned *qn, uint4 *qbuf, int cap, unsigned char *slice_flag, uint4 item) {
+  const unsigned i = atomicAdd(qn, 1u);
+  if (i < (unsigned)cap) qbuf[i] = item;
+  *slice_flag = 1;
+}
+
 template <int NH, int MODE, int kUnroll, bool TRIC = false>
 __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, SwitchF32 s32) {
   const int f = blockIdx.y + a.frame0;
@@ -628,33 +636,33 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
       if (MODE == EVAL_PARAM) acc.add_param(s32, r2, sig, df);
     };
     // pairs whose FP32 r^2 lies in (dmax2_lo, dmax2_hi] cannot decide the
-    // reference's inclusive test r^2 <= d_max^2: they are left to the FP64
-    // fix-up pass (k_band_fix).  bits(r^2) - bits(lo) - 1 is below the band
-    // width exactly for them (r^2 >= 0 orders like its bits; pairs below lo
-    // and dead entries, r^2 = 0, wrap to large values), so one unsigned min
-    // per pair finds them.
+    // reference's inclusive test r^2 <= d_max^2: they are queued for the
+    // FP64 fix-up pass (k_band_fix), and their slice flagged in case the
+    // queue is full.  bits(r^2) - bits(lo) - 1 is below the band width
+    // exactly for them (r^2 >= 0 orders like its bits; pairs below lo and
+    // dead entries, r^2 = 0, wrap to large values).
     const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
     const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
-    uint32_t band_min = 0xffffffffu;
     for (int k = 0; k < w; k += kUnroll) {
-      int p[kUnroll];
+      uint32_t en[kUnroll];  // list entries (partner rank | orientation), ~0 past the row's end
       uint4 qp[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) p[u] = (k + u < len) ? (int)(__ldcs(e + (size_t)(k + u) * 32) & kRankMask) : -1;
+      for (int u = 0; u < kUnroll; u++) en[u] = (k + u < len) ? __ldcs(e + (size_t)(k + u) * 32) : 0xffffffffu;
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) qp[u] = (p[u] >= 0) ? __ldg(q + p[u]) : qr;
+      for (int u = 0; u < kUnroll; u++) qp[u] = (en[u] != 0xffffffffu) ? __ldg(q + (en[u] & kRankMask)) : qr;
 #pragma unroll
       for (int u = 0; u < kUnroll; u++) {
         float dx, dy, dz;
         geo.delta(qr, qp[u], dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (p[u] >= 0 && r2 <= s32.dmax2_lo)
-          pair(p[u], dx, dy, dz, r2, qp[u].w);
-        else
-          band_min = min(band_min, __float_as_uint(r2) - band_lo);
+        if (en[u] != 0xffffffffu && r2 <= s32.dmax2_lo) {
+          pair((int)(en[u] & kRankMask), dx, dy, dz, r2, qp[u].w);
+        } else if (__float_as_uint(r2) - band_lo < band_w) {
+          band_push(a.band_qn, a.band_q, a.band_qcap, a.band_flag + (size_t)f * band_stride(a) + slice,
+                    make_uint4((unsigned)f, (unsigned)r, en[u], 0u));
+        }
       }
     }
-    if (__any_sync(0xffffffffu, band_min < band_w) && lane == 0) a.band_flag[(size_t)f * band_stride(a) + slice] = 1;
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
     if (++pending == kFlushSlices) {
       acc.flush_warp<MODE>(mytot, lane);
@@ -676,25 +684,132 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
   block_records_finish(a, f, gridDim.x);
 }
 
-// FP64 fix-up of the mixed NL pass: the slices flagged by k_eval_nl32 scan
-// their rows again; every pair whose FP32 r^2 lies in the band around
-// d_max^2 takes the reference's own FP64 test (dmax_exact, in the pair's
-// orientation) and, if kept, is evaluated at d_max^2 (both sides of the FP32
-// rounding agree there): partner and row derivatives by vector reductions
-// (before the finalize kernel), s / virial / parameter sums into the slice's
-// record.  The frame's last block adds the records of the flagged slices in
-// slice order to the frame's results and clears the flags, so the outcome
-// does not depend on timing.  With no flagged slice this is a scan of one
-// byte per slice.
+// One band pair of the mixed NL pass (queued or found again in its row):
+// the reference's own FP64 test (dmax_exact, in the pair's orientation) and,
+// if kept, the pair evaluated at d_max^2 (both sides of the FP32 rounding
+// agree there).  The partner's derivative goes out by a vector reduction; the
+// row's is added to (ax, ay, az, aw); s / virial / parameter sums into acc.
+template <int NH, int MODE, bool TRIC>
+__device__ __forceinline__ void band_pair(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32,
+                                          const FrameConst &fc, size_t fo, int r, uint4 qr, uint32_t en, uint4 qq,
+                                          Acc32 &acc, float &ax, float &ay, float &az, float &aw) {
+  float dx, dy, dz;
+  Geo32<TRIC>(fc).delta(qr, qq, dx, dy, dz);
+  const int p = (int)(en & kRankMask);
+  const double *xr = a.pos + (fo + a.slot_of_rank[fo + r]) * 3;
+  const double *xp = a.pos + (fo + a.slot_of_rank[fo + p]) * 3;
+  const bool in = (en & kOrientBit) ? dmax_exact(xr, xp, &fc.pbc, a.do_pbc, s32.dmax_2)
+                                    : dmax_exact(xp, xr, &fc.pbc, a.do_pbc, s32.dmax_2);
+  if (!in) return;
+  float sig, df;
+  sw32<NH>(sw, s32, s32.dmax2, sig, df);
+  if (MODE >= EVAL_PERATOM && sig < (float)kBondEps) {
+    sig = 0.f;
+    df = 0.f;
+  }
+  if (MODE == EVAL_VJP) df *= __uint_as_float(qr.w) + __uint_as_float(qq.w);
+  acc.add_s(sig);
+  if (MODE >= EVAL_DERIV) {
+    const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
+    ax -= ddx;
+    ay -= ddy;
+    az -= ddz;
+    aw += sig;
+    red_add_v4(a.acc32 + fo + p, ddx, ddy, ddz, MODE == EVAL_PERATOM ? sig : 0.f);
+    acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
+  }
+  if (MODE == EVAL_PARAM) acc.add_param(s32, s32.dmax2, sig, df);
+}
+
+// Queue order: frame, row, partner (a total order: a row lists a partner once).
+__device__ __forceinline__ bool band_less(const uint4 &x, const uint4 &y) {
+  if (x.x != y.x) return x.x < y.x;
+  if (x.y != y.y) return x.y < y.y;
+  return (x.z & kRankMask) < (y.z & kRankMask);
+}
+
+// FP64 fix-up of the mixed NL pass.  The pair kernel queued the pairs whose
+// FP32 r^2 lies in the band around d_max^2 (a few hundred among 1.6e8 at
+// 16 x 262,144 atoms).  With all of them in the queue, block (0,0) sorts it
+// in shared memory (bitonic), evaluates one pair per thread (band_pair),
+// and adds each frame's records to the frame's results in queue order, so
+// the sums do not depend on the order the pairs were queued in; it clears
+// the slices' flags.  With more pairs than the queue holds, every block
+// takes the flagged slices instead: their rows are scanned again, each band
+// pair evaluated, a record per slice, and the frame's last block adds the
+// records in slice order.  The last block of the launch resets the queue.
 template <int NH, int MODE, bool TRIC = false>
 __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
+  // the queue's sort (kBandQueueCap entries) or the slice path's reduction
+  __shared__ __align__(16) unsigned char smem[kBandQueueCap * sizeof(uint4)];
+  static_assert(kPartials * 256 * sizeof(double) <= sizeof(smem), "fix-up shared memory");
+  const unsigned nq = __ldcg(a.band_qn);
+  if (nq <= (unsigned)a.band_qcap) {
+    if (blockIdx.x != 0 || blockIdx.y != 0) return;
+    uint4 *sq = reinterpret_cast<uint4 *>(smem);
+    unsigned m = 1;
+    while (m < nq) m <<= 1;
+    for (unsigned i = threadIdx.x; i < m; i += blockDim.x)
+      sq[i] = i < nq ? __ldcg(a.band_q + i) : make_uint4(~0u, ~0u, ~0u, ~0u);
+    __syncthreads();
+    for (unsigned k = 2; k <= m; k <<= 1)
+      for (unsigned j = k >> 1; j > 0; j >>= 1) {
+        for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
+          const unsigned l = i ^ j;
+          if (l > i) {
+            const uint4 x = sq[i], y = sq[l];
+            if (band_less(y, x) == ((i & k) == 0)) {
+              sq[i] = y;
+              sq[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (unsigned i = threadIdx.x; i < nq; i += blockDim.x) {
+      const uint4 t = sq[i];
+      const int f = (int)t.x, r = (int)t.y;
+      const size_t fo = (size_t)f * a.ns;
+      const FrameConst &fc = a.fc[f];
+      const uint4 qr = a.q[fo + r];
+      Acc32 acc;
+      float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+      band_pair<NH, MODE, TRIC>(a, sw, s32, fc, fo, r, qr, t.z, a.q[fo + (t.z & kRankMask)], acc, ax, ay, az, aw);
+      if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f || aw != 0.f))
+        red_add_v4(a.acc32 + fo + r, ax, ay, az, MODE == EVAL_PERATOM ? aw : 0.f);
+      double part[kPartials];
+      acc.to_partials(part);
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) a.band_qrec[(size_t)i * kPartials + k] = part[k];
+      a.band_flag[(size_t)f * band_stride(a) + r / 32] = 0;
+    }
+    __syncthreads();
+    // each frame's run of the sorted queue, summed in order by its first thread
+    for (unsigned i = threadIdx.x; i < nq; i += blockDim.x) {
+      const unsigned f = sq[i].x;
+      if (i > 0 && sq[i - 1].x == f) continue;
+      double v[kPartials];
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) v[k] = 0.0;
+      for (unsigned j = i; j < nq && sq[j].x == f; j++)
+#pragma unroll
+        for (int k = 0; k < kPartials; k++) v[k] += a.band_qrec[(size_t)j * kPartials + k];
+      if (a.out_s) a.out_s[f] += v[0];
+      if (a.out_virial)
+        for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += v[1 + k];
+      if (a.out_dparam)
+        for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += v[10 + k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) a.band_qn[0] = 0u;
+    return;
+  }
   const int f = blockIdx.y + a.frame0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const size_t fo = (size_t)f * a.ns;
   const FrameConst &fc = a.fc[f];
   const Geo32<TRIC> geo(fc);
   const uint4 *__restrict__ q = a.q + fo;
-  float4 *__restrict__ acc4 = a.acc32 + fo;
   unsigned char *flag = a.band_flag + (size_t)f * band_stride(a);
   const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
   const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
@@ -726,34 +841,11 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
         geo.delta(qr, qq[u], dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         if ((__float_as_uint(r2) - band_lo) >= band_w) continue;  // dead entries: r2 = 0, never in the band
-        const int p = (int)(en[u] & kRankMask);
-        const double *xr = a.pos + (fo + a.slot_of_rank[fo + r]) * 3;
-        const double *xp = a.pos + (fo + a.slot_of_rank[fo + p]) * 3;
-        const bool in = (en[u] & kOrientBit) ? dmax_exact(xr, xp, &fc.pbc, a.do_pbc, s32.dmax_2)
-                                             : dmax_exact(xp, xr, &fc.pbc, a.do_pbc, s32.dmax_2);
-        if (!in) continue;
-        float sig, df;
-        sw32<NH>(sw, s32, s32.dmax2, sig, df);
-        if (MODE >= EVAL_PERATOM && sig < (float)kBondEps) {
-          sig = 0.f;
-          df = 0.f;
-        }
-        if (MODE == EVAL_VJP) df *= __uint_as_float(qr.w) + __uint_as_float(qq[u].w);
-        acc.add_s(sig);
-        if (MODE >= EVAL_DERIV) {
-          const float ddx = df * dx, ddy = df * dy, ddz = df * dz;
-          ax -= ddx;
-          ay -= ddy;
-          az -= ddz;
-          aw += sig;
-          red_add_v4(acc4 + p, ddx, ddy, ddz, MODE == EVAL_PERATOM ? sig : 0.f);
-          acc.add_vir(ddx, ddy, ddz, dx, dy, dz);
-        }
-        if (MODE == EVAL_PARAM) acc.add_param(s32, s32.dmax2, sig, df);
+        band_pair<NH, MODE, TRIC>(a, sw, s32, fc, fo, r, qr, en[u], qq[u], acc, ax, ay, az, aw);
       }
     }
     if (MODE >= EVAL_DERIV && (ax != 0.f || ay != 0.f || az != 0.f || aw != 0.f))
-      red_add_v4(acc4 + r, ax, ay, az, MODE == EVAL_PERATOM ? aw : 0.f);
+      red_add_v4(a.acc32 + fo + r, ax, ay, az, MODE == EVAL_PERATOM ? aw : 0.f);
     double part[kPartials];
     acc.to_partials(part);
     double *rec = a.band_rec + ((size_t)f * a.nslices + slice) * kPartials;
@@ -792,7 +884,7 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
     fv[0] = make_uint4(0u, 0u, 0u, 0u);
     fv[1] = make_uint4(0u, 0u, 0u, 0u);
   }
-  __shared__ double red[kPartials][256];
+  double(*red)[256] = reinterpret_cast<double(*)[256]>(smem);
   __shared__ int any_block;
   if (threadIdx.x == 0) any_block = 0;
   __syncthreads();
@@ -813,6 +905,12 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
         for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += red[1 + k][0];
       if (a.out_dparam)
         for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += red[10 + k][0];
+    }
+    // the launch's last frame resets the queue
+    __threadfence();
+    if (atomicAdd(&a.band_qn[1], 1u) == gridDim.y - 1u) {
+      a.band_qn[1] = 0u;
+      a.band_qn[0] = 0u;
     }
   }
 }

@@ -7,6 +7,7 @@
 namespace coordgpu {
 
 constexpr int kPartials = 12;  // s, virial[9], ds/dR0, ds/dD0
+constexpr int kBandQueueCap = 2048;  // band pairs the fix-up sorts in shared memory
 constexpr uint32_t kOrientBit = 0x80000000u;
 constexpr uint32_t kRankMask = 0x7fffffffu;
 
@@ -70,6 +71,13 @@ struct KArgs {
   unsigned char *band_flag;     // [nframes][nslices]
   double *band_rec;             // [nframes][nslices][kPartials] per flagged slice
   unsigned *band_tickets;       // [nframes]
+  // the band's pairs themselves, queued by the pair kernel: {frame, row rank,
+  // list entry, 0}; band_qn[0] counts them (beyond band_qcap only the flags
+  // above hold them), band_qn[1] is the fix-up's completion ticket
+  uint4 *band_q;                // [band_qcap]
+  unsigned *band_qn;            // [2]
+  double *band_qrec;            // [band_qcap][kPartials]
+  int band_qcap;
   double *out_s;                // [nframes]
   double *out_deriv;            // [nframes][ns][3] slot order
   double *out_virial;           // [nframes][9]

@@ -483,6 +483,35 @@ def test_mixed_triclinic_small_box_shifts(orc, spec):
     _check("mixed", got, orc.coordination(spec, pos, box, orc.all_pairs(0, 125)), spec)
 
 
+@pytest.mark.parametrize("m,a,kind", [(8, 0.25, "NLIST"), (8, 0.3, "NLIST"), (16, 0.25, "NLIST"),
+                                       (16, 0.3, "NLISTCELLS"), (10, 0.25, "none")])
+def test_mixed_dmax_band_on_a_lattice(orc, m, a, kind):
+    """A perfect simple-cubic lattice whose spacing is D_MAX: every
+    nearest-neighbour pair lies in the FP32 band around D_MAX^2 and is decided
+    by the FP64 fix-up (3 m^3 such pairs: 1,536 fit its queue, 12,288 take the
+    flagged-slice rescan; 0.25 is exact in binary, so those pairs are all in,
+    0.3 is not).  Values and the pair set against the oracle over two calls
+    (the fix-up resets its queue)."""
+    from plumed2_gb300.action import Coordination
+    from plumed2_gb300.frames import sc_sites
+    n = m ** 3
+    pos = sc_sites(n) * a
+    box = np.diag([m * a] * 3)
+    spec = "RATIONAL R_0=%.2f NN=6 MM=12 D_MAX=%.2f NOSTRETCH" % (0.8 * a, a)  # nonzero at D_MAX
+    nl = "" if kind == "none" else " %s NL_CUTOFF=%.2f NL_STRIDE=1" % (kind, 1.5 * a)
+    c = Coordination("GROUPA=1-%d SWITCH={%s}%s" % (n, spec, nl), precision="mixed")
+    for step in range(2):
+        got = c.calculate(pos, box, step)
+        if kind == "none":
+            pairs = orc.all_pairs(0, n)
+        else:
+            pairs = (orc.nl_classic if kind == "NLIST" else orc.nl_linkcells)(0, n, 0, pos, box, True, 1.5 * a)
+            assert np.array_equal(_sorted(c.pairs()), _sorted(pairs))
+        ref = orc.coordination(spec, pos, box, pairs)
+        _check("mixed", got, ref, "step %d" % step, dfloor=np.abs(ref[2]).max())
+    c.close()
+
+
 def test_rt20_switch_goldens(golden):
     """regtest/basic/rt20-switch-*: two atoms over switchtraj.xyz through the GPU."""
     from plumed2_gb300.action import Coordination
