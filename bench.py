@@ -756,9 +756,14 @@ def run_ours(args):
             pptr = [addr(host_pos[w]) for w in range(W)]
             for w in range(W):
                 ctxs[w].forward_host(pptr[w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+            # one stride untimed (each context tunes its passes on its first calls), then the timed steps
+            for k in range(1, 11):
+                for w in range(W):
+                    np.copyto(host_pos[w], hp[k % T, w])
+                    ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
             n_first = sum(ctxs[w].nl_size() for w in range(W))
             te = 0.0
-            for k in range(1, 1 + args.e2e_steps):
+            for k in range(11, 11 + args.e2e_steps):
                 for w in range(W):
                     np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
                 t0 = time.perf_counter()

@@ -1,6 +1,7 @@
 // coord_internal.h -- types shared by the host runtime and the sm_103a kernels.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace coordgpu {
@@ -124,6 +125,10 @@ struct FrameConst {
   // the same q in one FMA: q = rn(x * fx_s + fx_c) mod 2^32 with
   // fx_s = inv_l * 2^32 and fx_c = -grid.lo * fx_s (fixed_frame_finish)
   double fx_s[3], fx_c[3];
+  // the same q in integer arithmetic (fixed_v64): inv_l as mantissa and
+  // biased exponent, and (-grid.lo * inv_l * 2^64) mod 2^64
+  unsigned long long fxi_m[3], fxi_c[3];
+  int fxi_e[3];
   // generic (triclinic) periodic box on the mixed path: q holds the
   // fractional coordinates in the reduced lattice, component i =
   // frac(sum_j x_j invReduced(j,i)) * 2^32 (fx_m = invReduced * 2^32), so
@@ -140,11 +145,59 @@ struct FrameConst {
 #else
 #define COORD_HD
 #endif
-// Fills the one-FMA constants of the fixed-point frame from inv_l and grid.lo.
+// Fixed point in integer arithmetic: (x * S * 2^64) mod 2^64 for a double x
+// and a positive scale S = sm * 2^(se - 1075) (its 53-bit mantissa with the
+// implicit bit, and its biased exponent).  The two mantissas' exact 106-bit
+// product is shifted into place and truncated toward zero, then signed; the
+// error is below one unit of 2^-64.  No FP64 instruction: the O(N) kernels
+// that convert positions every step are bound by the FP64 pipe otherwise.
+COORD_HD inline unsigned long long fx_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long u;
+  std::memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+// The 106-bit product of two 53-bit integers as (hi, lo) 64-bit words, from
+// four 32 x 32 -> 64-bit multiplies (cheaper on the device than the generic
+// 64-bit multiply and high-word multiply).
+COORD_HD inline void fx_mul53(unsigned long long a, unsigned long long b, unsigned long long &lo,
+                              unsigned long long &hi) {
+  const unsigned long long a0 = (uint32_t)a, a1 = a >> 32, b0 = (uint32_t)b, b1 = b >> 32;
+  const unsigned long long p00 = a0 * b0, mid = a0 * b1 + a1 * b0;  // mid < 2^54
+  lo = p00 + (mid << 32);
+  hi = a1 * b1 + (mid >> 32) + (lo < p00 ? 1ull : 0ull);
+}
+COORD_HD inline unsigned long long fixed_v64(double x, unsigned long long sm, int se) {
+  const unsigned long long b = fx_bits(x);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  unsigned long long lo, hi;
+  fx_mul53(m, sm, lo, hi);
+  const int sh = (e ? e : 1) + se - 2086;  // x S 2^64 = (m sm) 2^sh
+  unsigned long long v;
+  if (sh >= 0)
+    v = sh >= 64 ? 0ull : lo << sh;
+  else if (sh > -64)
+    v = (lo >> -sh) | (hi << (64 + sh));
+  else
+    v = sh > -128 ? hi >> (-sh - 64) : 0ull;
+  return (b >> 63) ? 0ull - v : v;
+}
+
+// Fills the constants of the fixed-point frame from inv_l and grid.lo: the
+// one-FMA form and the integer form.
 COORD_HD inline void fixed_frame_finish(FrameConst &fc) {
   for (int k = 0; k < 3; k++) {
     fc.fx_s[k] = fc.inv_l[k] * 4294967296.0;
     fc.fx_c[k] = -(fc.grid.lo[k] * fc.fx_s[k]);
+    const unsigned long long sb = fx_bits(fc.inv_l[k]);
+    const bool ok = fc.inv_l[k] > 0.0 && ((sb >> 52) & 0x7ffu) != 0;
+    fc.fxi_e[k] = ok ? (int)((sb >> 52) & 0x7ffu) : 0;
+    fc.fxi_m[k] = ok ? ((sb & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : 0ull;
+    fc.fxi_c[k] = fixed_v64(-fc.grid.lo[k], fc.fxi_m[k], fc.fxi_e[k]);
   }
 }
 

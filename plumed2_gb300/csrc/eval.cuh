@@ -730,14 +730,15 @@ __device__ __forceinline__ bool band_less(const uint4 &x, const uint4 &y) {
 
 // FP64 fix-up of the mixed NL pass.  The pair kernel queued the pairs whose
 // FP32 r^2 lies in the band around d_max^2 (a few hundred among 1.6e8 at
-// 16 x 262,144 atoms).  With all of them in the queue, block (0,0) sorts it
-// in shared memory (bitonic), evaluates one pair per thread (band_pair),
-// and adds each frame's records to the frame's results in queue order, so
-// the sums do not depend on the order the pairs were queued in; it clears
-// the slices' flags.  With more pairs than the queue holds, every block
-// takes the flagged slices instead: their rows are scanned again, each band
-// pair evaluated, a record per slice, and the frame's last block adds the
-// records in slice order.  The last block of the launch resets the queue.
+// 16 x 262,144 atoms).  With all of them in the queue, the grid evaluates
+// one pair per thread (band_pair) into a record per pair and clears the
+// slices' flags; the launch's last block sorts the queue (bitonic, in shared
+// memory) and adds each frame's records to the frame's results in that
+// order, so the sums do not depend on the order the pairs were queued in.
+// With more pairs than the queue holds, every block takes the flagged
+// slices instead: their rows are scanned again, each band pair evaluated, a
+// record per slice, and the frame's last block adds the records in slice
+// order.  The last block of the launch resets the queue.
 template <int NH, int MODE, bool TRIC = false>
 __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
   // the queue's sort (kBandQueueCap entries) or the slice path's reduction
@@ -745,29 +746,10 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
   static_assert(kPartials * 256 * sizeof(double) <= sizeof(smem), "fix-up shared memory");
   const unsigned nq = __ldcg(a.band_qn);
   if (nq <= (unsigned)a.band_qcap) {
-    if (blockIdx.x != 0 || blockIdx.y != 0) return;
-    uint4 *sq = reinterpret_cast<uint4 *>(smem);
-    unsigned m = 1;
-    while (m < nq) m <<= 1;
-    for (unsigned i = threadIdx.x; i < m; i += blockDim.x)
-      sq[i] = i < nq ? __ldcg(a.band_q + i) : make_uint4(~0u, ~0u, ~0u, ~0u);
-    __syncthreads();
-    for (unsigned k = 2; k <= m; k <<= 1)
-      for (unsigned j = k >> 1; j > 0; j >>= 1) {
-        for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
-          const unsigned l = i ^ j;
-          if (l > i) {
-            const uint4 x = sq[i], y = sq[l];
-            if (band_less(y, x) == ((i & k) == 0)) {
-              sq[i] = y;
-              sq[l] = x;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    for (unsigned i = threadIdx.x; i < nq; i += blockDim.x) {
-      const uint4 t = sq[i];
+    // every block: the queued pairs one per thread, a record each
+    const unsigned nth = gridDim.x * gridDim.y * blockDim.x;
+    for (unsigned i = (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; i < nq; i += nth) {
+      const uint4 t = __ldcg(a.band_q + i);
       const int f = (int)t.x, r = (int)t.y;
       const size_t fo = (size_t)f * a.ns;
       const FrameConst &fc = a.fc[f];
@@ -783,25 +765,69 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
       for (int k = 0; k < kPartials; k++) a.band_qrec[(size_t)i * kPartials + k] = part[k];
       a.band_flag[(size_t)f * band_stride(a) + r / 32] = 0;
     }
+    // the launch's last block: the queue sorted with each pair's record
+    // index, each frame's records added in that order
+    __shared__ bool last_q;
+    __threadfence();
     __syncthreads();
-    // each frame's run of the sorted queue, summed in order by its first thread
-    for (unsigned i = threadIdx.x; i < nq; i += blockDim.x) {
-      const unsigned f = sq[i].x;
-      if (i > 0 && sq[i - 1].x == f) continue;
-      double v[kPartials];
-#pragma unroll
-      for (int k = 0; k < kPartials; k++) v[k] = 0.0;
-      for (unsigned j = i; j < nq && sq[j].x == f; j++)
-#pragma unroll
-        for (int k = 0; k < kPartials; k++) v[k] += a.band_qrec[(size_t)j * kPartials + k];
-      if (a.out_s) a.out_s[f] += v[0];
-      if (a.out_virial)
-        for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += v[1 + k];
-      if (a.out_dparam)
-        for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += v[10 + k];
+    if (threadIdx.x == 0) last_q = atomicAdd(&a.band_qn[1], 1u) == gridDim.x * gridDim.y - 1u;
+    __syncthreads();
+    if (!last_q) return;
+    __threadfence();
+    uint4 *sq = reinterpret_cast<uint4 *>(smem);
+    unsigned m = 1;
+    while (m < nq) m <<= 1;
+    for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
+      uint4 t = i < nq ? __ldcg(a.band_q + i) : make_uint4(~0u, ~0u, ~0u, ~0u);
+      t.w = i;
+      sq[i] = t;
     }
     __syncthreads();
-    if (threadIdx.x == 0) a.band_qn[0] = 0u;
+    for (unsigned k = 2; k <= m; k <<= 1)
+      for (unsigned j = k >> 1; j > 0; j >>= 1) {
+        for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
+          const unsigned l = i ^ j;
+          if (l > i) {
+            const uint4 x = sq[i], y = sq[l];
+            if (band_less(y, x) == ((i & k) == 0)) {
+              sq[i] = y;
+              sq[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    // each frame's run of the sorted queue, summed by one warp: lane l takes
+    // the run's entries l, l + 32, ... in order, then a fixed shuffle tree --
+    // an order set by the sorted queue alone
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (unsigned c0 = (threadIdx.x >> 5) * 32; c0 < nq; c0 += nw * 32) {
+      const unsigned i = c0 + lane;
+      unsigned heads = __ballot_sync(0xffffffffu, i < nq && (i == 0 || sq[i - 1].x != sq[i].x));
+      for (; heads; heads &= heads - 1u) {
+        const unsigned b = c0 + __ffs(heads) - 1, f = sq[b].x;
+        double v[kPartials];
+#pragma unroll
+        for (int k = 0; k < kPartials; k++) v[k] = 0.0;
+        for (unsigned j = b + lane; j < nq && sq[j].x == f; j += 32)
+#pragma unroll
+          for (int k = 0; k < kPartials; k++) v[k] += __ldcg(a.band_qrec + (size_t)sq[j].w * kPartials + k);
+#pragma unroll
+        for (int k = 0; k < kPartials; k++) v[k] = warp_sum(v[k]);
+        if (lane == 0) {
+          if (a.out_s) a.out_s[f] += v[0];
+          if (a.out_virial)
+            for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += v[1 + k];
+          if (a.out_dparam)
+            for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += v[10 + k];
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      a.band_qn[0] = 0u;
+      a.band_qn[1] = 0u;
+    }
     return;
   }
   const int f = blockIdx.y + a.frame0;

@@ -142,13 +142,11 @@ __device__ void block_partials_finish(const KArgs &a, int frame, double v[kParti
 // ---------------------------------------------------------------------------
 // fixed-point positions (mixed path and the FP32 neighbour-list prefilter)
 // ---------------------------------------------------------------------------
-// Two FP64 operations per coordinate (the FP64 pipe is the bound of the O(N)
-// kernels that convert positions): rn((x - lo) / L * 2^32) as one FMA and one
-// conversion; the low 32 bits of the 64-bit integer are the fraction of the
-// frame, wrapped exactly as frac() would (to within the final rounding).
-__device__ __forceinline__ uint32_t to_fixed_fma(double x, double s, double c) {
-  return (uint32_t)(unsigned long long)__double2ll_rn(fma(x, s, c));
-}
+// q = rn((x - lo) / L * 2^32) mod 2^32 per coordinate: the fraction of the
+// frame, wrapped as frac() would.  Orthorhombic frames (and no PBC) take it
+// in integer arithmetic (fixed_v64), generic boxes through the reduced cell
+// in FP64, and fixed_of_hi (the FP64 pass's image shifts need the high word
+// of the same rounding) as one FP64 FMA and one conversion per coordinate.
 __device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x) {
   if (fc.tric) {  // reduced fractional coordinates: three FMAs per component
     uint32_t v[3];
@@ -158,8 +156,12 @@ __device__ __forceinline__ uint4 fixed_of(const FrameConst &fc, const double *x)
           fma(x[0], fc.fx_m[i], fma(x[1], fc.fx_m[3 + i], x[2] * fc.fx_m[6 + i])));
     return make_uint4(v[0], v[1], v[2], 0u);
   }
-  return make_uint4(to_fixed_fma(x[0], fc.fx_s[0], fc.fx_c[0]), to_fixed_fma(x[1], fc.fx_s[1], fc.fx_c[1]),
-                    to_fixed_fma(x[2], fc.fx_s[2], fc.fx_c[2]), 0u);
+  // rn((x - lo) inv_l 2^32) mod 2^32 in integer arithmetic (fixed_v64)
+  uint32_t v[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    v[k] = (uint32_t)((fixed_v64(x[k], fc.fxi_m[k], fc.fxi_e[k]) + fc.fxi_c[k] + 0x80000000ull) >> 32);
+  return make_uint4(v[0], v[1], v[2], 0u);
 }
 // The same fixed-point positions with their high words: the 64-bit value
 // rn(x * 2^32 / L) is (box image) * 2^32 + q.
@@ -169,6 +171,16 @@ __device__ __forceinline__ uint4 fixed_of_hi(const FrameConst &fc, const double 
   for (int k = 0; k < 3; k++) v[k] = __double2ll_rn(fma(x[k], fc.fx_s[k], fc.fx_c[k]));
   hi = make_int4((int)(v[0] >> 32), (int)(v[1] >> 32), (int)(v[2] >> 32), 0);
   return make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], 0u);
+}
+// float -> double by re-biasing the exponent (exact, as the conversion
+// instruction is, without the FP64 pipe that bounds the O(N) kernels that
+// widen accumulators); subnormals, infinities and NaNs take the instruction.
+__device__ __forceinline__ double f2d_int(float v) {
+  const uint32_t b = __float_as_uint(v);
+  if ((b << 1) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // +-0
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e - 1u >= 254u) return (double)v;
+  return __hiloint2double((int)((b & 0x80000000u) | (((b >> 3) & 0x0fffffffu) + 0x38000000u)), (int)(b << 29));
 }
 __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float scale) {
   return (float)(int)(b - a) * scale;  // wraps modulo 2^32: minimum image
@@ -494,10 +506,16 @@ __global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double 
     const int s = s0 + t;
     const int r = rank_order ? a.rank_of_slot[fo + s] : s;
     const float4 v = a.acc32[fo + r];
-    const double g = a.g ? a.g[f] : 1.0;
-    sd[3 * t] = g * (double)v.x;
-    sd[3 * t + 1] = g * (double)v.y;
-    sd[3 * t + 2] = g * (double)v.z;
+    if (a.g) {  // backward: scaled by the frame's upstream dV/ds
+      const double g = __ldg(a.g + f);
+      sd[3 * t] = g * f2d_int(v.x);
+      sd[3 * t + 1] = g * f2d_int(v.y);
+      sd[3 * t + 2] = g * f2d_int(v.z);
+    } else {
+      sd[3 * t] = f2d_int(v.x);
+      sd[3 * t + 1] = f2d_int(v.y);
+      sd[3 * t + 2] = f2d_int(v.z);
+    }
     if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   __syncthreads();
@@ -1195,10 +1213,16 @@ __global__ void __launch_bounds__(kSlotBlock) k_finalize32(KArgs a, int rank_ord
     const int s = s0 + t;
     const int r = rank_order ? a.rank_of_slot[fo + s] : s;
     const float4 v = a.acc32[fo + r];
-    const double g = a.g ? a.g[f] : 1.0;
-    sd[3 * t] = g * (double)v.x;
-    sd[3 * t + 1] = g * (double)v.y;
-    sd[3 * t + 2] = g * (double)v.z;
+    if (a.g) {  // backward: scaled by the frame's upstream dV/ds
+      const double g = __ldg(a.g + f);
+      sd[3 * t] = g * f2d_int(v.x);
+      sd[3 * t + 1] = g * f2d_int(v.y);
+      sd[3 * t + 2] = g * f2d_int(v.z);
+    } else {
+      sd[3 * t] = f2d_int(v.x);
+      sd[3 * t + 1] = f2d_int(v.y);
+      sd[3 * t + 2] = f2d_int(v.z);
+    }
     if (a.out_peratom) a.out_peratom[fo + s] = (double)v.w;
     if (!a.keep_acc) a.acc32[fo + r] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
