@@ -746,9 +746,10 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
   static_assert(kPartials * 256 * sizeof(double) <= sizeof(smem), "fix-up shared memory");
   const unsigned nq = __ldcg(a.band_qn);
   if (nq <= (unsigned)a.band_qcap) {
-    // every block: the queued pairs one per thread, a record each
-    const unsigned nth = gridDim.x * gridDim.y * blockDim.x;
-    for (unsigned i = (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; i < nq; i += nth) {
+    // every block: the queued pairs one per thread, a record each, dealt
+    // round-robin over the blocks (their FP64 work spread over the SMs)
+    const unsigned nblk = gridDim.x * gridDim.y, nth = nblk * blockDim.x;
+    for (unsigned i = (blockIdx.y * gridDim.x + blockIdx.x) + nblk * threadIdx.x; i < nq; i += nth) {
       const uint4 t = __ldcg(a.band_q + i);
       const int f = (int)t.x, r = (int)t.y;
       const size_t fo = (size_t)f * a.ns;
