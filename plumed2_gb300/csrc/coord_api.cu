@@ -352,6 +352,7 @@ KArgs make_args(coord_ctx *c, int n_frames, const double *d_pos, unsigned flags,
                 double *virial, double *dparam) {
   KArgs a{};
   a.nframes = n_frames;
+  a.disp2_frames = n_frames;
   a.ns = (int)c->ns;
   a.nA = (int)(c->mode == MODE_SINGLE ? c->ns : c->nA);
   a.mode = c->mode;

@@ -64,7 +64,9 @@ void launch_eval_nl32(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s
   if (a.tric_band > 0.f) return launch_eval_nl32_tric(a, sw, s32, mode, nblocks, s);
   // persistent: nblocks blocks over all frames, at least one per frame, at
   // most one per 8 slices of a frame (8 warps per block)
-  const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
+  // (at most a.max_blocks: the records of a frame's blocks)
+  const int per_frame =
+      std::max(1, std::min(std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8), a.max_blocks));
   const dim3 g(per_frame, a.nframes);
   if (unroll >= 8) {
 #define CALL(N, M) k_eval_nl32<N, M, 8><<<g, 256, 0, s>>>(a, sw, s32)

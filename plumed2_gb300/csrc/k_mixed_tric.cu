@@ -54,7 +54,9 @@ int nh_tric(const SwitchParams &sw) { return mixed_nh(sw) == 3 ? 3 : 0; }
 void launch_eval_nl32_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, int nblocks,
                            cudaStream_t s) {
   const SwitchF32 w = widened(s32, a.tric_band);
-  const int per_frame = std::max(1, std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8));
+  // (at most a.max_blocks: the records of a frame's blocks)
+  const int per_frame =
+      std::max(1, std::min(std::min((nblocks + a.nframes - 1) / a.nframes, (a.nslices + 7) / 8), a.max_blocks));
   const dim3 g(per_frame, a.nframes);
 #define CALL(N, M) k_eval_nl32<N, M, 4, true><<<g, 256, 0, s>>>(a, sw, w)
   TRIC_DISPATCH_NL(nh_tric(sw), mode, CALL);

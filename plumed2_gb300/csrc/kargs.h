@@ -52,9 +52,10 @@ struct KArgs {
   int *slice_wn;                // [nframes][nslices] the slice's longest near part
   uint32_t *ell_far;            // like ell: the partition's scratch for far entries
   uint4 *q_build;               // [nframes][ns] fixed-point positions at the rebuild (rank order)
-  unsigned *disp2;              // [2][nframes] the largest squared displacement since the rebuild (FP32
-                                // bits, max over atoms) of this step, and of every step since the
+  unsigned *disp2;              // [2][disp2_frames] the largest squared displacement since the rebuild
+                                // (FP32 bits, max over atoms) of this step, and of every step since the
                                 // rebuild; measured by the gather; or null
+  int disp2_frames;             // the call's frame count (a launch over a chunk of frames keeps it)
   float near_r2;                // the partition's threshold: (d_max + skin)^2 (1 + 1e-5)
   float disp_ok2;               // near parts suffice while disp2 <= (skin/2)^2 (1 - 1e-5); < 0: off
   unsigned long long *nl_count; // [nframes][4]: pairs, self pairs, max row length, geometry error

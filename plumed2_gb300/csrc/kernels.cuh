@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(kSlotBlock) k_prep_host(KArgs a, const double 
     a.q[fo + r] = qq;
     if (a.disp2) d2 = disp2_of(a.fc[f], a.q_build[fo + r], qq);
   }
-  if (a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.nframes + f, d2, t < nb);
+  if (a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.disp2_frames + f, d2, t < nb);
 }
 __global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double *__restrict__ hderiv, int rank_order) {
   const int f = blockIdx.y + a.frame0;
@@ -597,7 +597,7 @@ __global__ void k_gather(KArgs a, int rank_order, int want64, int wantq, int wan
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   float d2 = 0.f;
   if (r < a.ns) d2 = gather_one(a, f, r, rank_order, want64, wantq, wantcell);
-  if (wantq && a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.nframes + f, d2, r < a.ns);
+  if (wantq && a.disp2) disp_max_block(a.disp2 + f, a.disp2 + a.disp2_frames + f, d2, r < a.ns);
 }
 
 // Orders each row of a rebuilt list near part first: entries whose FP32
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(256) k_nl_partition(KArgs a) {
     a.slice_wn[(size_t)f * a.nslices + slice] = wmax;
     if (slice == 0) {
       a.disp2[f] = 0u;
-      a.disp2[a.nframes + f] = 0u;
+      a.disp2[a.disp2_frames + f] = 0u;
     }
   }
 }

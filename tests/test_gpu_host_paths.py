@@ -113,3 +113,40 @@ def test_batched_host_call_equals_device_call(prec, path):
             assert abs(g[0][f] - ref[0][f]) <= tol * abs(ref[0][f])
             assert np.abs(g[1][f] - ref[1][f]).max() <= tol * np.abs(ref[1][f]).max()
             assert np.abs(g[2][f] - ref[2][f]).max() <= tol * np.abs(ref[2][f]).max()
+
+
+def test_pinned_batch_skin_follows_every_walker():
+    """The pinned batched call moves its walkers in chunks; the displacements
+    each chunk measures go to its own walkers' slots, so the skin chosen at a
+    rebuild (from the largest displacement of the interval over every walker)
+    is the device call's on the same trajectory, and so are the near parts."""
+    from plumed2_gb300.action import Coordination
+    from plumed2_gb300._lib import addr
+    n, F, L = 2744, 8, 14 * 0.31
+    line = "GROUPA=1-%d SWITCH={RATIONAL R_0=0.32 NN=6 MM=12 D_MAX=0.6} NLIST NL_CUTOFF=0.8 NL_STRIDE=10" % n
+    pin = lambda *shape: torch.zeros(*shape, dtype=torch.float64, pin_memory=True).numpy()
+    rng = np.random.default_rng(4)
+    traj = [np.stack([jittered_lattice(n, 0.31, 0.03, 90 + f) for f in range(F)])]
+    for k in range(1, 21):
+        # walker f moves with its own step size: the largest moves are the first chunk's
+        traj.append(traj[-1] + rng.normal(0.0, 1.0, (F, n, 3)) * (0.0003 * (F - np.arange(F)))[:, None, None])
+    boxes = np.ascontiguousarray(np.stack([np.diag([L] * 3).reshape(9)] * F))
+    ch = Coordination(line, precision="mixed")
+    pos, s, d, v = pin(F, n, 3), pin(F), pin(F, n, 3), pin(F, 9)
+    dev = torch.device("cuda:0")
+    cd = Coordination(line, precision="mixed")
+    sd = torch.zeros(F, dtype=torch.float64, device=dev)
+    dd = torch.zeros(F, n, 3, dtype=torch.float64, device=dev)
+    vd = torch.zeros(F, 9, dtype=torch.float64, device=dev)
+    for step in range(21):
+        pos[:] = traj[step]
+        ch.forward_host_batch(F, addr(pos), addr(boxes), step, 0, addr(s), addr(d), addr(v))
+        tp = torch.tensor(traj[step], dtype=torch.float64, device=dev)
+        cd.forward_device(tp.data_ptr(), boxes, F, sd.data_ptr(), dd.data_ptr(), vd.data_ptr(), step=step)
+        torch.cuda.synchronize()
+        for f in range(F):
+            assert abs(s[f] - sd[f].item()) <= 1e-6 * abs(sd[f].item()), (step, f)
+    for f in range(F):
+        assert ch.nl_near_size(f) == cd.nl_near_size(f), f
+    ch.close()
+    cd.close()
