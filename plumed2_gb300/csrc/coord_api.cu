@@ -324,9 +324,9 @@ int ensure_buffers(coord_ctx *c, int n_frames) {
   ENS(c->band_tickets, F);
   ENS(c->band_flag, F * (size_t)((nslices + 31) & ~31) + 32);
   ENS(c->band_rec, F * std::max(nslices, 1) * kPartials);
-  ENS(c->band_q, (size_t)kBandQueueCap);
-  ENS(c->band_qn, 2);
-  ENS(c->band_qrec, (size_t)kBandQueueCap * kPartials);
+  ENS(c->band_q, F * kBandQueueCap);
+  ENS(c->band_qn, F + 2);
+  ENS(c->band_qrec, F * kBandQueueCap * kPartials);
   ENS(c->cell_count, F * (size_t)c->ncell_cap);
   ENS(c->cell_fill, F * (size_t)c->ncell_cap);
   ENS(c->cell_start, F * ((size_t)c->ncell_cap + 1));

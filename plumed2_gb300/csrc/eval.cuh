@@ -551,9 +551,13 @@ __device__ __forceinline__ size_t band_stride(const KArgs &a) { return ((size_t)
 // the latency of the partner gathers needs more than registers)
 // Queues one band pair for k_band_fix and flags its slice (out of line: the
 // pair kernel's loop keeps its registers for the partner gathers).
-__device__ __noinline__ void band_push(unsigned *qn, uint4 *qbuf, int cap, unsigned char *slice_flag, uint4 item) {
+__device__ __noinline__ void band_push(unsigned *qn, uint4 *qbuf, int cap, unsigned *overflow,
+                                      unsigned char *slice_flag, uint4 item) {
   const unsigned i = atomicAdd(qn, 1u);
-  if (i < (unsigned)cap) qbuf[i] = item;
+  if (i < (unsigned)cap)
+    qbuf[i] = item;
+  else
+    *overflow = 1u;
   *slice_flag = 1;
 }
 
@@ -658,8 +662,8 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
         if (en[u] != 0xffffffffu && r2 <= s32.dmax2_lo) {
           pair((int)(en[u] & kRankMask), dx, dy, dz, r2, qp[u].w);
         } else if (__float_as_uint(r2) - band_lo < band_w) {
-          band_push(a.band_qn, a.band_q, a.band_qcap, a.band_flag + (size_t)f * band_stride(a) + slice,
-                    make_uint4((unsigned)f, (unsigned)r, en[u], 0u));
+          band_push(a.band_qn + f, a.band_q + (size_t)f * a.band_qcap, a.band_qcap, a.band_qn + a.disp2_frames,
+                    a.band_flag + (size_t)f * band_stride(a) + slice, make_uint4((unsigned)f, (unsigned)r, en[u], 0u));
         }
       }
     }
@@ -721,6 +725,25 @@ __device__ __forceinline__ void band_pair(const KArgs &a, const SwitchParams &sw
   if (MODE == EVAL_PARAM) acc.add_param(s32, s32.dmax2, sig, df);
 }
 
+// Adds a frame's fix-up sums (s, virial row-major, ds/dR_0, ds/dD_0) to its
+// results: every old value loaded before any store, so the twelve
+// read-modify-writes overlap instead of waiting on one another.
+__device__ __forceinline__ void add_frame_results(const KArgs &a, int f, const double v[kPartials]) {
+  double o[kPartials];
+  o[0] = a.out_s ? __ldcg(a.out_s + f) : 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; k++) o[1 + k] = a.out_virial ? __ldcg(a.out_virial + (size_t)f * 9 + k) : 0.0;
+#pragma unroll
+  for (int k = 0; k < 2; k++) o[10 + k] = a.out_dparam ? __ldcg(a.out_dparam + (size_t)f * 2 + k) : 0.0;
+  if (a.out_s) a.out_s[f] = o[0] + v[0];
+  if (a.out_virial)
+#pragma unroll
+    for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] = o[1 + k] + v[1 + k];
+  if (a.out_dparam)
+#pragma unroll
+    for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] = o[10 + k] + v[10 + k];
+}
+
 // Queue order: frame, row, partner (a total order: a row lists a partner once).
 __device__ __forceinline__ bool band_less(const uint4 &x, const uint4 &y) {
   if (x.x != y.x) return x.x < y.x;
@@ -728,30 +751,32 @@ __device__ __forceinline__ bool band_less(const uint4 &x, const uint4 &y) {
   return (x.z & kRankMask) < (y.z & kRankMask);
 }
 
-// FP64 fix-up of the mixed NL pass.  The pair kernel queued the pairs whose
-// FP32 r^2 lies in the band around d_max^2 (a few hundred among 1.6e8 at
-// 16 x 262,144 atoms).  With all of them in the queue, the grid evaluates
-// one pair per thread (band_pair) into a record per pair and clears the
-// slices' flags; the launch's last block sorts the queue (bitonic, in shared
-// memory) and adds each frame's records to the frame's results in that
-// order, so the sums do not depend on the order the pairs were queued in.
-// With more pairs than the queue holds, every block takes the flagged
-// slices instead: their rows are scanned again, each band pair evaluated, a
-// record per slice, and the frame's last block adds the records in slice
-// order.  The last block of the launch resets the queue.
+// FP64 fix-up of the mixed NL pass.  The pair kernel queued, per frame, the
+// pairs whose FP32 r^2 lies in the band around d_max^2 (about a hundred per
+// frame among 1e7 at 262,144 atoms).  With every frame's pairs in its queue,
+// a frame's blocks evaluate them one per thread (band_pair) into a record
+// per pair and clear the slices' flags; the frame's last block sorts the
+// frame's queue (bitonic, in shared memory) and adds the records to the
+// frame's results in that order, so the sums do not depend on the order the
+// pairs were queued in.  When some frame's queue overflowed, every block
+// takes the flagged slices instead: their rows are scanned again, each band
+// pair evaluated, a record per slice, and the frame's last block adds the
+// records in slice order.  Each frame's last block resets its queue.
 template <int NH, int MODE, bool TRIC = false>
 __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, SwitchF32 s32) {
   // the queue's sort (kBandQueueCap entries) or the slice path's reduction
-  __shared__ __align__(16) unsigned char smem[kBandQueueCap * sizeof(uint4)];
-  static_assert(kPartials * 256 * sizeof(double) <= sizeof(smem), "fix-up shared memory");
-  const unsigned nq = __ldcg(a.band_qn);
-  if (nq <= (unsigned)a.band_qcap) {
-    // every block: the queued pairs one per thread, a record each, dealt
-    // round-robin over the blocks (their FP64 work spread over the SMs)
-    const unsigned nblk = gridDim.x * gridDim.y, nth = nblk * blockDim.x;
-    for (unsigned i = (blockIdx.y * gridDim.x + blockIdx.x) + nblk * threadIdx.x; i < nq; i += nth) {
-      const uint4 t = __ldcg(a.band_q + i);
-      const int f = (int)t.x, r = (int)t.y;
+  __shared__ __align__(16) unsigned char smem[kPartials * 256 * sizeof(double)];
+  static_assert(kBandQueueCap * sizeof(uint4) <= sizeof(smem), "fix-up shared memory");
+  if (__ldcg(a.band_qn + a.disp2_frames) == 0u) {  // every frame's band pairs are in its queue
+    const int f = blockIdx.y + a.frame0;
+    const unsigned nq = __ldcg(a.band_qn + f);
+    const uint4 *qf = a.band_q + (size_t)f * a.band_qcap;
+    double *rf = a.band_qrec + (size_t)f * a.band_qcap * kPartials;
+    // the frame's blocks: its queued pairs one per thread, a record each,
+    // dealt round-robin over the blocks (their FP64 work spread over the SMs)
+    for (unsigned i = blockIdx.x + gridDim.x * threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+      const uint4 t = __ldcg(qf + i);
+      const int r = (int)t.y;
       const size_t fo = (size_t)f * a.ns;
       const FrameConst &fc = a.fc[f];
       const uint4 qr = a.q[fo + r];
@@ -763,15 +788,15 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
       double part[kPartials];
       acc.to_partials(part);
 #pragma unroll
-      for (int k = 0; k < kPartials; k++) a.band_qrec[(size_t)i * kPartials + k] = part[k];
+      for (int k = 0; k < kPartials; k++) rf[(size_t)i * kPartials + k] = part[k];
       a.band_flag[(size_t)f * band_stride(a) + r / 32] = 0;
     }
-    // the launch's last block: the queue sorted with each pair's record
-    // index, each frame's records added in that order
+    // the frame's last block: its queue sorted (row, partner) with each
+    // pair's record index, the records added in that order
     __shared__ bool last_q;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last_q = atomicAdd(&a.band_qn[1], 1u) == gridDim.x * gridDim.y - 1u;
+    if (threadIdx.x == 0) last_q = atomicAdd(&a.band_tickets[f], 1u) == gridDim.x - 1u;
     __syncthreads();
     if (!last_q) return;
     __threadfence();
@@ -779,7 +804,7 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
     unsigned m = 1;
     while (m < nq) m <<= 1;
     for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
-      uint4 t = i < nq ? __ldcg(a.band_q + i) : make_uint4(~0u, ~0u, ~0u, ~0u);
+      uint4 t = i < nq ? __ldcg(qf + i) : make_uint4(~0u, ~0u, ~0u, ~0u);
       t.w = i;
       sq[i] = t;
     }
@@ -798,36 +823,34 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
         }
         __syncthreads();
       }
-    // each frame's run of the sorted queue, summed by one warp: lane l takes
-    // the run's entries l, l + 32, ... in order, then a fixed shuffle tree --
-    // an order set by the sorted queue alone
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (unsigned c0 = (threadIdx.x >> 5) * 32; c0 < nq; c0 += nw * 32) {
-      const unsigned i = c0 + lane;
-      unsigned heads = __ballot_sync(0xffffffffu, i < nq && (i == 0 || sq[i - 1].x != sq[i].x));
-      for (; heads; heads &= heads - 1u) {
-        const unsigned b = c0 + __ffs(heads) - 1, f = sq[b].x;
-        double v[kPartials];
+    // warp w sums the sorted records w, w + 8, ... lane by lane (lane l:
+    // records w + 8 (l + 32 i)), then a fixed shuffle tree, then the warps'
+    // sums in warp order: an order set by the sorted queue alone
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double v[kPartials];
 #pragma unroll
-        for (int k = 0; k < kPartials; k++) v[k] = 0.0;
-        for (unsigned j = b + lane; j < nq && sq[j].x == f; j += 32)
+    for (int k = 0; k < kPartials; k++) v[k] = 0.0;
+    for (unsigned j = warp + nw * lane; j < nq; j += nw * 32)
 #pragma unroll
-          for (int k = 0; k < kPartials; k++) v[k] += __ldcg(a.band_qrec + (size_t)sq[j].w * kPartials + k);
+      for (int k = 0; k < kPartials; k++) v[k] += __ldcg(rf + (size_t)sq[j].w * kPartials + k);
 #pragma unroll
-        for (int k = 0; k < kPartials; k++) v[k] = warp_sum(v[k]);
-        if (lane == 0) {
-          if (a.out_s) a.out_s[f] += v[0];
-          if (a.out_virial)
-            for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += v[1 + k];
-          if (a.out_dparam)
-            for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += v[10 + k];
-        }
-      }
-    }
+    for (int k = 0; k < kPartials; k++) v[k] = warp_sum(v[k]);
+    __syncthreads();  // the records' reads are done with sq; its memory takes the warps' sums
+    double(*ws)[kPartials] = reinterpret_cast<double(*)[kPartials]>(smem);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) ws[warp][k] = v[k];
     __syncthreads();
     if (threadIdx.x == 0) {
-      a.band_qn[0] = 0u;
-      a.band_qn[1] = 0u;
+      double t[kPartials];
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) t[k] = 0.0;
+      for (int w = 0; w < nw; w++)
+#pragma unroll
+        for (int k = 0; k < kPartials; k++) t[k] += ws[w][k];
+      if (nq > 0) add_frame_results(a, f, t);
+      a.band_qn[f] = 0u;
+      a.band_tickets[f] = 0u;
     }
     return;
   }
@@ -927,17 +950,17 @@ __global__ void __launch_bounds__(256) k_band_fix(KArgs a, SwitchParams sw, Swit
   if (threadIdx.x == 0) {
     a.band_tickets[f] = 0u;
     if (any_block) {
-      if (a.out_s) a.out_s[f] += red[0][0];
-      if (a.out_virial)
-        for (int k = 0; k < 9; k++) a.out_virial[(size_t)f * 9 + k] += red[1 + k][0];
-      if (a.out_dparam)
-        for (int k = 0; k < 2; k++) a.out_dparam[(size_t)f * 2 + k] += red[10 + k][0];
+      double v[kPartials];
+#pragma unroll
+      for (int k = 0; k < kPartials; k++) v[k] = red[k][0];
+      add_frame_results(a, f, v);
     }
-    // the launch's last frame resets the queue
+    // the frame's queue count; the launch's last frame resets the overflow flag
+    a.band_qn[f] = 0u;
     __threadfence();
-    if (atomicAdd(&a.band_qn[1], 1u) == gridDim.y - 1u) {
-      a.band_qn[1] = 0u;
-      a.band_qn[0] = 0u;
+    if (atomicAdd(&a.band_qn[a.disp2_frames + 1], 1u) == gridDim.y - 1u) {
+      a.band_qn[a.disp2_frames + 1] = 0u;
+      a.band_qn[a.disp2_frames] = 0u;
     }
   }
 }

@@ -88,7 +88,7 @@ void launch_band_fix(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s3
   if (!(s32.dmax2_lo < s32.dmax2_hi)) return;  // no d_max: nothing to decide
   if (a.tric_band > 0.f) return launch_band_fix_tric(a, sw, s32, mode, s);
   const int chunks = (a.nslices + 31) / 32;  // one warp per 32 slices
-  const dim3 g(std::max(1, std::min((chunks + 7) / 8, 64)), a.nframes);
+  const dim3 g(std::max(1, std::min((chunks + 7) / 8, 8)), a.nframes);  // 8 blocks per frame: one wave
 #define CALL(N, M) k_band_fix<N, M><<<g, 256, 0, s>>>(a, sw, s32)
   NH_MODE_DISPATCH_NL(nh_compiled(sw), mode, CALL);
 #undef CALL

@@ -67,7 +67,7 @@ void launch_eval_nl32_tric(const KArgs &a, const SwitchParams &sw, const SwitchF
 void launch_band_fix_tric(const KArgs &a, const SwitchParams &sw, const SwitchF32 &s32, int mode, cudaStream_t s) {
   const SwitchF32 w = widened(s32, a.tric_band);
   const int chunks = (a.nslices + 31) / 32;
-  const dim3 g(std::max(1, std::min((chunks + 7) / 8, 64)), a.nframes);
+  const dim3 g(std::max(1, std::min((chunks + 7) / 8, 8)), a.nframes);  // 8 blocks per frame: one wave
 #define CALL(N, M) k_band_fix<N, M, true><<<g, 256, 0, s>>>(a, sw, w)
   TRIC_DISPATCH_NL(nh_tric(sw), mode, CALL);
 #undef CALL

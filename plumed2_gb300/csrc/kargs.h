@@ -7,7 +7,7 @@
 namespace coordgpu {
 
 constexpr int kPartials = 12;  // s, virial[9], ds/dR0, ds/dD0
-constexpr int kBandQueueCap = 2048;  // band pairs the fix-up sorts in shared memory
+constexpr int kBandQueueCap = 512;  // band pairs per frame the fix-up sorts in shared memory
 constexpr uint32_t kOrientBit = 0x80000000u;
 constexpr uint32_t kRankMask = 0x7fffffffu;
 
@@ -72,12 +72,14 @@ struct KArgs {
   unsigned char *band_flag;     // [nframes][nslices]
   double *band_rec;             // [nframes][nslices][kPartials] per flagged slice
   unsigned *band_tickets;       // [nframes]
-  // the band's pairs themselves, queued by the pair kernel: {frame, row rank,
-  // list entry, 0}; band_qn[0] counts them (beyond band_qcap only the flags
-  // above hold them), band_qn[1] is the fix-up's completion ticket
-  uint4 *band_q;                // [band_qcap]
-  unsigned *band_qn;            // [2]
-  double *band_qrec;            // [band_qcap][kPartials]
+  // the band's pairs themselves, queued per frame by the pair kernel:
+  // {frame, row rank, list entry, 0}; band_qn[f] counts frame f's (beyond
+  // band_qcap only the flags above hold them), band_qn[disp2_frames] is set
+  // when some frame's queue overflowed, band_qn[disp2_frames + 1] is the
+  // fix-up's completion ticket
+  uint4 *band_q;                // [disp2_frames][band_qcap]
+  unsigned *band_qn;            // [disp2_frames + 2]
+  double *band_qrec;            // [disp2_frames][band_qcap][kPartials]
   int band_qcap;
   double *out_s;                // [nframes]
   double *out_deriv;            // [nframes][ns][3] slot order

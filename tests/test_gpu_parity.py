@@ -483,14 +483,15 @@ def test_mixed_triclinic_small_box_shifts(orc, spec):
     _check("mixed", got, orc.coordination(spec, pos, box, orc.all_pairs(0, 125)), spec)
 
 
-@pytest.mark.parametrize("m,a,kind", [(8, 0.25, "NLIST"), (8, 0.3, "NLIST"), (16, 0.25, "NLIST"),
-                                       (16, 0.3, "NLISTCELLS"), (10, 0.25, "none")])
+@pytest.mark.parametrize("m,a,kind", [(5, 0.25, "NLIST"), (5, 0.3, "NLISTCELLS"), (8, 0.25, "NLIST"),
+                                       (8, 0.3, "NLIST"), (16, 0.25, "NLIST"), (16, 0.3, "NLISTCELLS"),
+                                       (10, 0.25, "none")])
 def test_mixed_dmax_band_on_a_lattice(orc, m, a, kind):
     """A perfect simple-cubic lattice whose spacing is D_MAX: every
     nearest-neighbour pair lies in the FP32 band around D_MAX^2 and is decided
-    by the FP64 fix-up (3 m^3 such pairs: 1,536 fit its queue, 12,288 take the
-    flagged-slice rescan; 0.25 is exact in binary, so those pairs are all in,
-    0.3 is not).  Values and the pair set against the oracle over two calls
+    by the FP64 fix-up (3 m^3 such pairs: 375 fit the frame's queue, 1,536
+    and 12,288 take the flagged-slice rescan; 0.25 is exact in binary, so
+    those pairs are all in, 0.3 is not).  Values and the pair set against the oracle over two calls
     (the fix-up resets its queue)."""
     from plumed2_gb300.action import Coordination
     from plumed2_gb300.frames import sc_sites
