@@ -699,7 +699,7 @@ def run_ours(args):
         # the pair-list layout's own count above; the count for a list of two
         # 4-byte indices per pair with FP32 derivatives (16 N + 8 P + 12 N)
         # beside it, for comparison
-        bytes_2idx = 8 * pairs_launch + 16 * W * n + 12 * W * n
+        bytes_2idx = 8 * pairs_per_step + 16 * W * n + 12 * W * n  # every list pair, as the reference's loop
         gbs_2idx = bytes_2idx / (kern_ms * 1e-3) / 1e9 if kern_ms > 0 else None
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": frac_hbm,
                 "traffic": None,
@@ -709,7 +709,9 @@ def run_ours(args):
                 "two_index_list": {"bytes_per_launch": bytes_2idx, "achieved": gbs_2idx,
                                    "frac": gbs_2idx / hbm_peak if gbs_2idx else None,
                                    "basis": "16 B/atom positions + 8 B/pair (two 4-byte indices) "
-                                            "+ 12 B/atom FP32 derivatives"},
+                                            "+ 12 B/atom FP32 derivatives, over every list pair (%d; the "
+                                            "far ones are known to be zero without being read)"
+                                            % pairs_per_step},
                 "peak_source": ("MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)" if mp.get("hbm_gbs")
                                 else "coord_measure_peaks copy microbenchmark (measured live)")}
         roof["traffic"] = eval_traffic(bytes_alg)

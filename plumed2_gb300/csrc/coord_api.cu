@@ -603,6 +603,21 @@ bool skin_eligible(const coord_ctx *c) {
   return c->p.precision == COORD_PREC_MIXED || fp64_prefilter(c);
 }
 
+// The every-pair kernels' tile: the context's, halved (down to `smallest`)
+// while a frame would have fewer tile pairs than two per SM -- a small
+// system (1,000 atoms: 136 tile pairs of 64) otherwise leaves most SMs idle.
+int fill_tile(const coord_ctx *c, const KArgs &a, int tile, int smallest) {
+  const bool tri = a.mode == MODE_SINGLE;
+  const long long ni = tri ? a.ns : a.nA, nj = tri ? a.ns : a.ns - a.nA;
+  while (tile > smallest) {
+    const long long ti = (ni + tile - 1) / tile, tj = (nj + tile - 1) / tile;
+    const long long ntp = tri ? ti * (ti + 1) / 2 : ti * tj;
+    if (ntp * a.nframes >= 2LL * std::max(c->nsm, 1)) break;
+    tile /= 2;
+  }
+  return tile;
+}
+
 // The pair pass and its finalize kernel (derivatives to slot order, scaled
 // by a.g when set).
 // gathered: the list build of this call already left the positions in rank
@@ -643,9 +658,9 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
       launch_pairs64(a, c->sw, mode, nl ? 1 : 0, c->stream);
   } else if (!nl) {
     if (mixed)
-      launch_allpairs32(a, c->sw, c->s32, mode, c->tile32, c->ap_blocks, c->stream);
+      launch_allpairs32(a, c->sw, c->s32, mode, fill_tile(c, a, c->tile32, 64), c->ap_blocks, c->stream);
     else
-      launch_allpairs64(a, c->sw, mode, c->tile64, c->ap_blocks, c->stream);
+      launch_allpairs64(a, c->sw, mode, fill_tile(c, a, c->tile64, 32), c->ap_blocks, c->stream);
   } else {
     if (mixed) {
       const int m = std::min(std::max(mode, 0), 4);
