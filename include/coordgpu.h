@@ -304,9 +304,10 @@ int coord_cmap_forward(coord_cmap *m, const double *pos, const double box[9], do
  * They are not the engine's whole position and force arrays indexed by
  * atom number.  The call allocates nothing and
  * clears the parts of the shared array that must start at zero; calls that
- * overlap on the GPU share the array and race.  The first call on a device
- * looks the array up with cudaGetSymbolAddress: make it before any stream
- * capture.  More than COORD_NOALLOC_MAX_SLOTS slots: COORD_ERR_ARG. */
+ * overlap on the GPU share the array and race.  Every call copies the frame
+ * constants and the groups from host memory the call owns only while it
+ * runs, so it cannot be captured into a CUDA graph (call it outside stream
+ * capture).  More than COORD_NOALLOC_MAX_SLOTS slots: COORD_ERR_ARG. */
 #define COORD_NOALLOC_MAX_SLOTS 32768
 int coord_forward_noalloc(coord_ctx *ctx, const int64_t *group_a, int64_t n_a, const int64_t *group_b, int64_t n_b,
                           const double *pos, const double box[9], double *s, double *deriv, double *virial,
