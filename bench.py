@@ -71,8 +71,8 @@ def parse():
     ap.add_argument("--quick", action="store_true", help="small sizes (for profiling captures)")
     ap.add_argument("--c2-steps", type=int, default=3,
                     help="timed graph replays of the batched 256-action workload (0: skip it)")
-    ap.add_argument("--workload", default="c4", choices=["c4", "c2", "c1", "c0"],
-                    help="c2 / c1 / c0: only that workload, as its own line")
+    ap.add_argument("--workload", default="c4", choices=["c4", "c3", "c2", "c1", "c0"],
+                    help="c3 / c2 / c1 / c0: only that workload, as its own line")
     return ap.parse_args()
 
 
@@ -383,6 +383,71 @@ def run_c1(dev, steps=100, cpu=True):
         tl = (time.perf_counter() - t0) / 5
         out["cpu_baseline"] = {"value": len(nl) / (tl + tb / 20), "unit": "pair-evals/s", "cores": nth,
                                "kind": "port", "sample": "five steps' pair loops (OpenMP) + 1/20 of the list build"}
+    return out
+
+
+def run_c3(dev, steps=60, cpu=True):
+    """The differentiation case: the C1 system (32,768 atoms in two slabs, NLIST NL_CUTOFF=1.4 NL_STRIDE=20,
+    frames moving by 0.002 nm Gaussian steps) under a 500-hill METAD bias (heights 1.2, sigma 0.05 s0,
+    centres uniform in [0.8 s0, 1.2 s0]): each step the CV with kept derivatives, the bias energy and dV/ds
+    on the device (k_bias_hills), then the backward (forces and box gradient).  Mixed and FP64.  The
+    forces are checked against central finite differences of the biased energy (h = 1e-6 nm) in
+    tests/test_gpu_backward.py."""
+    import torch
+    from plumed2_gb300 import _lib
+    from plumed2_gb300 import frames as FR
+    from plumed2_gb300.action import Coordination
+    spec = "RATIONAL R_0=0.35 NN=6 MM=12 D_MAX=1.2"
+    line = "GROUPA=1-16384 GROUPB=16385-32768 SWITCH={%s} NLIST NL_CUTOFF=1.4 NL_STRIDE=20" % spec
+    xs, box = FR.workload_c1(n_frames=steps + 20)
+    tx = torch.tensor(xs, dtype=torch.float64, device=dev)
+    s = torch.zeros(1, dtype=torch.float64, device=dev)
+    vir = torch.zeros(9, dtype=torch.float64, device=dev)
+    g = torch.zeros(1, dtype=torch.float64, device=dev)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    gpos = torch.zeros(32768, 3, dtype=torch.float64, device=dev)
+    gbox = torch.zeros(9, dtype=torch.float64, device=dev)
+    out = {"workload": "C1's 32,768-atom two-slab system over frames moving by 0.002 nm Gaussian steps, %s, NLIST "
+                       "NL_CUTOFF=1.4 NL_STRIDE=20, a 500-hill METAD bias on the CV; per step the CV with kept "
+                       "derivatives, the bias and dV/ds on the device, the backward (forces, box gradient); steps "
+                       "20..%d timed" % (spec, 19 + steps), "unit": "steps/s"}
+    for prec in ("mixed", "fp64"):
+        c = Coordination(line, precision=prec, device=dev.index or 0)
+        c.forward_device(tx[0].data_ptr(), box[None], 1, s.data_ptr(), 0, 0, step=0, flags=_lib.FLAG_NO_DERIV)
+        torch.cuda.synchronize()
+        s0 = s.item()
+        gen = torch.Generator(device="cpu").manual_seed(3)
+        centres = (s0 * (0.8 + 0.4 * torch.rand(1, 500, generator=gen, dtype=torch.float64))).to(dev)
+        sigmas = torch.full((1, 500), 0.05 * s0, dtype=torch.float64, device=dev)
+        heights = torch.full((1, 500), 1.2, dtype=torch.float64, device=dev)
+
+        def step(k):
+            c.forward_device(tx[k].data_ptr(), box[None], 1, s.data_ptr(), 0, vir.data_ptr(), step=k,
+                             flags=_lib.FLAG_SAVE)
+            _lib.bias_hills(1, s.data_ptr(), 500, centres.data_ptr(), sigmas.data_ptr(), heights.data_ptr(),
+                            energy.data_ptr(), g.data_ptr())
+            c.backward_device(tx[k].data_ptr(), box[None], 1, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(), 0)
+
+        for k in range(20):
+            step(k)
+        t = _time_calls(torch, step, list(range(20, 20 + steps)))
+        out[prec] = {"us_per_step": t * 1e6, "value": 1.0 / t}
+        c.close()
+    if cpu:
+        import oracle
+        oracle.build()
+        orc = oracle.Oracle()
+        nth = orc.max_threads()
+        t0 = time.perf_counter()
+        nl = orc.nl_classic_cells(1, 16384, 16384, xs[20], box, True, 1.4)
+        tb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for k in range(20, 25):
+            orc.coordination(spec, xs[k], box, nl, nthreads=nth)
+        tl = (time.perf_counter() - t0) / 5
+        out["cpu_baseline"] = {"value": 1.0 / (tl + tb / 20), "unit": "steps/s", "cores": nth, "kind": "port",
+                               "sample": "five steps' CV and derivative loops (OpenMP) + 1/20 of the list build; "
+                                         "the bias on one CV costs nothing beside them"}
     return out
 
 
@@ -791,11 +856,12 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(frames, box, budget_s=8.0, gpu_check=gpu_check)
-        c2 = c0 = c1 = None
+        c2 = c0 = c1 = c3 = None
         if args.c2_steps > 0:
             c2 = run_c2(dev, steps=args.c2_steps, cpu=not args.no_cpu_baseline)
             c0 = run_c0(dev, cpu=not args.no_cpu_baseline)
             c1 = run_c1(dev, cpu=not args.no_cpu_baseline)
+            c3 = run_c3(dev, cpu=not args.no_cpu_baseline)
         line_out = {
             "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -839,7 +905,8 @@ def run_ours(args):
                                                 "steps 11..20 after ten untimed ones",
                                         "host_path": host_path}},
             "gpu_launches": launches, "clocks": clk,
-            "other_configs": {"c2_batched_uneven_actions": c2, "c0_cpu_case": c0, "c1_mixed_single_cv": c1},
+            "other_configs": {"c2_batched_uneven_actions": c2, "c0_cpu_case": c0, "c1_mixed_single_cv": c1,
+                              "c3_metad_backward": c3},
         }
         print(json.dumps(line_out), flush=True)
     if ws > 1:
@@ -851,7 +918,7 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("c2", "c1", "c0"):
+    elif args.workload in ("c3", "c2", "c1", "c0"):
         import torch
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
@@ -859,6 +926,8 @@ def main():
             out = run_c2(dev, steps=args.steps, warmup=args.warmup, cpu=not args.no_cpu_baseline)
         elif args.workload == "c1":
             out = run_c1(dev, steps=args.steps, cpu=not args.no_cpu_baseline)
+        elif args.workload == "c3":
+            out = run_c3(dev, steps=args.steps, cpu=not args.no_cpu_baseline)
         else:
             out = run_c0(dev, cpu=not args.no_cpu_baseline)
         print(json.dumps(dict(out, metric=METRIC, n_gpus=1, steps=args.steps, warmup=args.warmup,

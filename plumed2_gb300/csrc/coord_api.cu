@@ -670,7 +670,7 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
       tev1 = nullptr;
       launch_band_fix(a, c->sw, c->s32, mode, c->stream);
     } else {
-      launch_eval_nl64(a, c->sw, mode, prefilter64 ? &c->s32 : nullptr, c->stream);
+      launch_eval_nl64(a, c->sw, mode, prefilter64 ? &c->s32 : nullptr, 2 * std::max(c->nsm, 1), c->stream);
     }
   }
   if (tev1) cudaEventRecord(tev1, c->stream);

@@ -98,7 +98,8 @@ void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaSt
   default: CALL(EVAL_DERIV); break; \
   }
 
-void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const SwitchF32 *prefilter, cudaStream_t s) {
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const SwitchF32 *prefilter, int min_blocks,
+                      cudaStream_t s) {
   if (prefilter) {
     // one warp per slice: (nslices + 7) / 8 blocks per frame, as many as
     // grid1(ns, 256) gives below
@@ -126,7 +127,15 @@ void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const Sw
     g_launches += 1;
     return;
   }
-#define CALL(M) k_eval_nl64<M><<<grid1(a.ns, 256, a.nframes), 256, 0, s>>>(a, sw)
+  // one thread per row: blocks of 256 rows, fewer (down to one warp) while
+  // the launch would have under min_blocks blocks -- on the FP64 pipe (two
+  // lanes per clock per SM) a small system otherwise runs on a few SMs; a
+  // frame's blocks stay within its max_blocks records
+  int bd = 256;
+  while (bd > 32 && (long long)((a.ns + bd - 1) / bd) * a.nframes < min_blocks &&
+         (a.ns + bd / 2 - 1) / (bd / 2) <= a.max_blocks)
+    bd /= 2;
+#define CALL(M) k_eval_nl64<M><<<grid1(a.ns, bd, a.nframes), bd, 0, s>>>(a, sw)
   if (mode == EVAL_PERATOM)
     CALL(EVAL_PERATOM);
   else if (mode == EVAL_VJP)

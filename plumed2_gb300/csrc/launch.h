@@ -32,7 +32,8 @@ void launch_pair_flags(const KArgs &a, cudaStream_t s);
 void launch_gather(const KArgs &a, int rank_order, int want64, int wantq, cudaStream_t s);
 // prefilter: the FP32 parameters of the switch, for the fixed-point screen of
 // k_eval_nl64q (orthorhombic frames of COORDINATION), or null
-void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const SwitchF32 *prefilter, cudaStream_t s);
+void launch_eval_nl64(const KArgs &a, const SwitchParams &sw, int mode, const SwitchF32 *prefilter, int min_blocks,
+                      cudaStream_t s);
 void launch_allpairs64(const KArgs &a, const SwitchParams &sw, int mode, int tile, int nblocks, cudaStream_t s);
 void launch_pairs64(const KArgs &a, const SwitchParams &sw, int mode, int use_flags, cudaStream_t s);
 void launch_finalize64(const KArgs &a, int rank_order, cudaStream_t s);
