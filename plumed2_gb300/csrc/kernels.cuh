@@ -229,9 +229,17 @@ __device__ __forceinline__ int cell_index_of(const FrameConst &fc, const double 
     }
   } else if (g.wrap) {
     for (int k = 0; k < 3; k++) {
-      double f = x[k] * fc.pbc.invbox[4 * k];
-      f = f - floor(f);
-      c[k] = min(max((int)(f * g.nc[k]), 0), g.nc[k] - 1);
+      if (fc.fxi_m[k]) {
+        // floor(frac(x / L) * n) in integer arithmetic: the top 32 bits of
+        // (x / L) 2^64 mod 2^64 (fixed_v64) times n, high word (the O(N)
+        // binning is otherwise bound by the FP64 pipe)
+        const unsigned long long v = fixed_v64(x[k], fc.fxi_m[k], fc.fxi_e[k]);
+        c[k] = min((int)(((v >> 32) * (unsigned long long)g.nc[k]) >> 32), g.nc[k] - 1);
+      } else {
+        double f = x[k] * fc.pbc.invbox[4 * k];
+        f = f - floor(f);
+        c[k] = min(max((int)(f * g.nc[k]), 0), g.nc[k] - 1);
+      }
     }
   } else {
     for (int k = 0; k < 3; k++) {
