@@ -516,9 +516,18 @@ __global__ void __launch_bounds__(kSlotBlock) k_finalize_host32(KArgs a, double 
     const float4 v = a.acc32[fo + r];
     if (a.g) {  // backward: scaled by the frame's upstream dV/ds
       const double g = __ldg(a.g + f);
-      sd[3 * t] = g * f2d_int(v.x);
-      sd[3 * t + 1] = g * f2d_int(v.y);
-      sd[3 * t + 2] = g * f2d_int(v.z);
+      if (fabs(g) > 1e-30 && fabs(g) < 1e30) {
+        // in FP32 (the accumulators hold FP32-accurate derivatives; the
+        // product adds at most 2^-24 relative), off the narrow FP64 pipe
+        const float gf = (float)g;
+        sd[3 * t] = f2d_int(gf * v.x);
+        sd[3 * t + 1] = f2d_int(gf * v.y);
+        sd[3 * t + 2] = f2d_int(gf * v.z);
+      } else {
+        sd[3 * t] = g * f2d_int(v.x);
+        sd[3 * t + 1] = g * f2d_int(v.y);
+        sd[3 * t + 2] = g * f2d_int(v.z);
+      }
     } else {
       sd[3 * t] = f2d_int(v.x);
       sd[3 * t + 1] = f2d_int(v.y);
@@ -1223,9 +1232,18 @@ __global__ void __launch_bounds__(kSlotBlock) k_finalize32(KArgs a, int rank_ord
     const float4 v = a.acc32[fo + r];
     if (a.g) {  // backward: scaled by the frame's upstream dV/ds
       const double g = __ldg(a.g + f);
-      sd[3 * t] = g * f2d_int(v.x);
-      sd[3 * t + 1] = g * f2d_int(v.y);
-      sd[3 * t + 2] = g * f2d_int(v.z);
+      if (fabs(g) > 1e-30 && fabs(g) < 1e30) {
+        // in FP32 (the accumulators hold FP32-accurate derivatives; the
+        // product adds at most 2^-24 relative), off the narrow FP64 pipe
+        const float gf = (float)g;
+        sd[3 * t] = f2d_int(gf * v.x);
+        sd[3 * t + 1] = f2d_int(gf * v.y);
+        sd[3 * t + 2] = f2d_int(gf * v.z);
+      } else {
+        sd[3 * t] = g * f2d_int(v.x);
+        sd[3 * t + 1] = g * f2d_int(v.y);
+        sd[3 * t + 2] = g * f2d_int(v.z);
+      }
     } else {
       sd[3 * t] = f2d_int(v.x);
       sd[3 * t + 1] = f2d_int(v.y);

@@ -207,10 +207,16 @@ def test_saved_forward_matches_recompute(prec):
                 assert np.all(b == 0.0)  # no grad_param requested
                 continue
             assert np.abs(a - b).max() <= tol * max(np.abs(a).max(), 1e-300), (name, k)
-        # the saved gradient is g times the forward's own derivatives
+        # the saved gradient is g times the forward's own derivatives: exactly
+        # on FP64; the mixed path forms the product in FP32 (its derivatives
+        # are FP32-accurate), within 2^-23 relative of each component
         if name in ("save", "save+dr0"):
             s_, der, vir, gp = got[:4]
-            assert np.abs(gp - g.cpu().numpy()[:, None, None] * der).max() <= 1e-14 * np.abs(gp).max()
+            want = g.cpu().numpy()[:, None, None] * der
+            if prec == "fp64":
+                assert np.abs(gp - want).max() <= 1e-14 * np.abs(gp).max()
+            else:
+                assert np.all(np.abs(gp - want) <= 2.0 ** -23 * np.abs(want))
 
 
 def test_c3_metad_backward_at_size(orc):
