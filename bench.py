@@ -407,10 +407,12 @@ def run_c3(dev, steps=60, cpu=True):
     energy = torch.zeros(1, dtype=torch.float64, device=dev)
     gpos = torch.zeros(32768, 3, dtype=torch.float64, device=dev)
     gbox = torch.zeros(9, dtype=torch.float64, device=dev)
+    gpar = torch.zeros(2, dtype=torch.float64, device=dev)
+    dpar = torch.zeros(2, dtype=torch.float64, device=dev)
     out = {"workload": "C1's 32,768-atom two-slab system over frames moving by 0.002 nm Gaussian steps, %s, NLIST "
                        "NL_CUTOFF=1.4 NL_STRIDE=20, a 500-hill METAD bias on the CV; per step the CV with kept "
-                       "derivatives, the bias and dV/ds on the device, the backward (forces, box gradient); steps "
-                       "20..%d timed" % (spec, 19 + steps), "unit": "steps/s"}
+                       "derivatives, the bias and dV/ds on the device, the backward (forces, box gradient, dV/dR_0 "
+                       "and dV/dD_0); steps 20..%d timed" % (spec, 19 + steps), "unit": "steps/s"}
     for prec in ("mixed", "fp64"):
         c = Coordination(line, precision=prec, device=dev.index or 0)
         c.forward_device(tx[0].data_ptr(), box[None], 1, s.data_ptr(), 0, 0, step=0, flags=_lib.FLAG_NO_DERIV)
@@ -423,10 +425,11 @@ def run_c3(dev, steps=60, cpu=True):
 
         def step(k):
             c.forward_device(tx[k].data_ptr(), box[None], 1, s.data_ptr(), 0, vir.data_ptr(), step=k,
-                             flags=_lib.FLAG_SAVE)
+                             flags=_lib.FLAG_SAVE | _lib.FLAG_DR0, dparam_ptr=dpar.data_ptr())
             _lib.bias_hills(1, s.data_ptr(), 500, centres.data_ptr(), sigmas.data_ptr(), heights.data_ptr(),
                             energy.data_ptr(), g.data_ptr())
-            c.backward_device(tx[k].data_ptr(), box[None], 1, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(), 0)
+            c.backward_device(tx[k].data_ptr(), box[None], 1, g.data_ptr(), gpos.data_ptr(), gbox.data_ptr(),
+                              gpar.data_ptr())
 
         for k in range(20):
             step(k)
