@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(256) k_nl_partition(KArgs a) {
   const int wmax = warp_max(nn);
   if (lane == 0) {
     a.slice_wn[(size_t)f * a.nslices + slice] = wmax;
-    if (slice == 0) {
+    if (slice == 0 && a.disp2) {
       a.disp2[f] = 0u;
       a.disp2[a.disp2_frames + f] = 0u;
     }
@@ -686,7 +686,8 @@ __global__ void __launch_bounds__(256) k_nl_partition(KArgs a) {
 // entry of a far part (beyond d_max + skin then) lies beyond d_max now,
 // where every switching function is exactly zero.
 __device__ __forceinline__ bool near_rows_only(const KArgs &a, int f) {
-  return a.row_near != nullptr && a.disp_ok2 >= 0.f && __uint_as_float(a.disp2[f]) <= a.disp_ok2;
+  return a.row_near != nullptr && a.disp2 != nullptr && a.disp_ok2 >= 0.f &&
+         __uint_as_float(a.disp2[f]) <= a.disp_ok2;
 }
 
 // ---------------------------------------------------------------------------
