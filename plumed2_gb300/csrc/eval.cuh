@@ -12,6 +12,8 @@
 // with dfunc = S f'(x)/(r0 r) the reference's dfunc and c_p the dependence of
 // the stretch constants on p (host_setup.cpp).
 #pragma once
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace coordgpu {
@@ -647,26 +649,35 @@ __global__ void __launch_bounds__(256, 4) k_eval_nl32(KArgs a, SwitchParams sw, 
     // dead entries, r^2 = 0, wrap to large values).
     const uint32_t band_lo = __float_as_uint(s32.dmax2_lo) + 1u;
     const uint32_t band_w = __float_as_uint(s32.dmax2_hi) - __float_as_uint(s32.dmax2_lo);
-    for (int k = 0; k < w; k += kUnroll) {
-      uint32_t en[kUnroll];  // list entries (partner rank | orientation), ~0 past the row's end
+    // kUnroll entries of every lane's row from entry k; kChecked: some rows
+    // may end before k + kUnroll (entries past a row's end read as ~0)
+    auto entries = [&](int k, auto checked) {
+      constexpr bool kChecked = decltype(checked)::value;
+      uint32_t en[kUnroll];  // list entries (partner rank | orientation)
       uint4 qp[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) en[u] = (k + u < len) ? __ldcs(e + (size_t)(k + u) * 32) : 0xffffffffu;
+      for (int u = 0; u < kUnroll; u++)
+        en[u] = (!kChecked || k + u < len) ? __ldcs(e + (size_t)(k + u) * 32) : 0xffffffffu;
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) qp[u] = (en[u] != 0xffffffffu) ? __ldg(q + (en[u] & kRankMask)) : qr;
+      for (int u = 0; u < kUnroll; u++)
+        qp[u] = (!kChecked || en[u] != 0xffffffffu) ? __ldg(q + (en[u] & kRankMask)) : qr;
 #pragma unroll
       for (int u = 0; u < kUnroll; u++) {
         float dx, dy, dz;
         geo.delta(qr, qp[u], dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (en[u] != 0xffffffffu && r2 <= s32.dmax2_lo) {
+        if ((!kChecked || en[u] != 0xffffffffu) && r2 <= s32.dmax2_lo) {
           pair((int)(en[u] & kRankMask), dx, dy, dz, r2, qp[u].w);
         } else if (__float_as_uint(r2) - band_lo < band_w) {
           band_push(a.band_qn + f, a.band_q + (size_t)f * a.band_qcap, a.band_qcap, a.band_qn + a.disp2_frames,
                     a.band_flag + (size_t)f * band_stride(a) + slice, make_uint4((unsigned)f, (unsigned)r, en[u], 0u));
         }
       }
-    }
+    };
+    // up to the slice's shortest row no entry needs the row-end test
+    const int kfast = (int)(__reduce_min_sync(0xffffffffu, (unsigned)len) / kUnroll) * kUnroll;
+    for (int k = 0; k < kfast; k += kUnroll) entries(k, std::false_type{});
+    for (int k = kfast; k < w; k += kUnroll) entries(k, std::true_type{});
     if (MODE >= EVAL_DERIV && len > 0) red_add_v4(acc4 + r, ax, ay, az, aw);
     if (++pending == kFlushSlices) {
       acc.flush_warp<MODE>(mytot, lane);
