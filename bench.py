@@ -83,6 +83,24 @@ def e2e_pairs(n_first: int, n_last: int, steps: int) -> int:
     return n_first * (steps - later) + n_last * later
 
 
+E2E_WINDOWS = 3  # timed windows of the end-to-end calls (the median is reported)
+
+HOST_PATH_TEXT = {
+    "chunked": "page-locked arrays on the copy engines, the walkers in four chunks beside the kernels of the "
+               "other chunks",
+    "direct": "kernels reading and writing the caller's arrays in place through the host page tables",
+    "staged": "staged through the context's pinned buffers",
+}
+
+
+def host_path_note(counts):
+    """How the timed host-array calls moved the caller's arrays, as the library reported each call
+    (coord_host_path): every path with its number of calls."""
+    total = sum(counts.values())
+    return "; ".join("%s: %d of %d calls" % (HOST_PATH_TEXT.get(k, str(k)), v, total)
+                     for k, v in sorted(counts.items(), key=lambda kv: -kv[1]))
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -814,13 +832,21 @@ def run_ours(args):
             # steps 0..10 untimed (the context's first calls tune its passes), then the timed steps 11..
             for k in range(0, 11):
                 cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
-            n_first = sum(cb.nl_size(w) for w in range(W))  # the lists of steps 11..19
-            t0 = time.perf_counter()
-            for k in range(11, 11 + args.e2e_steps):
-                cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
-            te_b = time.perf_counter() - t0
+            # three windows of e2e_steps steps (11.., then the next two), each ending on a rebuild step; the
+            # median window is reported, every window listed, and how each timed call moved the arrays counted
+            e2e_windows, batch_paths, k0 = [], {}, 11
+            for _ in range(E2E_WINDOWS):
+                n_first = sum(cb.nl_size(w) for w in range(W))  # the lists of the window's first steps
+                te_b = 0.0
+                for k in range(k0, k0 + args.e2e_steps):
+                    t0 = time.perf_counter()
+                    cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
+                    te_b += time.perf_counter() - t0
+                    batch_paths[cb.host_path()] = batch_paths.get(cb.host_path(), 0) + 1
+                e2e_windows.append(e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), args.e2e_steps) / te_b)
+                k0 += args.e2e_steps
             assert np.all(np.isfinite(hs)) and np.all(hs > 0)
-            e2e_v = e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), args.e2e_steps) / te_b
+            e2e_v = float(np.median(e2e_windows))
             cb.close()
             ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
             # one pageable position array per walker, which the MD engine rewrites in place every step (outside
@@ -840,18 +866,25 @@ def run_ours(args):
                 for w in range(W):
                     np.copyto(host_pos[w], hp[k % T, w])
                     ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-            n_first = sum(ctxs[w].nl_size() for w in range(W))
-            te = 0.0
-            for k in range(11, 11 + args.e2e_steps):
-                for w in range(W):
-                    np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
-                t0 = time.perf_counter()
-                for w in range(W):
-                    ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-                te += time.perf_counter() - t0
+            walker_windows, walker_paths, k0 = [], {}, 11
+            for _ in range(E2E_WINDOWS):
+                n_first = sum(ctxs[w].nl_size() for w in range(W))
+                te = 0.0
+                for k in range(k0, k0 + args.e2e_steps):
+                    for w in range(W):
+                        np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
+                    t0 = time.perf_counter()
+                    for w in range(W):
+                        ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+                    te += time.perf_counter() - t0
+                    for w in range(W):
+                        walker_paths[ctxs[w].host_path()] = walker_paths.get(ctxs[w].host_path(), 0) + 1
+                walker_windows.append(e2e_pairs(n_first, sum(ctxs[w].nl_size() for w in range(W)),
+                                                args.e2e_steps) / te)
+                k0 += args.e2e_steps
             # the results landed in the caller's arrays
             assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
-            e2e_walker = e2e_pairs(n_first, sum(ctxs[w].nl_size() for w in range(W)), args.e2e_steps) / te
+            e2e_walker = float(np.median(walker_windows))
             h2d = W * n * 3 * 8
             d2h = W * (n * 3 * 8 + 10 * 8)
             for x in ctxs:
@@ -896,17 +929,21 @@ def run_ours(args):
                                    "and the same neighbour list; targets |dCV|/CV <= 1e-6, force <= 1e-5 "
                                    "(norm-wise), bit-exact list"),
             "e2e": {"value": e2e_v, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "call": "coord_forward_batch (C ABI, pinned host arrays of all %d walkers by address), steps "
-                            "11..%d after eleven untimed ones (lists rebuilt on multiples of 10)"
-                            % (W, 10 + args.e2e_steps),
-                    "host_path": "copy engines: the walkers in four chunks, positions in and derivatives out "
-                                 "by cudaMemcpyAsync on two copy streams beside the kernels of the other chunks",
+                    "call": "coord_forward_batch (C ABI, pinned host arrays of all %d walkers by address): the "
+                            "median of %d windows of %d steps from step 11 on, each ending on a rebuild step (lists "
+                            "rebuilt on multiples of 10), after eleven untimed steps"
+                            % (W, E2E_WINDOWS, args.e2e_steps),
+                    "windows": e2e_windows if args.e2e_steps > 0 else None,
+                    "host_path": host_path_note(batch_paths) if args.e2e_steps > 0 else None,
                     "per_walker_call": {"value": e2e_walker, "unit": "pair-evals/s",
                                         "call": "coord_forward per walker and step (the plugin's call), one context "
                                                 "per walker, pageable host arrays: one position array per walker "
                                                 "rewritten in place between steps (untimed), as an MD engine does; "
-                                                "steps 11..20 after ten untimed ones",
-                                        "host_path": host_path}},
+                                                "the median of %d windows of %d steps from step 11 on, after ten "
+                                                "untimed steps" % (E2E_WINDOWS, args.e2e_steps),
+                                        "windows": walker_windows if args.e2e_steps > 0 else None,
+                                        "host_path": host_path_note(walker_paths) if args.e2e_steps > 0
+                                        else host_path}},
             "gpu_launches": launches, "clocks": clk,
             "other_configs": {"c2_batched_uneven_actions": c2, "c0_cpu_case": c0, "c1_mixed_single_cv": c1,
                               "c3_metad_backward": c3},

@@ -347,6 +347,18 @@ int coord_bias_restraint(int n_frames, const double *s, double at, double kappa,
  * reference counterpart. */
 int coord_host_memory_access(int device, int *pageable, int *host_page_tables);
 
+/* How the last host-array call of ctx (coord_forward, coord_forward_batch)
+ * moved the caller's arrays: COORD_HOST_PATH_STAGED through the context's
+ * pinned buffers, COORD_HOST_PATH_DIRECT by kernels that access the arrays in
+ * place, COORD_HOST_PATH_CHUNKED (page-locked arrays of several frames) by the
+ * copy engines, chunk by chunk beside the kernels of other chunks; -1 before
+ * the first such call or for a null ctx.  A rebuild step moves the arrays
+ * directly.  No reference counterpart (diagnostics). */
+#define COORD_HOST_PATH_STAGED 0
+#define COORD_HOST_PATH_DIRECT 1
+#define COORD_HOST_PATH_CHUNKED 2
+int coord_host_path(const coord_ctx *ctx);
+
 /* Kernel launches issued by this library since load (for launch accounting). */
 int64_t coord_launch_count(void);
 /* Average device time (ms) of the pair-evaluation kernel over the launches

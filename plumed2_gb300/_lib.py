@@ -116,6 +116,7 @@ def load() -> C.CDLL:
         L.coord_set_timing.argtypes = [_vp, C.c_int]
         L.coord_kernel_times.argtypes = [_vp, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
         L.coord_host_memory_access.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.coord_host_path.argtypes = [_vp]
         L.coord_apply_forces.argtypes = [_vp, C.c_int, _vp, C.c_int64, _vp, _vp, _vp]
         L.coord_bias_hills.argtypes = [C.c_int, _vp, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp]
         L.coord_bias_restraint.argtypes = [C.c_int, _vp, C.c_double, C.c_double, C.c_double, C.c_int, _vp, _vp, _vp]

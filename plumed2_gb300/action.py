@@ -286,6 +286,13 @@ class Coordination:
         check(self._L, self._ctx, self._L.coord_nl_size(self._ctx, frame, C.byref(n)))
         return n.value
 
+    # how the last host-array call moved the arrays (coord_host_path)
+    HOST_PATHS = {-1: None, 0: "staged", 1: "direct", 2: "chunked"}
+
+    def host_path(self):
+        """'staged', 'direct' or 'chunked' for the last forward_host / forward_host_batch, or None."""
+        return self.HOST_PATHS.get(self._L.coord_host_path(self._ctx))
+
     def nl_near_size(self, frame: int = 0):
         """(entries in the rows' near parts, skin): coord_nl_near_size."""
         n, sk = C.c_int64(), C.c_double()

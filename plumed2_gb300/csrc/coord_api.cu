@@ -78,6 +78,7 @@ struct coord_ctx {
   std::vector<int64_t> abs_host;  // GROUPA then GROUPB absolute indices
   bool has_dup = false;           // an absolute index in two slots
   int host_direct = -1;           // kernels access pageable host arrays in place (-1: not probed)
+  int host_path = -1;             // how the last host-array call moved its arrays (coord_host_path)
   bool groups_set = false;
   // the CV's pairing (COORD_CV_*); the sibling CVs' constants and per-atom
   // data by absolute index, copied per slot to the device when needed
@@ -628,8 +629,10 @@ void launch_evaluation(coord_ctx *c, const KArgs &a, int mode, const HostIO *io 
   const int rank_order = (nl && c->mode != MODE_PAIR) ? 1 : 0;
   const bool prefilter64 = !mixed && nl && c->mode != MODE_PAIR && fp64_prefilter(c);
   if (io && io->fused && io->pinned && nl && mixed && c->mode != MODE_PAIR && a.nframes >= 2 && !c->timing &&
-      (!io->deriv || a.out_deriv) && launch_evaluation_chunked(c, a, mode, io))
+      (!io->deriv || a.out_deriv) && launch_evaluation_chunked(c, a, mode, io)) {
+    c->host_path = COORD_HOST_PATH_CHUNKED;
     return;
+  }
   // positions for the pair kernel: fixed-point (mixed) or FP64 in rank order
   if (io && io->fused) {
     launch_prep_host(a, io->pos, rank_order, c->stream);
@@ -1482,6 +1485,7 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
     // variables.
     if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3))) return c->cuda_fail(e, "staging allocation");
     HostIO hio{pos, want_d ? deriv : nullptr, false, false};
+    c->host_path = COORD_HOST_PATH_DIRECT;
     int rc = forward_impl(c, 1, c->d_pos.p, box, step, flags, s, want_d ? c->d_deriv.p : nullptr,
                           want_d ? virial : nullptr, nullptr, nullptr, &hio);
     if (rc) return rc;
@@ -1491,6 +1495,7 @@ int coord_forward(coord_ctx *c, const double *pos, const double box[9], int64_t 
   if ((e = c->d_pos.ensure(n3)) || (e = c->d_deriv.ensure(n3)) || (e = c->d_s.ensure(1)) ||
       (e = c->d_virial.ensure(9)) || (e = c->h_pos.ensure(n3)) || (e = c->h_out.ensure(n3 + 10)))
     return c->cuda_fail(e, "staging allocation");
+  c->host_path = COORD_HOST_PATH_STAGED;
   if (n3) {
     std::memcpy(c->h_pos.p, pos, n3 * sizeof(double));
     if ((e = cudaMemcpyAsync(c->d_pos.p, c->h_pos.p, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
@@ -1548,6 +1553,7 @@ int coord_forward_batch(coord_ctx *c, int n_frames, const double *pos, const dou
       return at.type == cudaMemoryTypeHost;
     };
     HostIO hio{pos, want_d ? deriv : nullptr, false, locked(pos) && (!want_d || locked(deriv))};
+    c->host_path = COORD_HOST_PATH_DIRECT;  // COORD_HOST_PATH_CHUNKED when the chunked pass runs
     int rc = forward_impl(c, n_frames, c->d_pos.p, boxes, step, flags, s, want_d ? c->d_deriv.p : nullptr,
                           want_d ? virial : nullptr, nullptr, nullptr, &hio);
     if (rc) return rc;
@@ -1558,6 +1564,7 @@ int coord_forward_batch(coord_ctx *c, int n_frames, const double *pos, const dou
   if ((e = c->d_s.ensure(nf)) || (e = c->d_virial.ensure(9 * nf)) || (e = c->h_pos.ensure(n3)) ||
       (e = c->h_out.ensure(n3 + 10 * nf)))
     return c->cuda_fail(e, "staging allocation");
+  c->host_path = COORD_HOST_PATH_STAGED;
   std::memcpy(c->h_pos.p, pos, n3 * sizeof(double));
   if ((e = cudaMemcpyAsync(c->d_pos.p, c->h_pos.p, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
     return c->cuda_fail(e, "H2D positions");
@@ -1787,6 +1794,8 @@ int coord_apply_forces(coord_ctx *c, int n_frames, const double *ff, int64_t n_a
   if ((e = cudaGetLastError()) != cudaSuccess) return c->cuda_fail(e, "force application");
   return COORD_OK;
 }
+
+int coord_host_path(const coord_ctx *c) { return c ? c->host_path : -1; }
 
 int coord_host_memory_access(int device, int *pageable, int *host_page_tables) {
   int a = 0, b = 0;

@@ -36,6 +36,16 @@ def test_library_exports_every_declared_symbol(lib):
         getattr(lib, s)  # resolvable through ctypes
 
 
+def test_host_path_without_a_call(lib):
+    # no context, or no host-array call yet: -1; the codes the header defines
+    assert lib.coord_host_path(None) == -1
+    from plumed2_gb300.action import Coordination
+    assert Coordination.HOST_PATHS == {-1: None, 0: "staged", 1: "direct", 2: "chunked"}
+    hdr = open(os.path.join(ROOT, "include", "coordgpu.h")).read()
+    for name, code in (("STAGED", 0), ("DIRECT", 1), ("CHUNKED", 2)):
+        assert re.search(r"#define COORD_HOST_PATH_%s %d\b" % (name, code), hdr)
+
+
 def test_status_strings(lib):
     assert lib.coord_status_string(0) == b"ok"
     assert lib.coord_status_string(2) == b"CUDA error"

@@ -138,9 +138,15 @@ def test_pinned_batch_skin_follows_every_walker():
     sd = torch.zeros(F, dtype=torch.float64, device=dev)
     dd = torch.zeros(F, n, 3, dtype=torch.float64, device=dev)
     vd = torch.zeros(F, 9, dtype=torch.float64, device=dev)
+    from plumed2_gb300 import _lib
+    pageable, tables = _lib.host_memory_access(0)
+    direct = bool(pageable and tables) and os.environ.get("COORD_HOST_STAGED") != "1"
     for step in range(21):
         pos[:] = traj[step]
         ch.forward_host_batch(F, addr(pos), addr(boxes), step, 0, addr(s), addr(d), addr(v))
+        # the path the call reports: copy-engine chunks between rebuilds, the
+        # kernels' direct access on a rebuild step (or staging without access)
+        assert ch.host_path() == (("direct" if step % 10 == 0 else "chunked") if direct else "staged"), step
         tp = torch.tensor(traj[step], dtype=torch.float64, device=dev)
         cd.forward_device(tp.data_ptr(), boxes, F, sd.data_ptr(), dd.data_ptr(), vd.data_ptr(), step=step)
         torch.cuda.synchronize()
