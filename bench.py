@@ -101,6 +101,78 @@ def host_path_note(counts):
                      for k, v in sorted(counts.items(), key=lambda kv: -kv[1]))
 
 
+def measure_e2e(make_ctx, hp, hs, hd, hv, box, W, n, steps, addr):
+    """The end-to-end figures through the host-array C ABI: the batched call
+    (coord_forward_batch) over page-locked frames hp[T][W][n][3] with results
+    in hs, hd, hv, and the plugin's call (coord_forward) per walker on
+    pageable arrays.  Returns (batched value, its windows, its host paths,
+    per-walker value, its windows, its host paths); values in pair-evals/s."""
+    # all walkers in one call, page-locked host arrays
+    T = hp.shape[0]
+    cb = make_ctx()
+    hb = np.ascontiguousarray(np.stack([box.reshape(9)] * W))
+    A = (addr(hb), addr(hs), addr(hd), addr(hv))
+    # steps 0..10 untimed (the context's first calls tune its passes), then the timed steps 11..
+    for k in range(0, 11):
+        cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
+    # three windows of `steps` steps (11.., then the next two), each ending on a rebuild step; the
+    # median window is reported, every window listed, and how each timed call moved the arrays counted
+    e2e_windows, batch_paths, k0 = [], {}, 11
+    for _ in range(E2E_WINDOWS):
+        n_first = sum(cb.nl_size(w) for w in range(W))  # the lists of the window's first steps
+        te_b = 0.0
+        for k in range(k0, k0 + steps):
+            t0 = time.perf_counter()
+            cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
+            te_b += time.perf_counter() - t0
+            batch_paths[cb.host_path()] = batch_paths.get(cb.host_path(), 0) + 1
+        e2e_windows.append(e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), steps) / te_b)
+        k0 += steps
+    assert np.all(np.isfinite(hs)) and np.all(hs > 0)
+    e2e_v = float(np.median(e2e_windows))
+    cb.close()
+    ctxs = [make_ctx() for _ in range(W)]
+    # one pageable position array per walker, which the MD engine rewrites in place every step (outside
+    # the timed calls, as the integrator's update is not PLUMED's); force and virial arrays reused from
+    # step to step.  The call is the C ABI's coord_forward with the arrays' addresses, as the PLUMED
+    # plugin makes it.  (A fresh array per step, never an MD engine's pattern, runs about 1.5x slower on
+    # the direct host path: each first GPU touch of host pages costs address translations.)
+    host_pos = [np.array(hp[0, w]) for w in range(W)]
+    outs = [(np.zeros((n, 3)), np.zeros(9), np.zeros(1)) for _ in range(W)]
+    hbox = np.ascontiguousarray(box.reshape(9))
+    ptrs = [(addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
+    pptr = [addr(host_pos[w]) for w in range(W)]
+    for w in range(W):
+        ctxs[w].forward_host(pptr[w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+    # one stride untimed (each context tunes its passes on its first calls), then the timed steps
+    for k in range(1, 11):
+        for w in range(W):
+            np.copyto(host_pos[w], hp[k % T, w])
+            ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+    walker_windows, walker_paths, k0 = [], {}, 11
+    for _ in range(E2E_WINDOWS):
+        n_first = sum(ctxs[w].nl_size() for w in range(W))
+        te = 0.0
+        for k in range(k0, k0 + steps):
+            for w in range(W):
+                np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
+            t0 = time.perf_counter()
+            for w in range(W):
+                ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
+            te += time.perf_counter() - t0
+            for w in range(W):
+                walker_paths[ctxs[w].host_path()] = walker_paths.get(ctxs[w].host_path(), 0) + 1
+        walker_windows.append(e2e_pairs(n_first, sum(ctxs[w].nl_size() for w in range(W)),
+                                        steps) / te)
+        k0 += steps
+    # the results landed in the caller's arrays
+    assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
+    e2e_walker = float(np.median(walker_windows))
+    for x in ctxs:
+        x.close()
+    return e2e_v, e2e_windows, batch_paths, e2e_walker, walker_windows, walker_paths
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -821,74 +893,15 @@ def run_ours(args):
         e2e_walker = None
         if args.e2e_steps > 0:
             from plumed2_gb300._lib import addr
-            # all walkers in one call, pinned host arrays
-            cb = Coordination(line, precision="mixed", device=local)
             pin = lambda *shape: torch.empty(*shape, dtype=torch.float64, pin_memory=True).numpy()
             # the trajectory's frames in page-locked host memory, one per step of the stride
             hp, hs, hd, hv = pin(T, W, n, 3), pin(W), pin(W, n, 3), pin(W, 9)
             hp[:] = traj.cpu().numpy()
-            hb = np.ascontiguousarray(np.stack([box.reshape(9)] * W))
-            A = (addr(hb), addr(hs), addr(hd), addr(hv))
-            # steps 0..10 untimed (the context's first calls tune its passes), then the timed steps 11..
-            for k in range(0, 11):
-                cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
-            # three windows of e2e_steps steps (11.., then the next two), each ending on a rebuild step; the
-            # median window is reported, every window listed, and how each timed call moved the arrays counted
-            e2e_windows, batch_paths, k0 = [], {}, 11
-            for _ in range(E2E_WINDOWS):
-                n_first = sum(cb.nl_size(w) for w in range(W))  # the lists of the window's first steps
-                te_b = 0.0
-                for k in range(k0, k0 + args.e2e_steps):
-                    t0 = time.perf_counter()
-                    cb.forward_host_batch(W, addr(hp[k % T]), A[0], k, 0, A[1], A[2], A[3])
-                    te_b += time.perf_counter() - t0
-                    batch_paths[cb.host_path()] = batch_paths.get(cb.host_path(), 0) + 1
-                e2e_windows.append(e2e_pairs(n_first, sum(cb.nl_size(w) for w in range(W)), args.e2e_steps) / te_b)
-                k0 += args.e2e_steps
-            assert np.all(np.isfinite(hs)) and np.all(hs > 0)
-            e2e_v = float(np.median(e2e_windows))
-            cb.close()
-            ctxs = [Coordination(line, precision="mixed", device=local) for _ in range(W)]
-            # one pageable position array per walker, which the MD engine rewrites in place every step (outside
-            # the timed calls, as the integrator's update is not PLUMED's); force and virial arrays reused from
-            # step to step.  The call is the C ABI's coord_forward with the arrays' addresses, as the PLUMED
-            # plugin makes it.  (A fresh array per step, never an MD engine's pattern, runs about 1.5x slower on
-            # the direct host path: each first GPU touch of host pages costs address translations.)
-            host_pos = [np.array(hp[0, w]) for w in range(W)]
-            outs = [(np.zeros((n, 3)), np.zeros(9), np.zeros(1)) for _ in range(W)]
-            hbox = np.ascontiguousarray(box.reshape(9))
-            ptrs = [(addr(outs[w][2]), addr(outs[w][0]), addr(outs[w][1])) for w in range(W)]
-            pptr = [addr(host_pos[w]) for w in range(W)]
-            for w in range(W):
-                ctxs[w].forward_host(pptr[w], addr(hbox), 0, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-            # one stride untimed (each context tunes its passes on its first calls), then the timed steps
-            for k in range(1, 11):
-                for w in range(W):
-                    np.copyto(host_pos[w], hp[k % T, w])
-                    ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-            walker_windows, walker_paths, k0 = [], {}, 11
-            for _ in range(E2E_WINDOWS):
-                n_first = sum(ctxs[w].nl_size() for w in range(W))
-                te = 0.0
-                for k in range(k0, k0 + args.e2e_steps):
-                    for w in range(W):
-                        np.copyto(host_pos[w], hp[k % T, w])  # the MD engine's position update
-                    t0 = time.perf_counter()
-                    for w in range(W):
-                        ctxs[w].forward_host(pptr[w], addr(hbox), k, 0, ptrs[w][0], ptrs[w][1], ptrs[w][2])
-                    te += time.perf_counter() - t0
-                    for w in range(W):
-                        walker_paths[ctxs[w].host_path()] = walker_paths.get(ctxs[w].host_path(), 0) + 1
-                walker_windows.append(e2e_pairs(n_first, sum(ctxs[w].nl_size() for w in range(W)),
-                                                args.e2e_steps) / te)
-                k0 += args.e2e_steps
-            # the results landed in the caller's arrays
-            assert all(np.isfinite(outs[w][2][0]) and outs[w][2][0] > 0 for w in range(W))
-            e2e_walker = float(np.median(walker_windows))
+            e2e_v, e2e_windows, batch_paths, e2e_walker, walker_windows, walker_paths = measure_e2e(
+                lambda: Coordination(line, precision="mixed", device=local), hp, hs, hd, hv, box, W, n,
+                args.e2e_steps, addr)
             h2d = W * n * 3 * 8
             d2h = W * (n * 3 * 8 + 10 * 8)
-            for x in ctxs:
-                x.close()
         cpu = None
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(frames, box, budget_s=8.0, gpu_check=gpu_check)
